@@ -1,0 +1,27 @@
+"""GB300-native force-and-integrate engine for OpenCafeMol's coarse-grained
+protein force field (harmonic bonds, Go 10-12 contacts, flexible-local
+angles and dihedrals, excluded volume, Debye-Hueckel, HPS Lennard-Jones)
+with a Langevin integrator, behind the C ABI in include/ocm.h.
+"""
+from ._lib import LIB_PATH, OCMError, device_count, lib
+from .engine import ALL_GROUPS, Batch, Context
+from .forcefield import (AMINO_ACIDS, DebyeHuckelForceFieldGenerator,
+                         ExcludedVolumeForceFieldGenerator,
+                         FlexibleLocalAngleForceFieldGenerator,
+                         FlexibleLocalDihedralForceFieldGenerator, GoContactForceFieldGenerator,
+                         HarmonicBondForceFieldGenerator, LangevinIntegrator,
+                         LangevinIntegratorGenerator, LennardJonesAttractiveForceFieldGenerator,
+                         LennardJonesRepulsiveForceFieldGenerator, System, SystemGenerator,
+                         Topology, cutoff_ratio_for, fla_second_derivative_table,
+                         fla_spline_table, fld_fourier_table, fld_table_keys)
+
+__all__ = [
+    "LIB_PATH", "OCMError", "device_count", "lib", "ALL_GROUPS", "Batch", "Context",
+    "AMINO_ACIDS", "DebyeHuckelForceFieldGenerator", "ExcludedVolumeForceFieldGenerator",
+    "FlexibleLocalAngleForceFieldGenerator", "FlexibleLocalDihedralForceFieldGenerator",
+    "GoContactForceFieldGenerator", "HarmonicBondForceFieldGenerator", "LangevinIntegrator",
+    "LangevinIntegratorGenerator", "LennardJonesAttractiveForceFieldGenerator",
+    "LennardJonesRepulsiveForceFieldGenerator", "System", "SystemGenerator", "Topology",
+    "cutoff_ratio_for", "fla_second_derivative_table", "fla_spline_table", "fld_fourier_table",
+    "fld_table_keys",
+]

@@ -1,0 +1,942 @@
+// batch_engine.cu - persistent shared-memory kernel for many independent
+// systems (the batched ensemble and the serving loop).
+//
+// One CTA per SM (or more, by occupancy) pulls systems from a work queue
+// ordered by decreasing cost.  A claimed system is loaded into shared
+// memory (FP64 master positions, FP32 positions and parameters, velocities,
+// 64-bit fixed-point force accumulators) and advanced for the whole chunk
+// without touching global memory except for L2-resident static parameters:
+//   tiles:    every 32x32 cluster pair (I <= J) whose bounding boxes lie
+//             within the largest cutoff, recomputed every step - no
+//             neighbour list and no skin;
+//   bonded:   bonds, Go contacts, FLA, FLD;
+//   update:   Langevin step per bead, fused with zeroing the accumulators
+//             and recomputing each cluster's bounding box.
+// Two __syncthreads per step.  Results depend only on (system, seed, step):
+// a system gives the same trajectory alone or in any mix.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "batch_engine.hpp"
+#include "device_math.cuh"
+
+namespace ocm {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kMaxClusters = 64;  // 2048 beads per system
+
+struct BatchArgs {
+    BatchSys* sys;
+    const int32_t* order;
+    int n_order;
+    int* head;
+    double *x, *y, *z;
+    float *vx, *vy, *vz;
+    const unsigned char* blob;
+    int k;
+    int nmax;
+    double* energy;              // [slot][kNumSlots]
+    unsigned long long* forces;  // eval output [3][nmax]
+    uint32_t slots_enabled;
+};
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void sadd(unsigned long long* F, int nmax, int b, float3 f) {
+    atomicAdd(&F[b], to_fixed(f.x));
+    atomicAdd(&F[nmax + b], to_fixed(f.y));
+    atomicAdd(&F[2 * nmax + b], to_fixed(f.z));
+}
+
+__device__ __forceinline__ float3 dsep(const double* sxd, int nmax, int i, int j) {
+    return make_float3((float)(sxd[j] - sxd[i]), (float)(sxd[nmax + j] - sxd[nmax + i]),
+                       (float)(sxd[2 * nmax + j] - sxd[2 * nmax + i]));
+}
+
+template <int TERMS, bool LABELS, bool ENERGY>
+__device__ __forceinline__ void batch_tile(int I, int J, int mslot, const uint32_t* __restrict__ masks,
+                                           const float4* sx, const float4* sp0, const float4* sp1,
+                                           const uint32_t* slab, unsigned long long* sF, int nmax,
+                                           const PairConsts& pc, uint32_t excl_all, int lane,
+                                           float* eacc) {
+    const int ki = I * 32 + lane, kj = J * 32 + lane;
+    const float4 xi = sx[ki];
+    const float4 p0i = sp0[ki];
+    const float4 p1i = (TERMS & kTermLJA) ? sp1[ki] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const uint32_t labi = LABELS ? slab[ki] : 0u;
+    float4 xj = sx[kj];
+    float4 p0j = sp0[kj];
+    float4 p1j = (TERMS & kTermLJA) ? sp1[kj] : make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t labj = LABELS ? slab[kj] : 0u;
+    uint32_t mw[4] = {0u, 0u, 0u, 0u};
+    if (mslot >= 0) {
+#pragma unroll
+        for (int term = 0; term < 4; ++term)
+            if (TERMS & (1 << term)) mw[term] = masks[(size_t)mslot * 128 + term * 32 + lane];
+    }
+    const bool diag = I == J;
+    float3 fi = make_float3(0.f, 0.f, 0.f), fj = make_float3(0.f, 0.f, 0.f);
+    PairEnergy e;
+    e.zero();
+    const float3 nobox = make_float3(0.f, 0.f, 0.f);
+    for (int r = 0; r < 32; ++r) {
+        const bool do_pair = !diag || (r > 0 && (r < 16 || (r == 16 && lane < 16)));
+        if (do_pair) {
+            const float3 d = separation<false>(xi, xj, nobox, nobox);
+            const float r2 = norm2(d);
+            if (r2 < pc.list_rc2) {
+                uint32_t ex = excl_all;
+#pragma unroll
+                for (int term = 0; term < 4; ++term)
+                    if (TERMS & (1 << term)) ex |= ((mw[term] >> r) & 1u) << term;
+                if (LABELS) {
+#pragma unroll
+                    for (int term = 0; term < 4; ++term)
+                        if ((TERMS & (1 << term)) && (pc.uses_labels & (1 << term)) &&
+                            !labels_allow(labi, labj, term, pc.allow[term]))
+                            ex |= 1u << term;
+                }
+                const float s = pair_scalar<TERMS, ENERGY>(r2, p0i, p0j, p1i, p1j, ex, pc, e);
+                fi.x -= s * d.x;
+                fi.y -= s * d.y;
+                fi.z -= s * d.z;
+                fj.x += s * d.x;
+                fj.y += s * d.y;
+                fj.z += s * d.z;
+            }
+        }
+        const int src = (lane + 1) & 31;
+        xj.x = __shfl_sync(kFull, xj.x, src);
+        xj.y = __shfl_sync(kFull, xj.y, src);
+        xj.z = __shfl_sync(kFull, xj.z, src);
+        if (TERMS & kTermEXV) p0j.x = __shfl_sync(kFull, p0j.x, src);
+        if (TERMS & kTermDH) p0j.y = __shfl_sync(kFull, p0j.y, src);
+        if (TERMS & kTermLJR) {
+            p0j.z = __shfl_sync(kFull, p0j.z, src);
+            p0j.w = __shfl_sync(kFull, p0j.w, src);
+        }
+        if (TERMS & kTermLJA) {
+            p1j.x = __shfl_sync(kFull, p1j.x, src);
+            p1j.y = __shfl_sync(kFull, p1j.y, src);
+        }
+        if (LABELS) labj = __shfl_sync(kFull, labj, src);
+        fj.x = __shfl_sync(kFull, fj.x, src);
+        fj.y = __shfl_sync(kFull, fj.y, src);
+        fj.z = __shfl_sync(kFull, fj.z, src);
+    }
+    sadd(sF, nmax, ki, fi);
+    sadd(sF, nmax, kj, fj);
+    if (ENERGY) {
+        eacc[kSlotEXV] += e.exv;
+        eacc[kSlotDH] += e.dh;
+        eacc[kSlotLJR] += e.ljr;
+        eacc[kSlotLJA] += e.lja;
+    }
+}
+
+// Bounding box of cluster I from the FP32 positions (warp-wide).
+__device__ __forceinline__ void cluster_bbox(int I, int n, const float4* sx, float4* bc,
+                                             float4* bh, int lane) {
+    const int b = I * 32 + lane;
+    const float4 base = sx[I * 32];
+    float3 d = make_float3(0.f, 0.f, 0.f);
+    if (b < n) {
+        const float4 p = sx[b];
+        d = make_float3(p.x - base.x, p.y - base.y, p.z - base.z);
+    }
+    float lx = d.x, ly = d.y, lz = d.z, hx = d.x, hy = d.y, hz = d.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lx = fminf(lx, __shfl_xor_sync(kFull, lx, o));
+        ly = fminf(ly, __shfl_xor_sync(kFull, ly, o));
+        lz = fminf(lz, __shfl_xor_sync(kFull, lz, o));
+        hx = fmaxf(hx, __shfl_xor_sync(kFull, hx, o));
+        hy = fmaxf(hy, __shfl_xor_sync(kFull, hy, o));
+        hz = fmaxf(hz, __shfl_xor_sync(kFull, hz, o));
+    }
+    if (lane == 0) {
+        bc[I] = make_float4(base.x + 0.5f * (lx + hx), base.y + 0.5f * (ly + hy),
+                            base.z + 0.5f * (lz + hz), 0.f);
+        bh[I] = make_float4(0.5f * (hx - lx), 0.5f * (hy - ly), 0.5f * (hz - lz), 0.f);
+    }
+}
+
+__device__ __forceinline__ bool bbox_close(float4 ci, float4 hi, float4 cj, float4 hj, float cut2) {
+    const float gx = fmaxf(0.f, fabsf(cj.x - ci.x) - hi.x - hj.x);
+    const float gy = fmaxf(0.f, fabsf(cj.y - ci.y) - hi.y - hj.y);
+    const float gz = fmaxf(0.f, fabsf(cj.z - ci.z) - hi.z - hj.z);
+    return gx * gx + gy * gy + gz * gz < cut2;
+}
+
+template <int THREADS, int TERMS, bool LABELS, bool ENERGY, bool INTEGRATE>
+__global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
+    constexpr int NW = THREADS / 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nmax = a.nmax;
+    double* sxd = reinterpret_cast<double*>(smem);
+    unsigned long long* sF = reinterpret_cast<unsigned long long*>(smem + 24 * (size_t)nmax);
+    float4* sx = reinterpret_cast<float4*>(smem + 48 * (size_t)nmax);
+    float4* sp0 = reinterpret_cast<float4*>(smem + 64 * (size_t)nmax);
+    float* sv = reinterpret_cast<float*>(smem + 80 * (size_t)nmax);
+    float* sim = reinterpret_cast<float*>(smem + 92 * (size_t)nmax);
+    size_t off = 96 * (size_t)nmax;
+    float4* sp1 = nullptr;
+    uint32_t* slab = nullptr;
+    if ((TERMS & kTermLJA) || LABELS) {
+        sp1 = reinterpret_cast<float4*>(smem + off);
+        slab = reinterpret_cast<uint32_t*>(smem + off + 16 * (size_t)nmax);
+        off += 20 * (size_t)nmax;
+    }
+    float4* bc = reinterpret_cast<float4*>(smem + off);
+    float4* bh = bc + kMaxClusters;
+    __shared__ int s_claim;
+    __shared__ double s_energy[kNumSlots];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float nan = __int_as_float(0x7fc00000);
+
+    while (true) {
+        if (tid == 0) s_claim = atomicAdd(a.head, 1);
+        if (ENERGY && tid < kNumSlots) s_energy[tid] = 0.0;
+        __syncthreads();
+        const int q = s_claim;
+        if (q >= a.n_order) break;
+        const int slot = a.order[q];
+        const BatchSys& R = a.sys[slot];
+        const int n = R.n, nt = R.nt, npad = nt * 32;
+        const PairConsts pc = R.pc;
+        const LangevinConsts lc = R.lc;
+        const long long boff = R.bead_off;
+        const unsigned char* blob = a.blob + R.blob_off;
+        const float4* gp0 = reinterpret_cast<const float4*>(blob + R.off_p0);
+        const float4* gp1 = reinterpret_cast<const float4*>(blob + R.off_p1);
+        const uint32_t* glab = reinterpret_cast<const uint32_t*>(blob + R.off_lab);
+        const float* ginvm = reinterpret_cast<const float*>(blob + R.off_invm);
+        const BondTerm* bonds = reinterpret_cast<const BondTerm*>(blob + R.off_bonds);
+        const AngleTerm* angles = reinterpret_cast<const AngleTerm*>(blob + R.off_angles);
+        const DihedralTerm* dih = reinterpret_cast<const DihedralTerm*>(blob + R.off_dih);
+        const FlaTable* fla = reinterpret_cast<const FlaTable*>(blob + R.off_fla);
+        const FldTable* fld = reinterpret_cast<const FldTable*>(blob + R.off_fld);
+        const int32_t* tmask = reinterpret_cast<const int32_t*>(blob + R.off_tmask);
+        const uint32_t* masks = reinterpret_cast<const uint32_t*>(blob + R.off_masks);
+        const unsigned long long step0 = R.steps_done;
+        int K = 1;
+        if (INTEGRATE) {
+            const unsigned long long left = R.steps_target > step0 ? R.steps_target - step0 : 0ull;
+            K = (int)min((unsigned long long)a.k, left);
+        }
+        const uint32_t slots_en = INTEGRATE ? 0xffffffffu : a.slots_enabled;
+        uint32_t excl_all = 0u;
+        if (!(slots_en & (1u << kSlotEXV))) excl_all |= kTermEXV;
+        if (!(slots_en & (1u << kSlotDH))) excl_all |= kTermDH;
+        if (!(slots_en & (1u << kSlotLJR))) excl_all |= kTermLJR;
+        if (!(slots_en & (1u << kSlotLJA))) excl_all |= kTermLJA;
+
+        // ---- load ----
+        for (int b = tid; b < npad; b += THREADS) {
+            sF[b] = 0ull;
+            sF[nmax + b] = 0ull;
+            sF[2 * nmax + b] = 0ull;
+            if (b < n) {
+                const double px = a.x[boff + b], py = a.y[boff + b], pz = a.z[boff + b];
+                sxd[b] = px;
+                sxd[nmax + b] = py;
+                sxd[2 * nmax + b] = pz;
+                sx[b] = make_float4(__double2float_rn(px), __double2float_rn(py),
+                                    __double2float_rn(pz), 0.f);
+                sp0[b] = gp0[b];
+                sv[b] = a.vx[boff + b];
+                sv[nmax + b] = a.vy[boff + b];
+                sv[2 * nmax + b] = a.vz[boff + b];
+                sim[b] = ginvm[b];
+                if ((TERMS & kTermLJA) || LABELS) {
+                    sp1[b] = gp1[b];
+                    slab[b] = glab[b];
+                }
+            } else {
+                sx[b] = make_float4(nan, nan, nan, 0.f);
+                sp0[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+                sim[b] = 0.f;
+                if ((TERMS & kTermLJA) || LABELS) {
+                    sp1[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    slab[b] = 0xffffffffu;
+                }
+            }
+        }
+        __syncthreads();
+        for (int I = warp; I < nt; I += NW) cluster_bbox(I, n, sx, bc, bh, lane);
+        __syncthreads();
+
+        const float cut = sqrtf(pc.list_rc2) * 1.0001f + 1e-4f;
+        const float cut2 = cut * cut;
+        float eacc[kNumSlots];
+#pragma unroll
+        for (int k = 0; k < kNumSlots; ++k) eacc[k] = 0.f;
+
+        for (int st = 0; st < K; ++st) {
+            // ---- pair tiles (bounding-box culled) ----
+            if ((pc.terms & ~excl_all) != 0) {
+                for (int t = warp; t < R.n_tiles; t += NW) {
+                    int J = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+                    while ((J + 1) * (J + 2) / 2 <= t) ++J;
+                    while (J * (J + 1) / 2 > t) --J;
+                    const int I = t - J * (J + 1) / 2;
+                    if (!bbox_close(bc[I], bh[I], bc[J], bh[J], cut2)) continue;
+                    batch_tile<TERMS, LABELS, ENERGY>(I, J, tmask[t], masks, sx, sp0, sp1, slab, sF,
+                                                      nmax, pc, excl_all, lane, eacc);
+                }
+            }
+            // ---- bonded ----
+            for (int b = tid; b < R.n_bonds; b += THREADS) {
+                const BondTerm bt = bonds[b];
+                const int sl = bt.kind == kBondHarmonic ? kSlotHB : kSlotGO;
+                if (!(slots_en & (1u << sl))) continue;
+                const float3 d = dsep(sxd, nmax, bt.i, bt.j);
+                float en;
+                const float s = bond_scalar(bt.kind, norm2(d), bt.p0, bt.p1, en);
+                sadd(sF, nmax, bt.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
+                sadd(sF, nmax, bt.j, make_float3(s * d.x, s * d.y, s * d.z));
+                if (ENERGY) eacc[sl] += en;
+            }
+            if (slots_en & (1u << kSlotFLA)) {
+                for (int b = tid; b < R.n_angles; b += THREADS) {
+                    const AngleTerm g = angles[b];
+                    const float3 u = dsep(sxd, nmax, g.j, g.i);
+                    const float3 v = dsep(sxd, nmax, g.j, g.k);
+                    float3 f1, f3;
+                    float en;
+                    fla_forces(u, v, g.kk, fla[g.table], f1, f3, en);
+                    sadd(sF, nmax, g.i, f1);
+                    sadd(sF, nmax, g.k, f3);
+                    sadd(sF, nmax, g.j, make_float3(-f1.x - f3.x, -f1.y - f3.y, -f1.z - f3.z));
+                    if (ENERGY) eacc[kSlotFLA] += en;
+                }
+            }
+            if (slots_en & (1u << kSlotFLD)) {
+                for (int b = tid; b < R.n_dih; b += THREADS) {
+                    const DihedralTerm qd = dih[b];
+                    const float3 F = dsep(sxd, nmax, qd.j, qd.i);
+                    const float3 G = dsep(sxd, nmax, qd.k, qd.j);
+                    const float3 H = dsep(sxd, nmax, qd.k, qd.l);
+                    float3 f1, f2, f3, f4;
+                    float en;
+                    fld_forces(F, G, H, qd.kk, fld[qd.table], f1, f2, f3, f4, en);
+                    sadd(sF, nmax, qd.i, f1);
+                    sadd(sF, nmax, qd.j, f2);
+                    sadd(sF, nmax, qd.k, f3);
+                    sadd(sF, nmax, qd.l, f4);
+                    if (ENERGY) eacc[kSlotFLD] += en;
+                }
+            }
+            __syncthreads();
+            if (!INTEGRATE) break;
+            // ---- Langevin update + bounding boxes ----
+            const unsigned long long step = step0 + (unsigned long long)st;
+            for (int I = warp; I < nt; I += NW) {
+                const int b = I * 32 + lane;
+                if (b < n) {
+                    const float fx = (float)((double)(long long)sF[b] * kFixedInv);
+                    const float fy = (float)((double)(long long)sF[nmax + b] * kFixedInv);
+                    const float fz = (float)((double)(long long)sF[2 * nmax + b] * kFixedInv);
+                    sF[b] = 0ull;
+                    sF[nmax + b] = 0ull;
+                    sF[2 * nmax + b] = 0ull;
+                    const float im = sim[b];
+                    if (im > 0.f) {
+                        const float3 g = gaussian3(lc.seed, lc.stream, (uint32_t)b, step, kPurposeLangevin);
+                        const float sq = sqrtf(im) * lc.noise;
+                        const float fs = lc.fscale * im;
+                        const float vx = lc.vscale * sv[b] + fs * fx + sq * g.x;
+                        const float vy = lc.vscale * sv[nmax + b] + fs * fy + sq * g.y;
+                        const float vz = lc.vscale * sv[2 * nmax + b] + fs * fz + sq * g.z;
+                        sv[b] = vx;
+                        sv[nmax + b] = vy;
+                        sv[2 * nmax + b] = vz;
+                        const double px = sxd[b] + (double)vx * (double)lc.dt;
+                        const double py = sxd[nmax + b] + (double)vy * (double)lc.dt;
+                        const double pz = sxd[2 * nmax + b] + (double)vz * (double)lc.dt;
+                        sxd[b] = px;
+                        sxd[nmax + b] = py;
+                        sxd[2 * nmax + b] = pz;
+                        sx[b] = make_float4(__double2float_rn(px), __double2float_rn(py),
+                                            __double2float_rn(pz), 0.f);
+                    }
+                }
+                __syncwarp();
+                cluster_bbox(I, n, sx, bc, bh, lane);
+            }
+            __syncthreads();
+        }
+
+        // ---- write back ----
+        if (INTEGRATE) {
+            for (int b = tid; b < n; b += THREADS) {
+                a.x[boff + b] = sxd[b];
+                a.y[boff + b] = sxd[nmax + b];
+                a.z[boff + b] = sxd[2 * nmax + b];
+                a.vx[boff + b] = sv[b];
+                a.vy[boff + b] = sv[nmax + b];
+                a.vz[boff + b] = sv[2 * nmax + b];
+            }
+            if (tid == 0) a.sys[slot].steps_done = step0 + (unsigned long long)K;
+        } else {
+            for (int b = tid; b < n; b += THREADS) {
+                a.forces[b] = sF[b];
+                a.forces[nmax + b] = sF[nmax + b];
+                a.forces[2 * nmax + b] = sF[2 * nmax + b];
+            }
+        }
+        if (ENERGY) {
+#pragma unroll
+            for (int k = 0; k < kNumSlots; ++k) {
+                const double v = warp_sum_d((double)eacc[k]);
+                if (lane == 0 && v != 0.0) atomicAdd(&s_energy[k], v);
+            }
+            __syncthreads();
+            if (tid < kNumSlots) a.energy[(size_t)slot * kNumSlots + tid] = s_energy[tid];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_batch_velocity_init(int n, long long off, const float* __restrict__ invm,
+                                      float kT, uint32_t seed, float* vx, float* vy, float* vz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float im = invm[i];
+    const float3 g = gaussian3(seed, 1u, (uint32_t)i, 0ull, kPurposeVelocityInit);
+    const float s = im > 0.f ? sqrtf(kT * im) : 0.f;
+    vx[off + i] = s * g.x;
+    vy[off + i] = s * g.y;
+    vz[off + i] = s * g.z;
+}
+
+template <typename Fn>
+void launch_persistent(Fn fn, int threads, const BatchArgs& a, int max_grid, size_t smem,
+                       cudaStream_t s, int num_sms) {
+    OCM_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    OCM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    if (per_sm < 1) throw Error(6, "[error] batched kernel does not fit on an SM");
+    const int grid = std::max(1, std::min(max_grid, num_sms * per_sm));
+    fn<<<grid, threads, smem, s>>>(a);
+    OCM_CK(cudaGetLastError());
+}
+
+template <int THREADS, int TERMS, bool LABELS>
+void launch_batch_t(const BatchArgs& a, int max_grid, size_t smem, cudaStream_t s, bool integrate,
+                    bool energy, int num_sms) {
+    if (integrate)
+        launch_persistent(k_batch<THREADS, TERMS, LABELS, false, true>, THREADS, a, max_grid, smem, s, num_sms);
+    else if (energy)
+        launch_persistent(k_batch<THREADS, TERMS, LABELS, true, false>, THREADS, a, max_grid, smem, s, num_sms);
+    else
+        launch_persistent(k_batch<THREADS, TERMS, LABELS, false, false>, THREADS, a, max_grid, smem, s, num_sms);
+}
+
+template <int TERMS, bool LABELS>
+void launch_batch_threads(int threads, const BatchArgs& a, int grid, size_t smem, cudaStream_t s,
+                          bool integrate, bool energy, int num_sms) {
+    switch (threads) {
+        case 256: launch_batch_t<256, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms); break;
+        case 512: launch_batch_t<512, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms); break;
+        default: launch_batch_t<1024, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms); break;
+    }
+}
+
+int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
+
+struct BlobLayout {
+    int64_t size = 0;
+    int off_p0, off_p1, off_lab, off_invm, off_bonds, off_angles, off_dih, off_fla, off_fld,
+        off_tmask, off_masks;
+    int n_tiles, n_masks;
+};
+
+BlobLayout blob_layout(const CompiledSystem& c, int n_masks) {
+    BlobLayout L{};
+    const int64_t n = c.n;
+    const int nt = (int)((n + 31) / 32);
+    L.n_tiles = nt * (nt + 1) / 2;
+    L.n_masks = n_masks;
+    int64_t o = 0;
+    auto take = [&](int64_t bytes) {
+        const int64_t at = o;
+        o = align_up(o + bytes, 16);
+        return (int)at;
+    };
+    L.off_p0 = take(16 * n);
+    L.off_p1 = take(16 * n);
+    L.off_lab = take(4 * n);
+    L.off_invm = take(4 * n);
+    L.off_bonds = take((int64_t)sizeof(BondTerm) * c.bonds.size());
+    L.off_angles = take((int64_t)sizeof(AngleTerm) * c.angles.size());
+    L.off_dih = take((int64_t)sizeof(DihedralTerm) * c.dihedrals.size());
+    L.off_fla = take((int64_t)sizeof(FlaTable) * c.fla.size());
+    L.off_fld = take((int64_t)sizeof(FldTable) * c.fld.size());
+    L.off_tmask = take(4 * (int64_t)L.n_tiles);
+    L.off_masks = take(4 * 128 * (int64_t)n_masks);
+    L.size = align_up(o, 256);
+    return L;
+}
+
+// Exclusion masks in chain order: tile index t = J(J+1)/2 + I (I <= J).
+void build_masks(const CompiledSystem& c, std::vector<int32_t>& tmask, std::vector<uint32_t>& masks) {
+    const int nt = (int)((c.n + 31) / 32);
+    tmask.assign(nt * (nt + 1) / 2, -1);
+    masks.clear();
+    for (int64_t i = 0; i < c.n; ++i) {
+        for (int32_t e = c.ex_start[i]; e < c.ex_start[i + 1]; ++e) {
+            const int64_t j = c.ex_j[e];
+            if (j <= i) continue;
+            const int I = (int)(i >> 5), J = (int)(j >> 5);
+            const int t = J * (J + 1) / 2 + I;
+            if (tmask[t] < 0) {
+                tmask[t] = (int32_t)(masks.size() / 128);
+                masks.resize(masks.size() + 128, 0u);
+            }
+            uint32_t* w = &masks[(size_t)tmask[t] * 128];
+            const int li = (int)(i & 31), lj = (int)(j & 31);
+            for (int term = 0; term < kNumPairTerms; ++term) {
+                if (!(c.ex_bits[e] & (1 << term))) continue;
+                w[term * 32 + li] |= 1u << ((lj - li) & 31);
+                if (I == J) w[term * 32 + lj] |= 1u << ((li - lj) & 31);
+            }
+        }
+    }
+}
+
+void check_batchable(const CompiledSystem& c, int nmax) {
+    if (c.n <= 0) throw Error(1, "[error] system has no particles");
+    if (c.n > nmax)
+        throw Error(3, "[error] system of " + std::to_string(c.n) +
+                           " beads exceeds the batch's per-system limit " + std::to_string(nmax));
+    if (c.periodic) throw Error(6, "[error] the batched path runs non-periodic systems");
+    for (const auto& b : c.bonds)
+        if (b.periodic) throw Error(6, "[error] the batched path runs non-periodic systems");
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+int64_t RangeAllocator::alloc(int64_t size, int64_t align) {
+    if (size <= 0) size = 1;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+        const int64_t off = it->first, sz = it->second;
+        const int64_t a = align_up(off, align);
+        if (a + size <= off + sz) {
+            free_.erase(it);
+            if (a > off) free_[off] = a - off;
+            if (a + size < off + sz) free_[a + size] = off + sz - (a + size);
+            return a;
+        }
+    }
+    return -1;
+}
+
+void RangeAllocator::release(int64_t off, int64_t size) {
+    if (size <= 0) size = 1;
+    auto it = free_.emplace(off, size).first;
+    auto next = std::next(it);
+    if (next != free_.end() && it->first + it->second == next->first) {
+        it->second += next->second;
+        free_.erase(next);
+    }
+    if (it != free_.begin()) {
+        auto prev = std::prev(it);
+        if (prev->first + prev->second == it->first) {
+            prev->second += it->second;
+            free_.erase(it);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+BatchEngine::BatchEngine(int device, int64_t max_systems, int64_t max_beads, int32_t nmax)
+    : device_(device), max_systems_(max_systems), max_beads_(max_beads) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        throw Error(2, "[error] no CUDA device is available");
+    if (device < 0 || device >= count) throw Error(1, "[error] invalid device index");
+    if (max_systems <= 0 || max_beads <= 0 || nmax <= 0) throw Error(1, "[error] invalid batch capacity");
+    if (nmax > 32 * kMaxClusters)
+        throw Error(6, "[error] at most " + std::to_string(32 * kMaxClusters) + " beads per system");
+    OCM_CK(cudaSetDevice(device));
+    nmax_ = (int)align_up(nmax, 32);
+    OCM_CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device));
+    int optin = 0;
+    OCM_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    if ((int64_t)smem_bytes(nmax_, false) > optin)
+        throw Error(6, "[error] per-system bead limit does not fit in shared memory");
+    OCM_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    OCM_CK(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
+    OCM_CK(cudaEventCreate(&ev0_));
+    OCM_CK(cudaEventCreate(&ev1_));
+    OCM_CK(cudaEventCreateWithFlags(&ev_copy_, cudaEventDisableTiming));
+    slots_.resize(max_systems);
+    sys_host_.resize(max_systems);
+    std::memset(sys_host_.data(), 0, sizeof(BatchSys) * max_systems);
+    beads_.reset(max_beads);
+    // Static blobs: per bead ~ 40 B of parameters + ~4 terms of 24 B, plus
+    // the cluster-pair mask tables.
+    const int64_t blob_cap = max_beads * 256 + max_systems * 8192;
+    blob_.reset(blob_cap);
+    x_.alloc(max_beads); y_.alloc(max_beads); z_.alloc(max_beads);
+    vx_.alloc(max_beads); vy_.alloc(max_beads); vz_.alloc(max_beads);
+    blob_dev_.alloc(blob_cap);
+    sys_.alloc(max_systems);
+    OCM_CK(cudaMemset(sys_.p, 0, sizeof(BatchSys) * max_systems));
+    order_.alloc(max_systems);
+    head_.alloc(1);
+    energy_.alloc(max_systems * kNumSlots);
+    forces_.alloc(3 * nmax_);
+}
+
+BatchEngine::~BatchEngine() {
+    cudaSetDevice(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (copy_stream_) cudaStreamSynchronize(copy_stream_);
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
+    if (ev_copy_) cudaEventDestroy(ev_copy_);
+    if (stream_) cudaStreamDestroy(stream_);
+    if (copy_stream_) cudaStreamDestroy(copy_stream_);
+}
+
+size_t BatchEngine::smem_bytes(int nmax, bool general) const {
+    return (size_t)nmax * (general ? 116 : 96) + 2 * kMaxClusters * sizeof(float4);
+}
+
+int64_t BatchEngine::footprint(const SystemDesc& d) {
+    CompiledSystem c = compile_system(d);
+    std::vector<int32_t> tm;
+    std::vector<uint32_t> mk;
+    build_masks(c, tm, mk);
+    const BlobLayout L = blob_layout(c, (int)(mk.size() / 128));
+    return L.size + c.n * (3 * 8 + 3 * 4) + (int64_t)sizeof(BatchSys);
+}
+
+void BatchEngine::set_threads(int threads) {
+    if (threads != 256 && threads != 512 && threads != 1024)
+        throw Error(1, "[error] threads per CTA must be 256, 512 or 1024");
+    threads_ = threads;
+}
+
+int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double* vel, double T,
+                           double friction, double dt, int32_t seed, int64_t n_steps) {
+    OCM_CK(cudaSetDevice(device_));
+    if (n_steps < 0) throw Error(1, "[error] negative step count");
+    if (!(dt > 0) || !(friction >= 0) || !(T >= 0)) throw Error(1, "[error] invalid integrator parameters");
+    CompiledSystem c = compile_system(d);
+    check_batchable(c, nmax_);
+    const int64_t n = c.n;
+    for (int64_t i = 0; i < 3 * n; ++i)
+        if (!std::isfinite(pos[i])) throw Error(7, "[error] non-finite position");
+    int64_t slot = -1;
+    for (int64_t s = 0; s < max_systems_; ++s)
+        if (!slots_[s].used) {
+            slot = s;
+            break;
+        }
+    if (slot < 0) throw Error(3, "[error] no free slot in the batch");
+    std::vector<int32_t> tmask;
+    std::vector<uint32_t> masks;
+    build_masks(c, tmask, masks);
+    const BlobLayout L = blob_layout(c, (int)(masks.size() / 128));
+    const int64_t boff = beads_.alloc(n, 1);
+    if (boff < 0) throw Error(3, "[error] batch bead capacity exhausted");
+    const int64_t blob_off = blob_.alloc(L.size, 256);
+    if (blob_off < 0) {
+        beads_.release(boff, n);
+        throw Error(3, "[error] batch parameter memory exhausted");
+    }
+    // host blob
+    std::vector<unsigned char> blob(L.size, 0);
+    auto put = [&](int off, const void* src, size_t bytes) {
+        if (bytes) std::memcpy(blob.data() + off, src, bytes);
+    };
+    put(L.off_p0, c.p0.data(), 16 * n);
+    put(L.off_p1, c.p1.data(), 16 * n);
+    put(L.off_lab, c.labels.data(), 4 * n);
+    put(L.off_invm, c.inv_mass.data(), 4 * n);
+    put(L.off_bonds, c.bonds.data(), sizeof(BondTerm) * c.bonds.size());
+    put(L.off_angles, c.angles.data(), sizeof(AngleTerm) * c.angles.size());
+    put(L.off_dih, c.dihedrals.data(), sizeof(DihedralTerm) * c.dihedrals.size());
+    put(L.off_fla, c.fla.data(), sizeof(FlaTable) * c.fla.size());
+    put(L.off_fld, c.fld.data(), sizeof(FldTable) * c.fld.size());
+    put(L.off_tmask, tmask.data(), 4 * tmask.size());
+    put(L.off_masks, masks.data(), 4 * masks.size());
+
+    BatchSys R{};
+    R.bead_off = boff;
+    R.blob_off = blob_off;
+    R.n = (int)n;
+    R.nt = (int)((n + 31) / 32);
+    R.n_tiles = L.n_tiles;
+    R.n_bonds = (int)c.bonds.size();
+    R.n_angles = (int)c.angles.size();
+    R.n_dih = (int)c.dihedrals.size();
+    R.n_masks = L.n_masks;
+    R.off_p0 = L.off_p0; R.off_p1 = L.off_p1; R.off_lab = L.off_lab; R.off_invm = L.off_invm;
+    R.off_bonds = L.off_bonds; R.off_angles = L.off_angles; R.off_dih = L.off_dih;
+    R.off_fla = L.off_fla; R.off_fld = L.off_fld; R.off_tmask = L.off_tmask; R.off_masks = L.off_masks;
+    R.active = 1;
+    R.pc = c.pc;
+    const double vscale = std::exp(-friction * dt);
+    const double fscale = friction == 0 ? dt : (1.0 - vscale) / friction;
+    const double kT = constant::boltz * T;
+    R.lc.vscale = (float)vscale;
+    R.lc.fscale = (float)fscale;
+    R.lc.noise = (float)std::sqrt(kT * (1.0 - vscale * vscale));
+    R.lc.dt = (float)dt;
+    R.lc.seed = (uint32_t)seed;
+    R.lc.stream = 0u;
+    R.steps_done = 0;
+    R.steps_target = (unsigned long long)n_steps;
+
+    std::vector<double> px(n), py(n), pz(n);
+    for (int64_t i = 0; i < n; ++i) {
+        px[i] = pos[3 * i];
+        py[i] = pos[3 * i + 1];
+        pz[i] = pos[3 * i + 2];
+    }
+    cudaStream_t s = copy_stream_;
+    OCM_CK(cudaMemcpyAsync(blob_dev_.p + blob_off, blob.data(), L.size, cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(x_.p + boff, px.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(y_.p + boff, py.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(z_.p + boff, pz.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (vel) {
+        std::vector<float> vx(n), vy(n), vz(n);
+        for (int64_t i = 0; i < n; ++i) {
+            vx[i] = (float)vel[3 * i];
+            vy[i] = (float)vel[3 * i + 1];
+            vz[i] = (float)vel[3 * i + 2];
+        }
+        OCM_CK(cudaMemcpyAsync(vx_.p + boff, vx.data(), n * sizeof(float), cudaMemcpyHostToDevice, s));
+        OCM_CK(cudaMemcpyAsync(vy_.p + boff, vy.data(), n * sizeof(float), cudaMemcpyHostToDevice, s));
+        OCM_CK(cudaMemcpyAsync(vz_.p + boff, vz.data(), n * sizeof(float), cudaMemcpyHostToDevice, s));
+    } else {
+        k_batch_velocity_init<<<(int)((n + 255) / 256), 256, 0, s>>>(
+            (int)n, boff, reinterpret_cast<const float*>(blob_dev_.p + blob_off + L.off_invm),
+            (float)kT, (uint32_t)seed, vx_.p, vy_.p, vz_.p);
+        OCM_CK(cudaGetLastError());
+    }
+    OCM_CK(cudaMemcpyAsync(sys_.p + slot, &R, sizeof(BatchSys), cudaMemcpyHostToDevice, s));
+    // pageable copies above are complete on return except the record, keep
+    // the host objects alive until then
+    OCM_CK(cudaStreamSynchronize(s));
+    OCM_CK(cudaEventRecord(ev_copy_, s));
+
+    Slot& S = slots_[slot];
+    S.used = true;
+    S.bead_off = boff;
+    S.n = n;
+    S.blob_off = blob_off;
+    S.blob_size = L.size;
+    S.steps_target = (uint64_t)n_steps;
+    S.steps_done = 0;
+    S.terms = c.pc.terms;
+    S.labels = c.pc.uses_labels != 0;
+    for (int k = 0; k < kNumSlots; ++k) S.slot_group[k] = c.slot_group[k];
+    const double nt = (double)R.nt;
+    S.cost = nt * (nt + 1) / 2 + 0.05 * (double)n;
+    sys_host_[slot] = R;
+    return slot;
+}
+
+void BatchEngine::launch(bool integrate, bool energy, int k, const std::vector<int32_t>& order,
+                         cudaStream_t s) {
+    bool general = false;
+    int terms = 0;
+    for (int32_t q : order) {
+        terms |= slots_[q].terms;
+        general = general || slots_[q].labels;
+    }
+    if (terms & ~(kTermEXV | kTermDH)) general = true;
+    const size_t smem = smem_bytes(nmax_, general);
+    int optin = 0;
+    OCM_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+    if ((int64_t)smem > optin)
+        throw Error(6, "[error] these systems need more shared memory than one SM offers; "
+                       "create the batch with a smaller per-system bead limit");
+    OCM_CK(cudaMemcpyAsync(order_.p, order.data(), order.size() * sizeof(int32_t),
+                           cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemsetAsync(head_.p, 0, sizeof(int32_t), s));
+    BatchArgs a{};
+    a.sys = sys_.p;
+    a.order = order_.p;
+    a.n_order = (int)order.size();
+    a.head = head_.p;
+    a.x = x_.p; a.y = y_.p; a.z = z_.p;
+    a.vx = vx_.p; a.vy = vy_.p; a.vz = vz_.p;
+    a.blob = blob_dev_.p;
+    a.k = k;
+    a.nmax = nmax_;
+    a.energy = energy_.p;
+    a.forces = forces_.p;
+    a.slots_enabled = 0xffffffffu;
+    const int grid = (int)order.size();
+    if (general)
+        launch_batch_threads<15, true>(threads_, a, grid, smem, s, integrate, energy, num_sms_);
+    else
+        launch_batch_threads<kTermEXV | kTermDH, false>(threads_, a, grid, smem, s, integrate, energy, num_sms_);
+}
+
+void BatchEngine::run(int32_t k, bool sync) {
+    OCM_CK(cudaSetDevice(device_));
+    if (k <= 0) throw Error(1, "[error] steps per launch must be positive");
+    std::vector<int32_t> order;
+    for (int64_t s = 0; s < max_systems_; ++s)
+        if (slots_[s].used && slots_[s].steps_done < slots_[s].steps_target) order.push_back((int32_t)s);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t a, int32_t b) { return slots_[a].cost > slots_[b].cost; });
+    OCM_CK(cudaStreamWaitEvent(stream_, ev_copy_, 0));
+    OCM_CK(cudaEventRecord(ev0_, stream_));
+    if (!order.empty()) launch(true, false, k, order, stream_);
+    OCM_CK(cudaEventRecord(ev1_, stream_));
+    ran_ = true;
+    for (int32_t q : order)
+        slots_[q].steps_done = std::min<uint64_t>(slots_[q].steps_target, slots_[q].steps_done + k);
+    if (sync) OCM_CK(cudaStreamSynchronize(stream_));
+}
+
+double BatchEngine::last_run_ms() {
+    OCM_CK(cudaSetDevice(device_));
+    if (!ran_) return 0.0;
+    OCM_CK(cudaEventSynchronize(ev1_));
+    float ms = 0.f;
+    OCM_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    return ms;
+}
+
+void BatchEngine::sync_steps() { OCM_CK(cudaStreamSynchronize(stream_)); }
+
+void BatchEngine::finished(int64_t* out, int64_t cap, int64_t* n_out) {
+    OCM_CK(cudaSetDevice(device_));
+    sync_steps();
+    int64_t c = 0;
+    for (int64_t s = 0; s < max_systems_; ++s) {
+        if (!slots_[s].used || slots_[s].steps_done < slots_[s].steps_target) continue;
+        if (out && c < cap) out[c] = s;
+        ++c;
+    }
+    *n_out = c;
+}
+
+void BatchEngine::get_positions(int64_t slot, double* xyz) {
+    OCM_CK(cudaSetDevice(device_));
+    if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
+    sync_steps();
+    const Slot& S = slots_[slot];
+    std::vector<double> a(S.n), b(S.n), c(S.n);
+    OCM_CK(cudaMemcpy(a.data(), x_.p + S.bead_off, S.n * sizeof(double), cudaMemcpyDeviceToHost));
+    OCM_CK(cudaMemcpy(b.data(), y_.p + S.bead_off, S.n * sizeof(double), cudaMemcpyDeviceToHost));
+    OCM_CK(cudaMemcpy(c.data(), z_.p + S.bead_off, S.n * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < S.n; ++i) {
+        xyz[3 * i] = a[i];
+        xyz[3 * i + 1] = b[i];
+        xyz[3 * i + 2] = c[i];
+    }
+}
+
+void BatchEngine::get_velocities(int64_t slot, double* v) {
+    OCM_CK(cudaSetDevice(device_));
+    if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
+    sync_steps();
+    const Slot& S = slots_[slot];
+    std::vector<float> a(S.n), b(S.n), c(S.n);
+    OCM_CK(cudaMemcpy(a.data(), vx_.p + S.bead_off, S.n * sizeof(float), cudaMemcpyDeviceToHost));
+    OCM_CK(cudaMemcpy(b.data(), vy_.p + S.bead_off, S.n * sizeof(float), cudaMemcpyDeviceToHost));
+    OCM_CK(cudaMemcpy(c.data(), vz_.p + S.bead_off, S.n * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < S.n; ++i) {
+        v[3 * i] = a[i];
+        v[3 * i + 1] = b[i];
+        v[3 * i + 2] = c[i];
+    }
+}
+
+int64_t BatchEngine::steps_done(int64_t slot) {
+    if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
+    sync_steps();
+    return (int64_t)slots_[slot].steps_done;
+}
+
+void BatchEngine::get_state(int64_t slot, uint32_t groups, double* forces, double* energies) {
+    OCM_CK(cudaSetDevice(device_));
+    if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
+    const Slot& S = slots_[slot];
+    uint32_t en = 0;
+    for (int k = 0; k < kNumSlots; ++k)
+        if (S.slot_group[k] >= 0 && ((groups >> S.slot_group[k]) & 1u)) en |= 1u << k;
+    std::vector<int32_t> order{(int32_t)slot};
+    OCM_CK(cudaStreamWaitEvent(stream_, ev_copy_, 0));
+    OCM_CK(cudaMemsetAsync(energy_.p + slot * kNumSlots, 0, kNumSlots * sizeof(double), stream_));
+    // The eval kernel reads slots_enabled from the args.
+    {
+        bool general = S.labels || (S.terms & ~(kTermEXV | kTermDH));
+        const size_t smem = smem_bytes(nmax_, general);
+        OCM_CK(cudaMemcpyAsync(order_.p, order.data(), sizeof(int32_t), cudaMemcpyHostToDevice, stream_));
+        OCM_CK(cudaMemsetAsync(head_.p, 0, sizeof(int32_t), stream_));
+        BatchArgs a{};
+        a.sys = sys_.p; a.order = order_.p; a.n_order = 1; a.head = head_.p;
+        a.x = x_.p; a.y = y_.p; a.z = z_.p; a.vx = vx_.p; a.vy = vy_.p; a.vz = vz_.p;
+        a.blob = blob_dev_.p; a.k = 0; a.nmax = nmax_; a.energy = energy_.p; a.forces = forces_.p;
+        a.slots_enabled = en;
+        if (general) launch_batch_threads<15, true>(threads_, a, 1, smem, stream_, false, true, num_sms_);
+        else launch_batch_threads<kTermEXV | kTermDH, false>(threads_, a, 1, smem, stream_, false, true, num_sms_);
+    }
+    std::vector<unsigned long long> f(3 * nmax_);
+    double e[kNumSlots];
+    OCM_CK(cudaMemcpyAsync(f.data(), forces_.p, 3 * nmax_ * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaMemcpyAsync(e, energy_.p + slot * kNumSlots, sizeof(e), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaStreamSynchronize(stream_));
+    if (forces)
+        for (int64_t i = 0; i < S.n; ++i)
+            for (int c = 0; c < 3; ++c)
+                forces[3 * i + c] = (double)(long long)f[(size_t)c * nmax_ + i] * kFixedInv;
+    if (energies) {
+        for (int g = 0; g < 32; ++g) energies[g] = 0.0;
+        for (int k = 0; k < kNumSlots; ++k)
+            if (S.slot_group[k] >= 0) energies[S.slot_group[k]] += e[k];
+    }
+}
+
+void BatchEngine::retire(int64_t slot) {
+    OCM_CK(cudaSetDevice(device_));
+    if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
+    sync_steps();
+    Slot& S = slots_[slot];
+    beads_.release(S.bead_off, S.n);
+    blob_.release(S.blob_off, S.blob_size);
+    S = Slot();
+    BatchSys R{};
+    sys_host_[slot] = R;
+    OCM_CK(cudaMemcpyAsync(sys_.p + slot, &sys_host_[slot], sizeof(BatchSys), cudaMemcpyHostToDevice, stream_));
+    OCM_CK(cudaStreamSynchronize(stream_));
+}
+
+void BatchEngine::active(int64_t* n_active, int64_t* beads) {
+    int64_t a = 0, b = 0;
+    for (const auto& s : slots_)
+        if (s.used) {
+            ++a;
+            b += s.n;
+        }
+    *n_active = a;
+    *beads = b;
+}
+
+}  // namespace ocm

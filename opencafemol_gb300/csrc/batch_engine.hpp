@@ -1,0 +1,104 @@
+// batch_engine.hpp - many independent systems advanced by one persistent
+// kernel per chunk of steps.  Each CTA claims a system from a work queue
+// (largest first), pulls its state into shared memory, runs the chunk
+// there (cluster-pair tiles with per-step bounding-box culling, bonded
+// terms, Langevin update) and writes the state back.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <vector>
+
+#include "engine.hpp"
+#include "host_system.hpp"
+
+namespace ocm {
+
+// Device record of one admitted system.
+struct BatchSys {
+    long long bead_off;    // offset into the bead arena
+    long long blob_off;    // byte offset of the static blob
+    int n, nt, n_tiles;    // beads, 32-bead clusters, cluster pairs
+    int n_bonds, n_angles, n_dih, n_masks;
+    int off_p0, off_p1, off_lab, off_invm;   // byte offsets inside the blob
+    int off_bonds, off_angles, off_dih, off_fla, off_fld, off_tmask, off_masks;
+    int active;
+    PairConsts pc;
+    LangevinConsts lc;
+    unsigned long long steps_done, steps_target;
+};
+
+// First-fit range allocator (units are arbitrary).
+class RangeAllocator {
+  public:
+    explicit RangeAllocator(int64_t cap = 0) { reset(cap); }
+    void reset(int64_t cap) {
+        cap_ = cap;
+        free_.clear();
+        if (cap > 0) free_[0] = cap;
+    }
+    int64_t alloc(int64_t size, int64_t align = 1);  // -1 when full
+    void release(int64_t off, int64_t size);
+    int64_t capacity() const { return cap_; }
+  private:
+    int64_t cap_ = 0;
+    std::map<int64_t, int64_t> free_;  // offset -> size
+};
+
+class BatchEngine {
+  public:
+    BatchEngine(int device, int64_t max_systems, int64_t max_beads, int32_t max_beads_per_system);
+    ~BatchEngine();
+    static int64_t footprint(const SystemDesc& d);
+    int64_t admit(const SystemDesc& d, const double* pos, const double* vel, double T,
+                  double friction, double dt, int32_t seed, int64_t n_steps);
+    void run(int32_t steps_per_launch, bool sync);
+    void finished(int64_t* slots, int64_t cap, int64_t* n_out);
+    void get_positions(int64_t slot, double* xyz);
+    void get_velocities(int64_t slot, double* v);
+    int64_t steps_done(int64_t slot);
+    void get_state(int64_t slot, uint32_t groups, double* forces, double* energies);
+    void retire(int64_t slot);
+    void active(int64_t* n_active, int64_t* beads);
+    double last_run_ms();
+    void set_threads(int threads);  // 256/512/1024 (autotuner)
+    int threads() const { return threads_; }
+
+  private:
+    struct Slot {
+        bool used = false;
+        int64_t bead_off = 0, n = 0;
+        int64_t blob_off = 0, blob_size = 0;
+        uint64_t steps_target = 0, steps_done = 0;
+        double cost = 0;
+        int terms = 0;
+        bool labels = false;
+        int slot_group[kNumSlots];
+    };
+    void sync_steps();
+    void launch(bool integrate, bool energy, int k, const std::vector<int32_t>& order,
+                cudaStream_t s);
+    size_t smem_bytes(int nmax, bool general) const;
+
+    int device_;
+    int64_t max_systems_, max_beads_;
+    int nmax_;
+    int threads_ = 1024;
+    int num_sms_ = 0;
+    cudaStream_t stream_ = nullptr, copy_stream_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, ev_copy_ = nullptr;
+    bool ran_ = false;
+    std::vector<Slot> slots_;
+    RangeAllocator beads_, blob_;
+    DevBuf<double> x_, y_, z_;
+    DevBuf<float> vx_, vy_, vz_;
+    DevBuf<unsigned char> blob_dev_;
+    DevBuf<BatchSys> sys_;
+    DevBuf<int32_t> order_, head_;
+    DevBuf<double> energy_;
+    DevBuf<unsigned long long> forces_;
+    std::vector<BatchSys> sys_host_;
+};
+
+}  // namespace ocm

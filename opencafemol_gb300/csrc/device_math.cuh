@@ -1,0 +1,283 @@
+// device_math.cuh - per-pair and per-tuple arithmetic of the OpenCafeMol
+// coarse-grained force field, shared by the plain (global-memory) and the
+// batched (shared-memory) engines.
+//
+// Every function evaluates in FP32.  Forces leave these functions as FP32
+// and are accumulated by the callers in 64-bit fixed point (2^32 units per
+// kJ/mol/nm), which makes the summation order-independent.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "engine_types.h"
+
+namespace ocm {
+
+// ---------------------------------------------------------------------------
+// Fixed-point force accumulation.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long to_fixed(float f) {
+    return (unsigned long long)__float2ll_rn(f * kFixedScaleF);
+}
+__device__ __forceinline__ void fixed_add(unsigned long long* p, float f) {
+    atomicAdd(p, to_fixed(f));
+}
+
+// ---------------------------------------------------------------------------
+// Canonical FP32 separation.  d = xj - xi with periodic minimum image; every
+// operation is individually rounded (no contraction) so the host-side
+// brute-force enumeration can reproduce r^2 bit for bit.
+// ---------------------------------------------------------------------------
+template <bool PERIODIC>
+__device__ __forceinline__ float3 separation(float4 xi, float4 xj, const float3& box,
+                                             const float3& inv_box) {
+    float dx = __fsub_rn(xj.x, xi.x);
+    float dy = __fsub_rn(xj.y, xi.y);
+    float dz = __fsub_rn(xj.z, xi.z);
+    if (PERIODIC) {
+        dx = __fmaf_rn(-box.x, rintf(__fmul_rn(dx, inv_box.x)), dx);
+        dy = __fmaf_rn(-box.y, rintf(__fmul_rn(dy, inv_box.y)), dy);
+        dz = __fmaf_rn(-box.z, rintf(__fmul_rn(dz, inv_box.z)), dz);
+    }
+    return make_float3(dx, dy, dz);
+}
+__device__ __forceinline__ float norm2(float3 d) {
+    return __fmaf_rn(d.z, d.z, __fmaf_rn(d.y, d.y, __fmul_rn(d.x, d.x)));
+}
+
+// Label test of an interaction-group matrix: 4-bit label per term, 15 = the
+// particle takes no part in the term.
+__device__ __forceinline__ bool labels_allow(uint32_t li, uint32_t lj, int term,
+                                             unsigned long long allow) {
+    const uint32_t a = (li >> (4 * term)) & 15u;
+    const uint32_t b = (lj >> (4 * term)) & 15u;
+    if (a == 15u || b == 15u) return false;
+    return (allow >> (a * 8 + b)) & 1ull;
+}
+
+struct PairEnergy {
+    float exv, dh, ljr, lja;
+    __device__ void zero() { exv = dh = ljr = lja = 0.f; }
+};
+
+// All pair terms for one (i, j).  Returns the scalar s with F_i = s * (x_i -
+// x_j) = -s * d.  excl is the per-term exclusion bits of this pair (bit t set
+// = term t excluded), already combined with the interaction-group test.
+//
+// Terms (reference expressions):
+//   EXV  eps (si+sj)^12 (r^-12 - rc^-12)                 ExcludedVolumeForceFieldGenerator.cpp:25-27
+//   DH   qi qj k (exp(-r/lD)/r - exp(-rc/lD)/rc)         DebyeHuckelForceFieldGenerator.cpp:54-57
+//   LJR  step(t-r) e (4(s^12-s^6)+1), t = 2^(1/6) s      LennardJonesRepulsiveForceFieldGenerator.cpp:35-43
+//   LJA  e (step(r-t) 4(s^12-s^6) - step(t-r)) * S(r)    LennardJonesAttractiveForceFieldGenerator.cpp:40-50,114-115
+template <int TERMS, bool ENERGY>
+__device__ __forceinline__ float pair_scalar(float r2, float4 pi, float4 pj, float4 qi, float4 qj,
+                                             uint32_t excl, const PairConsts& pc,
+                                             PairEnergy& e) {
+    const float rinv = rsqrtf(r2);
+    const float r2inv = rinv * rinv;
+    float s = 0.f;
+    if ((TERMS & kTermEXV) && !(excl & kTermEXV) && r2 < pc.exv_rc2) {
+        const float S = pi.x + pj.x;
+        const float S2 = S * S;
+        const float u = S2 * r2inv;
+        const float u3 = u * u * u;
+        const float u6 = u3 * u3;
+        s += 12.f * pc.exv_eps * u6 * r2inv;
+        if (ENERGY) {
+            const float w = S2 * pc.exv_inv_rc2;
+            const float w3 = w * w * w;
+            e.exv += pc.exv_eps * (u6 - w3 * w3);
+        }
+    }
+    if ((TERMS & kTermDH) && !(excl & kTermDH) && r2 < pc.dh_rc2) {
+        const float r = r2 * rinv;
+        const float ex = exp2f(-r * pc.dh_inv_lambda_log2e);
+        const float qq = pi.y * pj.y * pc.dh_k;
+        s += qq * ex * (pc.dh_inv_lambda + rinv) * r2inv;
+        if (ENERGY) e.dh += qq * (ex * rinv - pc.dh_corr);
+    }
+    if ((TERMS & kTermLJR) && !(excl & kTermLJR) && r2 < pc.ljr_rc2) {
+        const float sig = 0.5f * (pi.w + pj.w);
+        const float sig2 = sig * sig;
+        if (r2 <= sig2 * kTwoPow1_3) {
+            const float eps = 0.5f * (pi.z + pj.z);
+            const float s2 = sig2 * r2inv;
+            const float s6 = s2 * s2 * s2;
+            const float s12 = s6 * s6;
+            s += 24.f * eps * (2.f * s12 - s6) * r2inv;
+            if (ENERGY) e.ljr += eps * (4.f * (s12 - s6) + 1.f);
+        }
+    }
+    if ((TERMS & kTermLJA) && !(excl & kTermLJA) && r2 < pc.lja_rc2) {
+        const float sig = 0.5f * (qi.y + qj.y);
+        const float sig2 = sig * sig;
+        const float eps = 0.5f * (qi.x + qj.x);
+        float E, dEdr_over_r;  // dE/dr / r of the unswitched potential
+        if (r2 < sig2 * kTwoPow1_3) {
+            E = -eps;
+            dEdr_over_r = 0.f;
+        } else {
+            const float s2 = sig2 * r2inv;
+            const float s6 = s2 * s2 * s2;
+            const float s12 = s6 * s6;
+            E = 4.f * eps * (s12 - s6);
+            dEdr_over_r = -24.f * eps * (2.f * s12 - s6) * r2inv;
+        }
+        const float r = r2 * rinv;
+        if (r > pc.lja_rs) {
+            // OpenMM switching function S = 1 - 10x^3 + 15x^4 - 6x^5.
+            const float x = (r - pc.lja_rs) * pc.lja_inv_width;
+            const float x2 = x * x;
+            const float x3 = x2 * x;
+            const float sw = 1.f + x3 * (-10.f + x * (15.f - 6.f * x));
+            const float dsw = x2 * (-30.f + x * (60.f - 30.f * x)) * pc.lja_inv_width;
+            dEdr_over_r = dEdr_over_r * sw + E * dsw * rinv;
+            E *= sw;
+        }
+        s -= dEdr_over_r;
+        if (ENERGY) e.lja += E;
+    }
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Bond-like terms (explicit lists, no cutoff).
+// ---------------------------------------------------------------------------
+// Harmonic bond 1/2 k (r - r0)^2 (HarmonicBondForceFieldGenerator.cpp:5-10).
+// Go 10-12: k (5 (r0/r)^12 - 6 (r0/r)^10) (GoContactForceFieldGenerator.cpp:5-7).
+// Returns s with F_a = s * (x_a - x_b).
+__device__ __forceinline__ float bond_scalar(int kind, float r2, float p0, float p1, float& energy) {
+    if (kind == kBondHarmonic) {  // p0 = r0, p1 = k
+        const float r = sqrtf(r2);
+        const float dr = r - p0;
+        energy = 0.5f * p1 * dr * dr;
+        return -p1 * dr / r;
+    } else {  // Go: p0 = k, p1 = r0
+        const float inv = 1.f / r2;
+        const float t2 = p1 * p1 * inv;
+        const float t10 = t2 * t2 * t2 * t2 * t2;
+        const float t12 = t10 * t2;
+        energy = p0 * (5.f * t12 - 6.f * t10);
+        return 60.f * p0 * (t12 - t10) * inv;
+    }
+}
+
+// Flexible-local angle (FlexibleLocalAngleForceFieldGenerator.cpp:21-25):
+// E = k (spline(theta) - Emin + step(tmin-theta)(30 (tmin-theta) + y0)
+//                             + step(theta-tmax)(30 (theta-tmax) + y9)),
+// spline = natural cubic spline through 10 equidistant nodes, 0 outside.
+// Writes forces on the three particles.
+__device__ __forceinline__ void fla_forces(float3 u, float3 v, float kk, const FlaTable& t,
+                                           float3& f1, float3& f3, float& energy) {
+    // u = x1 - x2, v = x3 - x2
+    const float3 n = make_float3(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x);
+    const float nn = fmaxf(norm2(n), 1e-30f);
+    const float nlen = sqrtf(nn);
+    const float dot = u.x * v.x + u.y * v.y + u.z * v.z;
+    const float theta = atan2f(nlen, dot);
+    float S = 0.f, dS = 0.f;
+    if (theta < t.theta_min) {
+        S = 30.f * (t.theta_min - theta) + t.y[0];
+        dS = -30.f;
+    } else if (theta > t.theta_max) {
+        S = 30.f * (theta - t.theta_max) + t.y[9];
+        dS = 30.f;
+    } else {
+        const float pos = (theta - t.theta_min) * t.inv_h;
+        int k = min(8, max(0, (int)floorf(pos)));
+        const float B = pos - (float)k;
+        const float A = 1.f - B;
+        const float yk = t.y[k], yk1 = t.y[k + 1];
+        const float mk = t.m[k], mk1 = t.m[k + 1];  // M * h^2 / 6
+        S = A * yk + B * yk1 + (A * A * A - A) * mk + (B * B * B - B) * mk1;
+        dS = ((yk1 - yk) + (1.f - 3.f * A * A) * mk + (3.f * B * B - 1.f) * mk1) * t.inv_h;
+    }
+    energy = kk * (S - t.emin);
+    const float dE = kk * dS;
+    const float uu = norm2(u), vv = norm2(v);
+    // dtheta/dx1 = (u x n)/(|u|^2 |n|), dtheta/dx3 = -(v x n)/(|v|^2 |n|)
+    const float3 un = make_float3(u.y * n.z - u.z * n.y, u.z * n.x - u.x * n.z, u.x * n.y - u.y * n.x);
+    const float3 vn = make_float3(v.y * n.z - v.z * n.y, v.z * n.x - v.x * n.z, v.x * n.y - v.y * n.x);
+    const float c1 = -dE / (uu * nlen);
+    const float c3 = dE / (vv * nlen);
+    f1 = make_float3(c1 * un.x, c1 * un.y, c1 * un.z);
+    f3 = make_float3(c3 * vn.x, c3 * vn.y, c3 * vn.z);
+}
+
+// Flexible-local dihedral (FlexibleLocalDihedralForceFieldGenerator.cpp:28-36):
+// E = k (c - Emin + sum_n a_n cos(n phi) + b_n sin(n phi)), phi in the IUPAC
+// convention.  F = x1 - x2, G = x2 - x3, H = x4 - x3.
+__device__ __forceinline__ void fld_forces(float3 F, float3 G, float3 H, float kk,
+                                           const FldTable& t, float3& f1, float3& f2,
+                                           float3& f3, float3& f4, float& energy) {
+    const float3 A = make_float3(F.y * G.z - F.z * G.y, F.z * G.x - F.x * G.z, F.x * G.y - F.y * G.x);
+    const float3 B = make_float3(H.y * G.z - H.z * G.y, H.z * G.x - H.x * G.z, H.x * G.y - H.y * G.x);
+    const float AA = fmaxf(norm2(A), 1e-30f);
+    const float BB = fmaxf(norm2(B), 1e-30f);
+    const float GG = norm2(G);
+    const float Gl = sqrtf(GG);
+    const float inv_ab = rsqrtf(AA * BB);
+    const float c1 = (A.x * B.x + A.y * B.y + A.z * B.z) * inv_ab;
+    const float s1 = -Gl * (F.x * B.x + F.y * B.y + F.z * B.z) * inv_ab;
+    // multiple angles
+    const float c2 = c1 * c1 - s1 * s1, s2 = 2.f * s1 * c1;
+    const float c3 = c1 * c2 - s1 * s2, s3 = s1 * c2 + c1 * s2;
+    energy = kk * (t.c[0] - t.emin + t.c[1] * c1 + t.c[2] * s1 + t.c[3] * c2 + t.c[4] * s2 +
+                   t.c[5] * c3 + t.c[6] * s3);
+    const float dE = kk * (-t.c[1] * s1 + t.c[2] * c1 - 2.f * t.c[3] * s2 + 2.f * t.c[4] * c2 -
+                           3.f * t.c[5] * s3 + 3.f * t.c[6] * c3);
+    // Blondel-Karplus gradients.
+    const float ga = Gl / AA, gb = Gl / BB;
+    const float fg = (F.x * G.x + F.y * G.y + F.z * G.z) / (AA * Gl);
+    const float hg = (H.x * G.x + H.y * G.y + H.z * G.z) / (BB * Gl);
+    // dphi/dx1 = -ga A ; dphi/dx4 = gb B
+    const float3 d1 = make_float3(-ga * A.x, -ga * A.y, -ga * A.z);
+    const float3 d4 = make_float3(gb * B.x, gb * B.y, gb * B.z);
+    // dphi/dx2 = ga A + fg A - hg B ; dphi/dx3 = -gb B - fg A + hg B
+    const float3 d2 = make_float3((ga + fg) * A.x - hg * B.x, (ga + fg) * A.y - hg * B.y,
+                                  (ga + fg) * A.z - hg * B.z);
+    const float3 d3 = make_float3(-fg * A.x + (hg - gb) * B.x, -fg * A.y + (hg - gb) * B.y,
+                                  -fg * A.z + (hg - gb) * B.z);
+    f1 = make_float3(-dE * d1.x, -dE * d1.y, -dE * d1.z);
+    f2 = make_float3(-dE * d2.x, -dE * d2.y, -dE * d2.z);
+    f3 = make_float3(-dE * d3.x, -dE * d3.y, -dE * d3.z);
+    f4 = make_float3(-dE * d4.x, -dE * d4.y, -dE * d4.z);
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, SC'11),
+// written from the published round function.  Box-Muller turns pairs of
+// uniforms in (0, 1] into normals.
+// ---------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int round = 0; round < 10; ++round) {
+        const uint32_t lo0 = kPhiloxM0 * c.x;
+        const uint32_t hi0 = __umulhi(kPhiloxM0, c.x);
+        const uint32_t lo1 = kPhiloxM1 * c.z;
+        const uint32_t hi1 = __umulhi(kPhiloxM1, c.z);
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += kPhiloxW0;
+        k1 += kPhiloxW1;
+    }
+    return c;
+}
+__device__ __forceinline__ float uniform_open0(uint32_t x) {
+    return (float)((x >> 8) + 1u) * (1.0f / 16777216.0f);
+}
+// Three standard normals for (bead, step) of a stream.
+__device__ __forceinline__ float3 gaussian3(uint32_t seed, uint32_t stream, uint32_t bead,
+                                            unsigned long long step, uint32_t purpose) {
+    const U4 r = philox4x32_10(U4{bead, (uint32_t)step, (uint32_t)(step >> 32), purpose}, seed,
+                               kPhiloxKey1 ^ stream);
+    const float u1 = uniform_open0(r.x), u2 = uniform_open0(r.y);
+    const float u3 = uniform_open0(r.z), u4 = uniform_open0(r.w);
+    const float a = sqrtf(-2.f * logf(u1));
+    const float b = sqrtf(-2.f * logf(u3));
+    float s2, c2, s4, c4;
+    sincospif(2.f * u2, &s2, &c2);
+    sincospif(2.f * u4, &s4, &c4);
+    return make_float3(a * c2, a * s2, b * c4);
+}
+
+}  // namespace ocm

@@ -1,0 +1,146 @@
+// engine.hpp - host classes of the plain (single-system) and batched engines.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "host_system.hpp"
+
+namespace ocm {
+
+void cuda_check(cudaError_t e, const char* what);
+#define OCM_CK(x) ::ocm::cuda_check((x), #x)
+
+// Owning device buffer.
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw Error(3, std::string("[error] device allocation of ") +
+                               std::to_string(count * sizeof(T)) + " bytes failed: " +
+                               cudaGetErrorString(e));
+        }
+        n = count;
+    }
+    void upload(const std::vector<T>& v, cudaStream_t s) {
+        if (v.size() > n) alloc(v.size());
+        if (!v.empty())
+            OCM_CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+};
+
+struct ListFlags {
+    enum : int { kTileOverflow = 1, kMaskOverflow = 2, kSkinViolation = 4 };
+};
+
+// Device-resident single system, the part of an OpenMM Context + Langevin
+// integrator that the reference drives through Simulator::run.
+class PlainContext {
+  public:
+    PlainContext(const SystemDesc& d, double temperature, double friction, double dt,
+                 int32_t seed, int device);
+    ~PlainContext();
+    void set_positions(const double* xyz);
+    void get_positions(double* xyz);
+    void set_velocities(const double* v);
+    void get_velocities(double* v);
+    void set_velocities_to_temperature(double temperature, int32_t seed);
+    void get_state(uint32_t groups, double* forces, double* energy);
+    void group_energies(double* energies32);
+    double kinetic_energy();
+    void step(int64_t n);
+    void set_list_options(int32_t interval, double skin);
+    void list_pairs(int64_t* out, int64_t cap, int64_t* n_out);
+    void cluster_order(int64_t* out, int64_t cap, int64_t* n_out);
+
+    int device = 0;
+    int64_t n = 0, np = 0, nc = 0;
+    int64_t steps_done = 0, list_builds = 0;
+    int32_t rebuild_interval = 10;
+    double skin = 0.25;
+    bool reorder = false;
+    int64_t tiles_last = 0, masked_last = 0;
+    CompiledSystem cs;
+
+  private:
+    void rebuild(cudaStream_t s);
+    void launch_forces(cudaStream_t s, bool energy, uint32_t slots_enabled, int r);
+    void launch_integrate(cudaStream_t s, int r);
+    void ensure_capacity();
+    cudaGraphExec_t graph_for(int chunk);
+    void clear_graphs();
+    void eval(uint32_t groups, bool energy, double* forces, double* slot_energy);
+    uint32_t slots_for_groups(uint32_t groups) const;
+    void check_positions_set() const;
+
+    cudaStream_t stream_ = nullptr;
+    std::map<int, cudaGraphExec_t> graphs_;
+    bool positions_set_ = false;
+    LangevinConsts lc_{};
+    int cell_dims_[3] = {1, 1, 1};
+    int64_t n_cells_ = 0;
+    int64_t tile_cap_ = 0, mask_cap_ = 0;
+    float3 box_{0, 0, 0}, inv_box_{0, 0, 0};
+
+    // per particle (original order)
+    DevBuf<double> x_, y_, z_;
+    DevBuf<float> vx_, vy_, vz_, invm_;
+    DevBuf<unsigned long long> F_;  // 3*n, SoA
+    DevBuf<float4> xq_, ref_, p0_, p1_;
+    DevBuf<uint32_t> lab_;
+    DevBuf<int32_t> slot_;
+    // cluster order
+    DevBuf<int32_t> perm_;
+    DevBuf<float4> xs_, p0s_, p1s_;
+    DevBuf<uint32_t> labs_;
+    DevBuf<float4> bb_c_, bb_h_;
+    DevBuf<int32_t> tile_count_, tile_start_, tile_j_, tile_mask_;
+    DevBuf<uint32_t> masks_;
+    DevBuf<int32_t> mask_count_;
+    // cell sort
+    DevBuf<uint32_t> cell_rank_;
+    DevBuf<int32_t> cell_key_, cell_count_, cell_start_, cell_fill_, bucket_;
+    // exclusions
+    DevBuf<int32_t> ex_start_, ex_j_;
+    DevBuf<uint8_t> ex_bits_;
+    // bonded
+    DevBuf<BondTerm> bonds_;
+    DevBuf<AngleTerm> angles_;
+    DevBuf<DihedralTerm> dihedrals_;
+    DevBuf<FlaTable> fla_;
+    DevBuf<FldTable> fld_;
+    // misc
+    DevBuf<double> energy_;           // kNumSlots
+    DevBuf<int32_t> flags_;           // ListFlags bits
+    DevBuf<uint32_t> maxdisp_;        // float bits, since last build
+    DevBuf<unsigned long long> step_base_;
+    DevBuf<double> ke_;
+    // snapshot for retries
+    DevBuf<double> sx_, sy_, sz_;
+    DevBuf<float> svx_, svy_, svz_;
+    DevBuf<unsigned long long> sstep_;
+    int32_t* h_flags_ = nullptr;  // pinned
+};
+
+// Many independent systems, each advanced inside one CTA's shared memory.
+class BatchEngine;
+
+}  // namespace ocm

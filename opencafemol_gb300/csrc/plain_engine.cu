@@ -1,0 +1,1261 @@
+// plain_engine.cu - the plain single-system path.
+//
+// Per step: one fused force kernel (cluster-pair tiles for every pair term,
+// plus bond, Go-contact, FLA and FLD segments in the same grid) and one
+// Langevin kernel that also zeroes the fixed-point force buffer.  Every
+// `rebuild_interval` steps the cluster layout and tile list are rebuilt:
+//   cell keys -> counting sort by Morton rank (periodic systems) ->
+//   gather into cluster order -> cluster bounding boxes -> tile count /
+//   scan / fill -> exclusion masks.
+// A chunk of steps (rebuild + steps) is captured once into a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "device_math.cuh"
+#include "engine.hpp"
+
+namespace ocm {
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess)
+        throw Error(2, std::string("[error] CUDA: ") + what + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+constexpr int kForceThreads = 128;
+constexpr int kWarpsPerForceBlock = kForceThreads / 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float4 shfl4(float4 v, int src) {
+    v.x = __shfl_sync(kFull, v.x, src);
+    v.y = __shfl_sync(kFull, v.y, src);
+    v.z = __shfl_sync(kFull, v.z, src);
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// Rebuild kernels
+// ---------------------------------------------------------------------------
+__global__ void k_cell_keys(int n, const float4* __restrict__ xq, int nx, int ny, int nz,
+                            float3 box, const uint32_t* __restrict__ cell_rank,
+                            int32_t* __restrict__ key, int32_t* __restrict__ count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = xq[i];
+    const int cx = min(nx - 1, max(0, (int)(p.x * ((float)nx / box.x))));
+    const int cy = min(ny - 1, max(0, (int)(p.y * ((float)ny / box.y))));
+    const int cz = min(nz - 1, max(0, (int)(p.z * ((float)nz / box.z))));
+    const int k = (int)cell_rank[(cz * ny + cy) * nx + cx];
+    key[i] = k;
+    atomicAdd(&count[k], 1);
+}
+
+// Exclusive scan of m ints into out[0..m] by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan(int m, const int32_t* __restrict__ in,
+                                               int32_t* __restrict__ out) {
+    __shared__ int32_t part[1024];
+    const int t = threadIdx.x;
+    const int per = (m + 1023) / 1024;
+    const int b = t * per, e = min(m, b + per);
+    int32_t s = 0;
+    for (int i = b; i < e; ++i) s += in[i];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int32_t v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int32_t run = part[t] - s;
+    for (int i = b; i < e; ++i) {
+        const int32_t v = in[i];
+        out[i] = run;
+        run += v;
+    }
+    if (t == 1023) out[m] = part[1023];
+}
+
+__global__ void k_bucket_scatter(int n, const int32_t* __restrict__ key,
+                                 const int32_t* __restrict__ start, int32_t* __restrict__ fill,
+                                 int32_t* __restrict__ bucket) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int k = key[i];
+    bucket[start[k] + atomicAdd(&fill[k], 1)] = i;
+}
+
+// Order each cell's members by particle index: the result is the unique
+// stable order (Morton rank, index), independent of atomic timing.
+__global__ void k_bucket_sort(int n_cells, const int32_t* __restrict__ start,
+                              const int32_t* __restrict__ bucket, int32_t* __restrict__ perm) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cells) return;
+    const int b = start[c], e = start[c + 1];
+    for (int i = b; i < e; ++i) {
+        const int v = bucket[i];
+        int j = i - 1;
+        while (j >= b && perm[j] > v) {
+            perm[j + 1] = perm[j];
+            --j;
+        }
+        perm[j + 1] = v;
+    }
+}
+
+__global__ void k_gather_sorted(int np, const int32_t* __restrict__ perm,
+                                const float4* __restrict__ xq, const float4* __restrict__ p0,
+                                const float4* __restrict__ p1, const uint32_t* __restrict__ lab,
+                                int32_t* __restrict__ slot, float4* __restrict__ xs,
+                                float4* __restrict__ p0s, float4* __restrict__ p1s,
+                                uint32_t* __restrict__ labs, float4* __restrict__ ref,
+                                uint32_t* __restrict__ maxdisp) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) *maxdisp = 0u;
+    if (k >= np) return;
+    const int o = perm[k];
+    if (o >= 0) {
+        slot[o] = k;
+        const float4 p = xq[o];
+        xs[k] = p;
+        ref[o] = p;
+        p0s[k] = p0[o];
+        p1s[k] = p1[o];
+        labs[k] = lab[o];
+    } else {
+        const float nan = __int_as_float(0x7fc00000);
+        xs[k] = make_float4(nan, nan, nan, 0.f);
+        p0s[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        p1s[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        labs[k] = 0xffffffffu;
+    }
+}
+
+template <bool PERIODIC>
+__global__ void k_bbox(int nc, const float4* __restrict__ xs, const int32_t* __restrict__ perm,
+                       float3 box, float3 inv_box, float4* __restrict__ bc,
+                       float4* __restrict__ bh) {
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (I >= nc) return;
+    const float4 base = xs[I * 32];
+    const bool valid = perm[I * 32 + lane] >= 0;
+    float3 d = make_float3(0.f, 0.f, 0.f);
+    if (valid) d = separation<PERIODIC>(base, xs[I * 32 + lane], box, inv_box);
+    float lx = d.x, ly = d.y, lz = d.z, hx = d.x, hy = d.y, hz = d.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lx = fminf(lx, __shfl_xor_sync(kFull, lx, o));
+        ly = fminf(ly, __shfl_xor_sync(kFull, ly, o));
+        lz = fminf(lz, __shfl_xor_sync(kFull, lz, o));
+        hx = fmaxf(hx, __shfl_xor_sync(kFull, hx, o));
+        hy = fmaxf(hy, __shfl_xor_sync(kFull, hy, o));
+        hz = fmaxf(hz, __shfl_xor_sync(kFull, hz, o));
+    }
+    if (lane == 0) {
+        bc[I] = make_float4(base.x + 0.5f * (lx + hx), base.y + 0.5f * (ly + hy),
+                            base.z + 0.5f * (lz + hz), 0.f);
+        bh[I] = make_float4(0.5f * (hx - lx), 0.5f * (hy - ly), 0.5f * (hz - lz), 0.f);
+    }
+}
+
+template <bool PERIODIC>
+__device__ __forceinline__ bool boxes_close(float4 ci, float4 hi, float4 cj, float4 hj,
+                                            float3 box, float3 inv_box, float cut, float cut2) {
+    float dx = cj.x - ci.x, dy = cj.y - ci.y, dz = cj.z - ci.z;
+    float gx, gy, gz;
+    if (PERIODIC) {
+        dx -= box.x * rintf(dx * inv_box.x);
+        dy -= box.y * rintf(dy * inv_box.y);
+        dz -= box.z * rintf(dz * inv_box.z);
+        // Boxes this large relative to the period may meet through another
+        // image: treat that dimension as overlapping.
+        gx = (hi.x + hj.x + cut >= 0.5f * box.x) ? 0.f : fmaxf(0.f, fabsf(dx) - hi.x - hj.x);
+        gy = (hi.y + hj.y + cut >= 0.5f * box.y) ? 0.f : fmaxf(0.f, fabsf(dy) - hi.y - hj.y);
+        gz = (hi.z + hj.z + cut >= 0.5f * box.z) ? 0.f : fmaxf(0.f, fabsf(dz) - hi.z - hj.z);
+    } else {
+        gx = fmaxf(0.f, fabsf(dx) - hi.x - hj.x);
+        gy = fmaxf(0.f, fabsf(dy) - hi.y - hj.y);
+        gz = fmaxf(0.f, fabsf(dz) - hi.z - hj.z);
+    }
+    return gx * gx + gy * gy + gz * gz < cut2;
+}
+
+template <bool PERIODIC, bool FILL>
+__global__ void k_tiles(int nc, const float4* __restrict__ bc, const float4* __restrict__ bh,
+                        float3 box, float3 inv_box, float cut, float cut2,
+                        int32_t* __restrict__ count, const int32_t* __restrict__ start,
+                        int32_t* __restrict__ tile_j, int32_t* __restrict__ tile_mask, int cap,
+                        int32_t* __restrict__ flags) {
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (I >= nc) return;
+    if (FILL && start[nc] > cap) {
+        if (I == 0 && lane == 0) atomicOr(flags, ListFlags::kTileOverflow);
+        return;
+    }
+    const float4 ci = bc[I], hi = bh[I];
+    int pos = FILL ? start[I] : 0;
+    for (int J0 = I; J0 < nc; J0 += 32) {
+        const int J = J0 + lane;
+        bool ok = false;
+        if (J < nc) ok = boxes_close<PERIODIC>(ci, hi, bc[J], bh[J], box, inv_box, cut, cut2);
+        const unsigned b = __ballot_sync(kFull, ok);
+        if (FILL && ok) {
+            const int at = pos + __popc(b & ((1u << lane) - 1u));
+            tile_j[at] = J;
+            tile_mask[at] = -1;
+        }
+        pos += __popc(b);
+    }
+    if (!FILL && lane == 0) count[I] = pos;
+}
+
+__device__ __forceinline__ int find_tile(const int32_t* __restrict__ start,
+                                         const int32_t* __restrict__ tile_j, int a, int b) {
+    int lo = start[a], hi = start[a + 1] - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int v = tile_j[mid];
+        if (v == b) return mid;
+        if (v < b) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return -1;
+}
+
+template <bool FILLBITS>
+__global__ void k_excl(int nnz, int nc, int tile_cap, const int32_t* __restrict__ ex_i, const int32_t* __restrict__ ex_j,
+                       const uint8_t* __restrict__ ex_bits, const int32_t* __restrict__ slot,
+                       const int32_t* __restrict__ start, const int32_t* __restrict__ tile_j,
+                       int32_t* __restrict__ tile_mask, uint32_t* __restrict__ masks,
+                       int32_t* __restrict__ mask_count, int mask_cap,
+                       int32_t* __restrict__ flags) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nnz) return;
+    if (start[nc] > tile_cap) return;  // overflowed list: never read past capacity
+    const int i = ex_i[e], j = ex_j[e];
+    if (i >= j) return;
+    const int si = slot[i], sj = slot[j];
+    const int ci = si >> 5, cj = sj >> 5;
+    const int a = min(ci, cj), b = max(ci, cj);
+    const int t = find_tile(start, tile_j, a, b);
+    if (t < 0) return;
+    if (!FILLBITS) {
+        if (atomicCAS(&tile_mask[t], -1, -2) == -1) {
+            const int m = atomicAdd(mask_count, 1);
+            if (m >= mask_cap) {
+                atomicOr(flags, ListFlags::kMaskOverflow);
+                tile_mask[t] = -1;
+                return;
+            }
+            for (int w = 0; w < 128; ++w) masks[(size_t)m * 128 + w] = 0u;
+            __threadfence();
+            tile_mask[t] = m;
+        }
+        return;
+    }
+    const int m = tile_mask[t];
+    if (m < 0) return;
+    const int bits = ex_bits[e];
+    // word (term, i-lane) bit r: pair (i-lane, (i-lane + r) & 31)
+    int la, lb;
+    if (ci <= cj) {
+        la = si & 31;
+        lb = sj & 31;
+    } else {
+        la = sj & 31;
+        lb = si & 31;
+    }
+    for (int term = 0; term < kNumPairTerms; ++term) {
+        if (!(bits & (1 << term))) continue;
+        atomicOr(&masks[(size_t)m * 128 + term * 32 + la], 1u << ((lb - la) & 31));
+        if (ci == cj) atomicOr(&masks[(size_t)m * 128 + term * 32 + lb], 1u << ((la - lb) & 31));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused force kernel
+// ---------------------------------------------------------------------------
+struct ForceArgs {
+    int tile_cap;
+    int nc, blocks_tiles, blocks_bonds, blocks_angles, blocks_dih;
+    int n;
+    const float4 *xs, *p0s, *p1s;
+    const uint32_t* labs;
+    const int32_t *perm, *tile_start, *tile_j, *tile_mask;
+    const uint32_t* masks;
+    const double *x, *y, *z;
+    int n_bonds, n_angles, n_dih;
+    const BondTerm* bonds;
+    const AngleTerm* angles;
+    const FlaTable* fla;
+    const DihedralTerm* dih;
+    const FldTable* fld;
+    unsigned long long* F;
+    PairConsts pc;
+    float3 box, inv_box;
+    uint32_t slots_enabled;
+    uint32_t excl_all;
+    double* energy;
+};
+
+__device__ __forceinline__ void add_force(unsigned long long* F, int n, int i, float3 f) {
+    fixed_add(&F[i], f.x);
+    fixed_add(&F[n + i], f.y);
+    fixed_add(&F[2 * n + i], f.z);
+}
+
+__device__ __forceinline__ float3 bonded_sep(const ForceArgs& a, int i, int j, int periodic) {
+    // x_j - x_i from the FP64 positions, minimum image when the force is periodic.
+    float3 d = make_float3((float)(a.x[j] - a.x[i]), (float)(a.y[j] - a.y[i]),
+                           (float)(a.z[j] - a.z[i]));
+    if (periodic) {
+        d.x -= a.box.x * rintf(d.x * a.inv_box.x);
+        d.y -= a.box.y * rintf(d.y * a.inv_box.y);
+        d.z -= a.box.z * rintf(d.z * a.inv_box.z);
+    }
+    return d;
+}
+
+template <int TERMS, bool PERIODIC, bool ENERGY>
+__global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
+    const int lane = threadIdx.x & 31;
+    int blk = blockIdx.x;
+    if (blk < a.blocks_tiles) {
+        // ---------------- cluster-pair tiles ----------------
+        const int I = blk * kWarpsPerForceBlock + (threadIdx.x >> 5);
+        if (I >= a.nc) return;
+        if (a.tile_start[a.nc] > a.tile_cap) return;  // overflowed list (flagged for a retry)
+        const int ki = I * 32 + lane;
+        const float4 xi = a.xs[ki];
+        const float4 p0i = a.p0s[ki];
+        const float4 p1i = (TERMS & kTermLJA) ? a.p1s[ki] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint32_t labi = a.labs[ki];
+        const bool labels = a.pc.uses_labels != 0;
+        float3 fi = make_float3(0.f, 0.f, 0.f);
+        double eacc[4] = {0.0, 0.0, 0.0, 0.0};
+        const int t0 = a.tile_start[I], t1 = a.tile_start[I + 1];
+        for (int t = t0; t < t1; ++t) {
+            const int J = a.tile_j[t];
+            const int m = a.tile_mask[t];
+            const int kj = J * 32 + lane;
+            float4 xj = a.xs[kj];
+            float4 p0j = a.p0s[kj];
+            float4 p1j = (TERMS & kTermLJA) ? a.p1s[kj] : make_float4(0.f, 0.f, 0.f, 0.f);
+            uint32_t labj = a.labs[kj];
+            float3 fj = make_float3(0.f, 0.f, 0.f);
+            uint32_t mw[4] = {0u, 0u, 0u, 0u};
+            if (m >= 0) {
+#pragma unroll
+                for (int term = 0; term < 4; ++term)
+                    if (TERMS & (1 << term)) mw[term] = a.masks[(size_t)m * 128 + term * 32 + lane];
+            }
+            const bool diag = (J == I);
+            PairEnergy e;
+            e.zero();
+            for (int r = 0; r < 32; ++r) {
+                const bool do_pair = !diag || (r > 0 && (r < 16 || (r == 16 && lane < 16)));
+                if (do_pair) {
+                    const float3 d = separation<PERIODIC>(xi, xj, a.box, a.inv_box);
+                    const float r2 = norm2(d);
+                    if (r2 < a.pc.list_rc2) {
+                        uint32_t ex = a.excl_all;
+#pragma unroll
+                        for (int term = 0; term < 4; ++term)
+                            if (TERMS & (1 << term)) ex |= ((mw[term] >> r) & 1u) << term;
+                        if (labels) {
+#pragma unroll
+                            for (int term = 0; term < 4; ++term)
+                                if ((TERMS & (1 << term)) && (a.pc.uses_labels & (1 << term)) &&
+                                    !labels_allow(labi, labj, term, a.pc.allow[term]))
+                                    ex |= 1u << term;
+                        }
+                        const float s = pair_scalar<TERMS, ENERGY>(r2, p0i, p0j, p1i, p1j, ex, a.pc, e);
+                        fi.x -= s * d.x;
+                        fi.y -= s * d.y;
+                        fi.z -= s * d.z;
+                        fj.x += s * d.x;
+                        fj.y += s * d.y;
+                        fj.z += s * d.z;
+                    }
+                }
+                const int src = (lane + 1) & 31;
+                xj = shfl4(xj, src);
+                if (TERMS & kTermEXV) p0j.x = __shfl_sync(kFull, p0j.x, src);
+                if (TERMS & kTermDH) p0j.y = __shfl_sync(kFull, p0j.y, src);
+                if (TERMS & kTermLJR) {
+                    p0j.z = __shfl_sync(kFull, p0j.z, src);
+                    p0j.w = __shfl_sync(kFull, p0j.w, src);
+                }
+                if (TERMS & kTermLJA) {
+                    p1j.x = __shfl_sync(kFull, p1j.x, src);
+                    p1j.y = __shfl_sync(kFull, p1j.y, src);
+                }
+                if (labels) labj = __shfl_sync(kFull, labj, src);
+                fj.x = __shfl_sync(kFull, fj.x, src);
+                fj.y = __shfl_sync(kFull, fj.y, src);
+                fj.z = __shfl_sync(kFull, fj.z, src);
+            }
+            const int oj = a.perm[kj];
+            if (oj >= 0) add_force(a.F, a.n, oj, fj);
+            if (ENERGY) {
+                eacc[0] += e.exv;
+                eacc[1] += e.dh;
+                eacc[2] += e.ljr;
+                eacc[3] += e.lja;
+            }
+        }
+        const int oi = a.perm[ki];
+        if (oi >= 0) add_force(a.F, a.n, oi, fi);
+        if (ENERGY) {
+#pragma unroll
+            for (int term = 0; term < 4; ++term) {
+                if (!(TERMS & (1 << term))) continue;
+                const double v = warp_sum(eacc[term]);
+                if (lane == 0 && v != 0.0) atomicAdd(&a.energy[term], v);
+            }
+        }
+        return;
+    }
+    blk -= a.blocks_tiles;
+    if (blk < a.blocks_bonds) {
+        // ---------------- harmonic bonds and Go contacts ----------------
+        const int t = blk * kForceThreads + threadIdx.x;
+        float eh = 0.f, eg = 0.f;
+        if (t < a.n_bonds) {
+            const BondTerm b = a.bonds[t];
+            const int slot = b.kind == kBondHarmonic ? kSlotHB : kSlotGO;
+            if (a.slots_enabled & (1u << slot)) {
+                const float3 d = bonded_sep(a, b.i, b.j, b.periodic);
+                float en;
+                const float s = bond_scalar(b.kind, norm2(d), b.p0, b.p1, en);
+                add_force(a.F, a.n, b.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
+                add_force(a.F, a.n, b.j, make_float3(s * d.x, s * d.y, s * d.z));
+                if (b.kind == kBondHarmonic) eh = en;
+                else eg = en;
+            }
+        }
+        if (ENERGY) {
+            const double vh = warp_sum((double)eh), vg = warp_sum((double)eg);
+            if (lane == 0) {
+                if (vh != 0.0) atomicAdd(&a.energy[kSlotHB], vh);
+                if (vg != 0.0) atomicAdd(&a.energy[kSlotGO], vg);
+            }
+        }
+        return;
+    }
+    blk -= a.blocks_bonds;
+    if (blk < a.blocks_angles) {
+        const int t = blk * kForceThreads + threadIdx.x;
+        float en = 0.f;
+        if (t < a.n_angles && (a.slots_enabled & (1u << kSlotFLA))) {
+            const AngleTerm g = a.angles[t];
+            const float3 u = bonded_sep(a, g.j, g.i, g.periodic);  // x1 - x2
+            const float3 v = bonded_sep(a, g.j, g.k, g.periodic);  // x3 - x2
+            float3 f1, f3;
+            fla_forces(u, v, g.kk, a.fla[g.table], f1, f3, en);
+            add_force(a.F, a.n, g.i, f1);
+            add_force(a.F, a.n, g.k, f3);
+            add_force(a.F, a.n, g.j, make_float3(-f1.x - f3.x, -f1.y - f3.y, -f1.z - f3.z));
+        }
+        if (ENERGY) {
+            const double v = warp_sum((double)en);
+            if (lane == 0 && v != 0.0) atomicAdd(&a.energy[kSlotFLA], v);
+        }
+        return;
+    }
+    blk -= a.blocks_angles;
+    {
+        const int t = blk * kForceThreads + threadIdx.x;
+        float en = 0.f;
+        if (t < a.n_dih && (a.slots_enabled & (1u << kSlotFLD))) {
+            const DihedralTerm q = a.dih[t];
+            const float3 F = bonded_sep(a, q.j, q.i, q.periodic);  // x1 - x2
+            const float3 G = bonded_sep(a, q.k, q.j, q.periodic);  // x2 - x3
+            const float3 H = bonded_sep(a, q.k, q.l, q.periodic);  // x4 - x3
+            float3 f1, f2, f3, f4;
+            fld_forces(F, G, H, q.kk, a.fld[q.table], f1, f2, f3, f4, en);
+            add_force(a.F, a.n, q.i, f1);
+            add_force(a.F, a.n, q.j, f2);
+            add_force(a.F, a.n, q.k, f3);
+            add_force(a.F, a.n, q.l, f4);
+        }
+        if (ENERGY) {
+            const double v = warp_sum((double)en);
+            if (lane == 0 && v != 0.0) atomicAdd(&a.energy[kSlotFLD], v);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Langevin integrator (OpenMM LangevinIntegrator, leapfrog form):
+//   v <- vscale v + fscale F/m + noise sqrt(1/m) N(0,1);  x <- x + v dt
+// ---------------------------------------------------------------------------
+struct IntegrateArgs {
+    int n;
+    unsigned long long* F;
+    float *vx, *vy, *vz;
+    double *x, *y, *z;
+    const float* invm;
+    float4 *xq, *xs;
+    const int32_t* slot;
+    const float4* ref;
+    LangevinConsts lc;
+    const unsigned long long* step_base;
+    int r;
+    int periodic;
+    double box[3], inv_box[3];
+    float3 fbox, finv_box;
+    float disp_limit2;
+    uint32_t* maxdisp;
+    int32_t* flags;
+};
+
+__device__ __forceinline__ double wrap_coord(double x, double L, double invL) {
+    const double k = floor(__dmul_rn(x, invL));
+    return __dsub_rn(x, __dmul_rn(k, L));
+}
+
+__global__ void k_integrate(IntegrateArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const unsigned long long step = *a.step_base + (unsigned long long)a.r;
+    const float fx = (float)((double)(long long)a.F[i] * kFixedInv);
+    const float fy = (float)((double)(long long)a.F[a.n + i] * kFixedInv);
+    const float fz = (float)((double)(long long)a.F[2 * a.n + i] * kFixedInv);
+    a.F[i] = 0ull;
+    a.F[a.n + i] = 0ull;
+    a.F[2 * a.n + i] = 0ull;
+    const float im = a.invm[i];
+    double x = a.x[i], y = a.y[i], z = a.z[i];
+    if (im > 0.f) {
+        const float3 g = gaussian3(a.lc.seed, a.lc.stream, (uint32_t)i, step, kPurposeLangevin);
+        const float sq = sqrtf(im) * a.lc.noise;
+        const float fs = a.lc.fscale * im;
+        const float vx = a.lc.vscale * a.vx[i] + fs * fx + sq * g.x;
+        const float vy = a.lc.vscale * a.vy[i] + fs * fy + sq * g.y;
+        const float vz = a.lc.vscale * a.vz[i] + fs * fz + sq * g.z;
+        a.vx[i] = vx;
+        a.vy[i] = vy;
+        a.vz[i] = vz;
+        x += (double)vx * (double)a.lc.dt;
+        y += (double)vy * (double)a.lc.dt;
+        z += (double)vz * (double)a.lc.dt;
+        a.x[i] = x;
+        a.y[i] = y;
+        a.z[i] = z;
+    }
+    float4 p;
+    if (a.periodic) {
+        p = make_float4(__double2float_rn(wrap_coord(x, a.box[0], a.inv_box[0])),
+                        __double2float_rn(wrap_coord(y, a.box[1], a.inv_box[1])),
+                        __double2float_rn(wrap_coord(z, a.box[2], a.inv_box[2])), 0.f);
+    } else {
+        p = make_float4(__double2float_rn(x), __double2float_rn(y), __double2float_rn(z), 0.f);
+    }
+    a.xq[i] = p;
+    a.xs[a.slot[i]] = p;
+    const float4 q = a.ref[i];
+    float3 d = a.periodic ? separation<true>(q, p, a.fbox, a.finv_box)
+                          : separation<false>(q, p, a.fbox, a.finv_box);
+    const float d2 = norm2(d);
+    if (d2 > a.disp_limit2) atomicOr(a.flags, ListFlags::kSkinViolation);
+    atomicMax(a.maxdisp, __float_as_uint(d2));
+}
+
+__global__ void k_positions_to_float(int n, const double* __restrict__ x,
+                                     const double* __restrict__ y, const double* __restrict__ z,
+                                     int periodic, double bx, double by, double bz, double ibx,
+                                     double iby, double ibz, float4* __restrict__ xq) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (periodic)
+        xq[i] = make_float4(__double2float_rn(wrap_coord(x[i], bx, ibx)),
+                            __double2float_rn(wrap_coord(y[i], by, iby)),
+                            __double2float_rn(wrap_coord(z[i], bz, ibz)), 0.f);
+    else
+        xq[i] = make_float4(__double2float_rn(x[i]), __double2float_rn(y[i]),
+                            __double2float_rn(z[i]), 0.f);
+}
+
+__global__ void k_advance(unsigned long long* step_base, int k) { *step_base += (unsigned long long)k; }
+
+__global__ void k_velocity_init(int n, const float* __restrict__ invm, float kT, uint32_t seed,
+                                uint32_t stream, float* vx, float* vy, float* vz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float im = invm[i];
+    const float3 g = gaussian3(seed, stream, (uint32_t)i, 0ull, kPurposeVelocityInit);
+    const float s = im > 0.f ? sqrtf(kT * im) : 0.f;
+    vx[i] = s * g.x;
+    vy[i] = s * g.y;
+    vz[i] = s * g.z;
+}
+
+__global__ void k_kinetic(int n, const float* __restrict__ invm, const float* __restrict__ vx,
+                          const float* __restrict__ vy, const float* __restrict__ vz, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    if (i < n && invm[i] > 0.f) {
+        const double m = 1.0 / (double)invm[i];
+        e = 0.5 * m * ((double)vx[i] * vx[i] + (double)vy[i] * vy[i] + (double)vz[i] * vz[i]);
+    }
+    e = warp_sum(e);
+    if ((threadIdx.x & 31) == 0 && e != 0.0) atomicAdd(out, e);
+}
+
+// Verification: emit every pair the tiles make the kernel test whose FP32
+// r^2 is below the largest cutoff squared.
+template <bool PERIODIC>
+__global__ void k_list_pairs(int nc, const float4* __restrict__ xs, const int32_t* __restrict__ perm,
+                             const int32_t* __restrict__ tile_start, const int32_t* __restrict__ tile_j,
+                             float3 box, float3 inv_box, float rc2, long long* out, long long cap,
+                             unsigned long long* count, long long tile_cap) {
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (I >= nc) return;
+    if ((long long)tile_start[nc] > tile_cap) return;
+    const float4 xi = xs[I * 32 + lane];
+    const int oi = perm[I * 32 + lane];
+    for (int t = tile_start[I]; t < tile_start[I + 1]; ++t) {
+        const int J = tile_j[t];
+        const bool diag = J == I;
+        for (int r = 0; r < 32; ++r) {
+            const int jl = (lane + r) & 31;
+            const bool do_pair = !diag || (r > 0 && (r < 16 || (r == 16 && lane < 16)));
+            const float4 xj = xs[J * 32 + jl];
+            const int oj = perm[J * 32 + jl];
+            if (do_pair && oi >= 0 && oj >= 0) {
+                const float r2 = norm2(separation<PERIODIC>(xi, xj, box, inv_box));
+                if (r2 < rc2) {
+                    const unsigned long long at = atomicAdd(count, 1ull);
+                    if ((long long)at < cap) {
+                        out[2 * at] = min(oi, oj);
+                        out[2 * at + 1] = max(oi, oj);
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int TERMS>
+void launch_forces_t(const ForceArgs& a, int grid, cudaStream_t s, bool periodic, bool energy) {
+    if (periodic) {
+        if (energy) k_forces<TERMS, true, true><<<grid, kForceThreads, 0, s>>>(a);
+        else k_forces<TERMS, true, false><<<grid, kForceThreads, 0, s>>>(a);
+    } else {
+        if (energy) k_forces<TERMS, false, true><<<grid, kForceThreads, 0, s>>>(a);
+        else k_forces<TERMS, false, false><<<grid, kForceThreads, 0, s>>>(a);
+    }
+}
+
+uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    auto spread = [](uint32_t v) {
+        uint32_t r = 0;
+        for (int b = 0; b < 10; ++b) r |= ((v >> b) & 1u) << (3 * b);
+        return r;
+    };
+    return spread(x) | (spread(y) << 1) | (spread(z) << 2);
+}
+
+inline int div_up(int64_t a, int b) { return (int)((a + b - 1) / b); }
+
+}  // namespace
+
+// ===========================================================================
+// PlainContext
+// ===========================================================================
+PlainContext::PlainContext(const SystemDesc& d, double temperature, double friction, double dt,
+                           int32_t seed, int dev)
+    : device(dev) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        throw Error(2, "[error] no CUDA device is available");
+    if (dev < 0 || dev >= count) throw Error(1, "[error] invalid device index");
+    OCM_CK(cudaSetDevice(dev));
+    if (!(dt > 0)) throw Error(1, "[error] step size must be positive");
+    if (!(friction >= 0)) throw Error(1, "[error] friction must be >= 0");
+    if (!(temperature >= 0)) throw Error(1, "[error] temperature must be >= 0");
+    cs = compile_system(d);
+    n = cs.n;
+    if (n <= 0) throw Error(1, "[error] system has no particles");
+    if (n > (1 << 27)) throw Error(6, "[error] system too large");
+    np = ((n + 31) / 32) * 32;
+    nc = np / 32;
+    OCM_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    OCM_CK(cudaMallocHost(&h_flags_, 16 * sizeof(int32_t)));
+
+    // Langevin constants (OpenMM LangevinIntegrator).
+    const double vscale = std::exp(-friction * dt);
+    const double fscale = friction == 0 ? dt : (1.0 - vscale) / friction;
+    const double kT = constant::boltz * temperature;
+    lc_.vscale = (float)vscale;
+    lc_.fscale = (float)fscale;
+    lc_.noise = (float)std::sqrt(kT * (1.0 - vscale * vscale));
+    lc_.dt = (float)dt;
+    lc_.seed = (uint32_t)seed;
+    lc_.stream = 0u;
+
+    box_ = make_float3((float)cs.box[0], (float)cs.box[1], (float)cs.box[2]);
+    inv_box_ = make_float3(cs.box[0] > 0 ? (float)(1.0 / cs.box[0]) : 0.f,
+                           cs.box[1] > 0 ? (float)(1.0 / cs.box[1]) : 0.f,
+                           cs.box[2] > 0 ? (float)(1.0 / cs.box[2]) : 0.f);
+    reorder = cs.periodic && n > 2048;
+
+    cudaStream_t s = stream_;
+    x_.alloc(n); y_.alloc(n); z_.alloc(n);
+    vx_.alloc(n); vy_.alloc(n); vz_.alloc(n);
+    OCM_CK(cudaMemsetAsync(vx_.p, 0, n * sizeof(float), s));
+    OCM_CK(cudaMemsetAsync(vy_.p, 0, n * sizeof(float), s));
+    OCM_CK(cudaMemsetAsync(vz_.p, 0, n * sizeof(float), s));
+    invm_.upload(cs.inv_mass, s);
+    F_.alloc(3 * n);
+    OCM_CK(cudaMemsetAsync(F_.p, 0, 3 * n * sizeof(unsigned long long), s));
+    xq_.alloc(n); ref_.alloc(n);
+    {
+        std::vector<float4> p0(n), p1(n);
+        for (int64_t i = 0; i < n; ++i) {
+            p0[i] = make_float4(cs.p0[4 * i], cs.p0[4 * i + 1], cs.p0[4 * i + 2], cs.p0[4 * i + 3]);
+            p1[i] = make_float4(cs.p1[4 * i], cs.p1[4 * i + 1], cs.p1[4 * i + 2], cs.p1[4 * i + 3]);
+        }
+        p0_.upload(p0, s);
+        p1_.upload(p1, s);
+    }
+    lab_.upload(cs.labels, s);
+    slot_.alloc(n);
+    perm_.alloc(np);
+    {
+        std::vector<int32_t> id(np);
+        for (int64_t k = 0; k < np; ++k) id[k] = k < n ? (int32_t)k : -1;
+        perm_.upload(id, s);
+    }
+    xs_.alloc(np); p0s_.alloc(np); p1s_.alloc(np); labs_.alloc(np);
+    bb_c_.alloc(nc); bb_h_.alloc(nc);
+    tile_count_.alloc(nc); tile_start_.alloc(nc + 1);
+    tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, std::max<int64_t>(4096, nc * 48));
+    tile_j_.alloc(tile_cap_); tile_mask_.alloc(tile_cap_);
+    mask_cap_ = std::max<int64_t>(256, std::min<int64_t>(tile_cap_, nc * 8));
+    masks_.alloc(mask_cap_ * 128);
+    mask_count_.alloc(1);
+
+    if (reorder) {
+        // Cells of ~1 nm tiling the box; visiting order = Morton rank.
+        for (int a = 0; a < 3; ++a)
+            cell_dims_[a] = (int)std::max(1.0, std::min(1023.0, std::floor(cs.box[a] / 1.0)));
+        n_cells_ = (int64_t)cell_dims_[0] * cell_dims_[1] * cell_dims_[2];
+        std::vector<std::pair<uint32_t, uint32_t>> codes(n_cells_);
+        for (int cz = 0; cz < cell_dims_[2]; ++cz)
+            for (int cy = 0; cy < cell_dims_[1]; ++cy)
+                for (int cx = 0; cx < cell_dims_[0]; ++cx) {
+                    const uint32_t c = (uint32_t)((cz * cell_dims_[1] + cy) * cell_dims_[0] + cx);
+                    codes[c] = {morton3(cx, cy, cz), c};
+                }
+        std::sort(codes.begin(), codes.end());
+        std::vector<uint32_t> rank(n_cells_);
+        for (int64_t k = 0; k < n_cells_; ++k) rank[codes[k].second] = (uint32_t)k;
+        cell_rank_.upload(rank, s);
+        cell_key_.alloc(n);
+        cell_count_.alloc(n_cells_);
+        cell_start_.alloc(n_cells_ + 1);
+        cell_fill_.alloc(n_cells_);
+        bucket_.alloc(n);
+    }
+    // exclusions (CSR -> flat (i, j, bits))
+    {
+        std::vector<int32_t> ei(cs.ex_j.size());
+        for (int64_t i = 0; i < n; ++i)
+            for (int32_t e = cs.ex_start[i]; e < cs.ex_start[i + 1]; ++e) ei[e] = (int32_t)i;
+        ex_start_.upload(ei, s);  // row index of each entry
+        ex_j_.upload(cs.ex_j, s);
+        ex_bits_.upload(cs.ex_bits, s);
+    }
+    bonds_.upload(cs.bonds, s);
+    angles_.upload(cs.angles, s);
+    dihedrals_.upload(cs.dihedrals, s);
+    fla_.upload(cs.fla, s);
+    fld_.upload(cs.fld, s);
+    energy_.alloc(kNumSlots);
+    flags_.alloc(1);
+    OCM_CK(cudaMemsetAsync(flags_.p, 0, sizeof(int32_t), s));
+    maxdisp_.alloc(1);
+    step_base_.alloc(1);
+    OCM_CK(cudaMemsetAsync(step_base_.p, 0, sizeof(unsigned long long), s));
+    ke_.alloc(1);
+    sx_.alloc(n); sy_.alloc(n); sz_.alloc(n);
+    svx_.alloc(n); svy_.alloc(n); svz_.alloc(n);
+    sstep_.alloc(1);
+    OCM_CK(cudaStreamSynchronize(s));
+}
+
+PlainContext::~PlainContext() {
+    cudaSetDevice(device);
+    clear_graphs();
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (h_flags_) cudaFreeHost(h_flags_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void PlainContext::clear_graphs() {
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+}
+
+void PlainContext::check_positions_set() const {
+    if (!positions_set_) throw Error(5, "[error] positions have not been set");
+}
+
+void PlainContext::set_positions(const double* xyz) {
+    OCM_CK(cudaSetDevice(device));
+    std::vector<double> a(n), b(n), c(n);
+    for (int64_t i = 0; i < n; ++i) {
+        a[i] = xyz[3 * i];
+        b[i] = xyz[3 * i + 1];
+        c[i] = xyz[3 * i + 2];
+        if (!std::isfinite(a[i]) || !std::isfinite(b[i]) || !std::isfinite(c[i]))
+            throw Error(7, "[error] non-finite position for particle " + std::to_string(i));
+    }
+    x_.upload(a, stream_);
+    y_.upload(b, stream_);
+    z_.upload(c, stream_);
+    k_positions_to_float<<<div_up(n, 256), 256, 0, stream_>>>(
+        (int)n, x_.p, y_.p, z_.p, cs.periodic ? 1 : 0, cs.box[0], cs.box[1], cs.box[2],
+        cs.box[0] > 0 ? 1.0 / cs.box[0] : 0.0, cs.box[1] > 0 ? 1.0 / cs.box[1] : 0.0,
+        cs.box[2] > 0 ? 1.0 / cs.box[2] : 0.0, xq_.p);
+    OCM_CK(cudaGetLastError());
+    OCM_CK(cudaStreamSynchronize(stream_));
+    positions_set_ = true;
+}
+
+void PlainContext::get_positions(double* xyz) {
+    OCM_CK(cudaSetDevice(device));
+    check_positions_set();
+    std::vector<double> a(n), b(n), c(n);
+    OCM_CK(cudaMemcpyAsync(a.data(), x_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaMemcpyAsync(b.data(), y_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaMemcpyAsync(c.data(), z_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaStreamSynchronize(stream_));
+    for (int64_t i = 0; i < n; ++i) {
+        xyz[3 * i] = a[i];
+        xyz[3 * i + 1] = b[i];
+        xyz[3 * i + 2] = c[i];
+    }
+}
+
+void PlainContext::set_velocities(const double* v) {
+    OCM_CK(cudaSetDevice(device));
+    std::vector<float> a(n), b(n), c(n);
+    for (int64_t i = 0; i < n; ++i) {
+        a[i] = (float)v[3 * i];
+        b[i] = (float)v[3 * i + 1];
+        c[i] = (float)v[3 * i + 2];
+    }
+    vx_.upload(a, stream_);
+    vy_.upload(b, stream_);
+    vz_.upload(c, stream_);
+    OCM_CK(cudaStreamSynchronize(stream_));
+}
+
+void PlainContext::get_velocities(double* v) {
+    OCM_CK(cudaSetDevice(device));
+    std::vector<float> a(n), b(n), c(n);
+    OCM_CK(cudaMemcpyAsync(a.data(), vx_.p, n * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaMemcpyAsync(b.data(), vy_.p, n * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaMemcpyAsync(c.data(), vz_.p, n * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaStreamSynchronize(stream_));
+    for (int64_t i = 0; i < n; ++i) {
+        v[3 * i] = a[i];
+        v[3 * i + 1] = b[i];
+        v[3 * i + 2] = c[i];
+    }
+}
+
+void PlainContext::set_velocities_to_temperature(double temperature, int32_t seed) {
+    OCM_CK(cudaSetDevice(device));
+    const float kT = (float)(constant::boltz * temperature);
+    k_velocity_init<<<div_up(n, 256), 256, 0, stream_>>>((int)n, invm_.p, kT, (uint32_t)seed, 1u,
+                                                         vx_.p, vy_.p, vz_.p);
+    OCM_CK(cudaGetLastError());
+    OCM_CK(cudaStreamSynchronize(stream_));
+}
+
+double PlainContext::kinetic_energy() {
+    OCM_CK(cudaSetDevice(device));
+    OCM_CK(cudaMemsetAsync(ke_.p, 0, sizeof(double), stream_));
+    k_kinetic<<<div_up(n, 256), 256, 0, stream_>>>((int)n, invm_.p, vx_.p, vy_.p, vz_.p, ke_.p);
+    OCM_CK(cudaGetLastError());
+    double ke = 0;
+    OCM_CK(cudaMemcpyAsync(&ke, ke_.p, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaStreamSynchronize(stream_));
+    return ke;
+}
+
+void PlainContext::rebuild(cudaStream_t s) {
+    const int np_i = (int)np, n_i = (int)n, nc_i = (int)nc;
+    if (reorder) {
+        OCM_CK(cudaMemsetAsync(cell_count_.p, 0, n_cells_ * sizeof(int32_t), s));
+        OCM_CK(cudaMemsetAsync(cell_fill_.p, 0, n_cells_ * sizeof(int32_t), s));
+        k_cell_keys<<<div_up(n, 256), 256, 0, s>>>(n_i, xq_.p, cell_dims_[0], cell_dims_[1],
+                                                   cell_dims_[2], box_, cell_rank_.p, cell_key_.p,
+                                                   cell_count_.p);
+        k_scan<<<1, 1024, 0, s>>>((int)n_cells_, cell_count_.p, cell_start_.p);
+        k_bucket_scatter<<<div_up(n, 256), 256, 0, s>>>(n_i, cell_key_.p, cell_start_.p,
+                                                        cell_fill_.p, bucket_.p);
+        k_bucket_sort<<<div_up(n_cells_, 128), 128, 0, s>>>((int)n_cells_, cell_start_.p,
+                                                           bucket_.p, perm_.p);
+    }
+    k_gather_sorted<<<div_up(np, 256), 256, 0, s>>>(np_i, perm_.p, xq_.p, p0_.p, p1_.p, lab_.p,
+                                                    slot_.p, xs_.p, p0s_.p, p1s_.p, labs_.p,
+                                                    ref_.p, maxdisp_.p);
+    const bool per = cs.periodic;
+    const int wblocks = div_up(nc * 32, 128);
+    if (per) k_bbox<true><<<wblocks, 128, 0, s>>>(nc_i, xs_.p, perm_.p, box_, inv_box_, bb_c_.p, bb_h_.p);
+    else k_bbox<false><<<wblocks, 128, 0, s>>>(nc_i, xs_.p, perm_.p, box_, inv_box_, bb_c_.p, bb_h_.p);
+    const float cut = (float)(cs.max_cutoff + skin) * 1.0001f + 1e-4f;
+    const float cut2 = cut * cut;
+    if (per) {
+        k_tiles<true, false><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2,
+                                                     tile_count_.p, nullptr, nullptr, nullptr, 0,
+                                                     flags_.p);
+    } else {
+        k_tiles<false, false><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut,
+                                                      cut2, tile_count_.p, nullptr, nullptr, nullptr,
+                                                      0, flags_.p);
+    }
+    k_scan<<<1, 1024, 0, s>>>(nc_i, tile_count_.p, tile_start_.p);
+    if (per) {
+        k_tiles<true, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2,
+                                                    nullptr, tile_start_.p, tile_j_.p, tile_mask_.p,
+                                                    (int)tile_cap_, flags_.p);
+    } else {
+        k_tiles<false, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut,
+                                                     cut2, nullptr, tile_start_.p, tile_j_.p,
+                                                     tile_mask_.p, (int)tile_cap_, flags_.p);
+    }
+    const int nnz = (int)cs.ex_j.size();
+    OCM_CK(cudaMemsetAsync(mask_count_.p, 0, sizeof(int32_t), s));
+    if (nnz > 0) {
+        k_excl<false><<<div_up(nnz, 256), 256, 0, s>>>(nnz, nc_i, (int)tile_cap_, ex_start_.p, ex_j_.p, ex_bits_.p, slot_.p,
+                                                        tile_start_.p, tile_j_.p, tile_mask_.p,
+                                                        masks_.p, mask_count_.p, (int)mask_cap_,
+                                                        flags_.p);
+        k_excl<true><<<div_up(nnz, 256), 256, 0, s>>>(nnz, nc_i, (int)tile_cap_, ex_start_.p, ex_j_.p, ex_bits_.p, slot_.p,
+                                                       tile_start_.p, tile_j_.p, tile_mask_.p,
+                                                       masks_.p, mask_count_.p, (int)mask_cap_,
+                                                       flags_.p);
+    }
+    OCM_CK(cudaGetLastError());
+}
+
+void PlainContext::launch_forces(cudaStream_t s, bool energy, uint32_t slots_enabled, int) {
+    ForceArgs a{};
+    a.nc = (int)nc;
+    a.tile_cap = (int)tile_cap_;
+    a.n = (int)n;
+    a.blocks_tiles = div_up(nc, kWarpsPerForceBlock);
+    a.n_bonds = (int)cs.bonds.size();
+    a.n_angles = (int)cs.angles.size();
+    a.n_dih = (int)cs.dihedrals.size();
+    a.blocks_bonds = div_up(a.n_bonds, kForceThreads);
+    a.blocks_angles = div_up(a.n_angles, kForceThreads);
+    a.blocks_dih = div_up(a.n_dih, kForceThreads);
+    a.xs = xs_.p; a.p0s = p0s_.p; a.p1s = p1s_.p; a.labs = labs_.p; a.perm = perm_.p;
+    a.tile_start = tile_start_.p; a.tile_j = tile_j_.p; a.tile_mask = tile_mask_.p;
+    a.masks = masks_.p;
+    a.x = x_.p; a.y = y_.p; a.z = z_.p;
+    a.bonds = bonds_.p; a.angles = angles_.p; a.fla = fla_.p; a.dih = dihedrals_.p; a.fld = fld_.p;
+    a.F = F_.p;
+    a.pc = cs.pc;
+    a.box = box_;
+    a.inv_box = inv_box_;
+    a.slots_enabled = slots_enabled;
+    uint32_t excl_all = 0;
+    const int pair_slots[4] = {kSlotEXV, kSlotDH, kSlotLJR, kSlotLJA};
+    for (int t = 0; t < 4; ++t)
+        if (!(slots_enabled & (1u << pair_slots[t]))) excl_all |= 1u << t;
+    a.excl_all = excl_all;
+    a.energy = energy_.p;
+    int blocks_tiles = a.blocks_tiles;
+    if ((cs.pc.terms & ~excl_all & 15) == 0) {
+        a.blocks_tiles = 0;
+        blocks_tiles = 0;
+    }
+    const int grid = blocks_tiles + a.blocks_bonds + a.blocks_angles + a.blocks_dih;
+    if (grid == 0) return;
+    const int terms = cs.pc.terms;
+    const bool per = cs.periodic;
+    if ((terms & ~(kTermEXV | kTermDH)) == 0) launch_forces_t<kTermEXV | kTermDH>(a, grid, s, per, energy);
+    else if ((terms & ~(kTermLJR | kTermLJA | kTermDH)) == 0)
+        launch_forces_t<kTermLJR | kTermLJA | kTermDH>(a, grid, s, per, energy);
+    else launch_forces_t<15>(a, grid, s, per, energy);
+    OCM_CK(cudaGetLastError());
+}
+
+void PlainContext::launch_integrate(cudaStream_t s, int r) {
+    IntegrateArgs a{};
+    a.n = (int)n;
+    a.F = F_.p;
+    a.vx = vx_.p; a.vy = vy_.p; a.vz = vz_.p;
+    a.x = x_.p; a.y = y_.p; a.z = z_.p;
+    a.invm = invm_.p;
+    a.xq = xq_.p; a.xs = xs_.p; a.slot = slot_.p; a.ref = ref_.p;
+    a.lc = lc_;
+    a.step_base = step_base_.p;
+    a.r = r;
+    a.periodic = cs.periodic ? 1 : 0;
+    for (int k = 0; k < 3; ++k) {
+        a.box[k] = cs.box[k];
+        a.inv_box[k] = cs.box[k] > 0 ? 1.0 / cs.box[k] : 0.0;
+    }
+    a.fbox = box_;
+    a.finv_box = inv_box_;
+    const float half = (float)(0.5 * skin);
+    a.disp_limit2 = half * half;
+    a.maxdisp = maxdisp_.p;
+    a.flags = flags_.p;
+    k_integrate<<<div_up(n, 256), 256, 0, s>>>(a);
+    OCM_CK(cudaGetLastError());
+}
+
+void PlainContext::ensure_capacity() {
+    // Build once eagerly, read the sizes back and grow the buffers if needed.
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        OCM_CK(cudaMemsetAsync(flags_.p, 0, sizeof(int32_t), stream_));
+        rebuild(stream_);
+        int32_t total = 0, masks = 0, flags = 0;
+        OCM_CK(cudaMemcpyAsync(&total, tile_start_.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
+        OCM_CK(cudaMemcpyAsync(&masks, mask_count_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
+        OCM_CK(cudaMemcpyAsync(&flags, flags_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
+        OCM_CK(cudaStreamSynchronize(stream_));
+        bool grown = false;
+        if (total > tile_cap_ || (int64_t)total * 5 / 4 + 64 > tile_cap_) {
+            const int64_t want = std::min<int64_t>(nc * (nc + 1) / 2, (int64_t)total * 2 + 1024);
+            if (want > tile_cap_) {
+                tile_cap_ = want;
+                tile_j_.alloc(tile_cap_);
+                tile_mask_.alloc(tile_cap_);
+                grown = total > 0;
+                clear_graphs();
+            }
+        }
+        if (masks > mask_cap_ || (int64_t)masks * 5 / 4 + 16 > mask_cap_) {
+            const int64_t want = std::min<int64_t>(tile_cap_, (int64_t)masks * 2 + 256);
+            if (want > mask_cap_) {
+                mask_cap_ = want;
+                masks_.alloc(mask_cap_ * 128);
+                clear_graphs();
+            }
+        }
+        if (!(flags & (ListFlags::kTileOverflow | ListFlags::kMaskOverflow)) && total <= tile_cap_ &&
+            masks <= mask_cap_) {
+            tiles_last = total;
+            masked_last = masks;
+            list_builds++;
+            return;
+        }
+        (void)grown;
+    }
+    throw Error(4, "[error] tile list capacity could not be established");
+}
+
+uint32_t PlainContext::slots_for_groups(uint32_t groups) const {
+    uint32_t s = 0;
+    for (int k = 0; k < kNumSlots; ++k)
+        if (cs.slot_group[k] >= 0 && (groups >> cs.slot_group[k]) & 1u) s |= 1u << k;
+    return s;
+}
+
+void PlainContext::eval(uint32_t groups, bool energy, double* forces, double* slot_energy) {
+    OCM_CK(cudaSetDevice(device));
+    check_positions_set();
+    ensure_capacity();
+    OCM_CK(cudaMemsetAsync(energy_.p, 0, kNumSlots * sizeof(double), stream_));
+    OCM_CK(cudaMemsetAsync(F_.p, 0, 3 * n * sizeof(unsigned long long), stream_));
+    launch_forces(stream_, energy, slots_for_groups(groups), 0);
+    std::vector<unsigned long long> f;
+    if (forces) {
+        f.resize(3 * n);
+        OCM_CK(cudaMemcpyAsync(f.data(), F_.p, 3 * n * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, stream_));
+    }
+    double e[kNumSlots];
+    OCM_CK(cudaMemcpyAsync(e, energy_.p, sizeof(e), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaMemsetAsync(F_.p, 0, 3 * n * sizeof(unsigned long long), stream_));
+    OCM_CK(cudaStreamSynchronize(stream_));
+    if (forces)
+        for (int64_t i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c)
+                forces[3 * i + c] = (double)(long long)f[c * n + i] * kFixedInv;
+    if (slot_energy)
+        for (int k = 0; k < kNumSlots; ++k) slot_energy[k] = e[k];
+}
+
+void PlainContext::get_state(uint32_t groups, double* forces, double* energy) {
+    double se[kNumSlots];
+    eval(groups, energy != nullptr, forces, se);
+    if (energy) {
+        double tot = 0;
+        for (int k = 0; k < kNumSlots; ++k)
+            if (cs.slot_group[k] >= 0 && ((groups >> cs.slot_group[k]) & 1u)) tot += se[k];
+        *energy = tot;
+    }
+}
+
+void PlainContext::group_energies(double* e32) {
+    double se[kNumSlots];
+    eval(0xffffffffu, true, nullptr, se);
+    for (int g = 0; g < 32; ++g) e32[g] = 0.0;
+    for (int k = 0; k < kNumSlots; ++k)
+        if (cs.slot_group[k] >= 0) e32[cs.slot_group[k]] += se[k];
+}
+
+cudaGraphExec_t PlainContext::graph_for(int chunk) {
+    auto it = graphs_.find(chunk);
+    if (it != graphs_.end()) return it->second;
+    cudaGraph_t g;
+    OCM_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    try {
+        rebuild(stream_);
+        const uint32_t all = slots_for_groups(0xffffffffu);
+        for (int r = 0; r < chunk; ++r) {
+            launch_forces(stream_, false, all, r);
+            launch_integrate(stream_, r);
+        }
+        k_advance<<<1, 1, 0, stream_>>>(step_base_.p, chunk);
+    } catch (...) {
+        cudaStreamEndCapture(stream_, &g);
+        throw;
+    }
+    OCM_CK(cudaStreamEndCapture(stream_, &g));
+    cudaGraphExec_t exec;
+    OCM_CK(cudaGraphInstantiate(&exec, g, 0));
+    cudaGraphDestroy(g);
+    graphs_[chunk] = exec;
+    return exec;
+}
+
+void PlainContext::step(int64_t nsteps) {
+    OCM_CK(cudaSetDevice(device));
+    check_positions_set();
+    if (nsteps < 0) throw Error(1, "[error] negative step count");
+    if (nsteps == 0) return;
+    if (graphs_.empty()) ensure_capacity();
+    for (int attempt = 0; attempt < 12; ++attempt) {
+        cudaStream_t s = stream_;
+        OCM_CK(cudaMemcpyAsync(sx_.p, x_.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(sy_.p, y_.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(sz_.p, z_.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(svx_.p, vx_.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(svy_.p, vy_.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(svz_.p, vz_.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(sstep_.p, step_base_.p, sizeof(unsigned long long),
+                               cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemsetAsync(flags_.p, 0, sizeof(int32_t), s));
+        int64_t left = nsteps;
+        int64_t launches = 0;
+        while (left > 0) {
+            const int chunk = (int)std::min<int64_t>(left, rebuild_interval);
+            OCM_CK(cudaGraphLaunch(graph_for(chunk), s));
+            left -= chunk;
+            launches++;
+        }
+        OCM_CK(cudaMemcpyAsync(h_flags_, flags_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        OCM_CK(cudaStreamSynchronize(s));
+        const int32_t flags = h_flags_[0];
+        if (flags == 0) {
+            steps_done += nsteps;
+            list_builds += launches;
+            return;
+        }
+        // restore and retry with more capacity / more frequent rebuilds
+        OCM_CK(cudaMemcpyAsync(x_.p, sx_.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(y_.p, sy_.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(z_.p, sz_.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(vx_.p, svx_.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(vy_.p, svy_.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(vz_.p, svz_.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemcpyAsync(step_base_.p, sstep_.p, sizeof(unsigned long long),
+                               cudaMemcpyDeviceToDevice, s));
+        OCM_CK(cudaMemsetAsync(F_.p, 0, 3 * n * sizeof(unsigned long long), s));
+        k_positions_to_float<<<div_up(n, 256), 256, 0, s>>>(
+            (int)n, x_.p, y_.p, z_.p, cs.periodic ? 1 : 0, cs.box[0], cs.box[1], cs.box[2],
+            cs.box[0] > 0 ? 1.0 / cs.box[0] : 0.0, cs.box[1] > 0 ? 1.0 / cs.box[1] : 0.0,
+            cs.box[2] > 0 ? 1.0 / cs.box[2] : 0.0, xq_.p);
+        OCM_CK(cudaStreamSynchronize(s));
+        if (flags & ListFlags::kSkinViolation) {
+            if (rebuild_interval == 1)
+                throw Error(7, "[error] particles moved more than half the skin in one step");
+            rebuild_interval = std::max(1, rebuild_interval / 2);
+        }
+        if (flags & (ListFlags::kTileOverflow | ListFlags::kMaskOverflow)) {
+            tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, tile_cap_ * 2);
+            tile_j_.alloc(tile_cap_);
+            tile_mask_.alloc(tile_cap_);
+            mask_cap_ = std::min<int64_t>(tile_cap_, mask_cap_ * 2);
+            masks_.alloc(mask_cap_ * 128);
+        }
+        clear_graphs();
+        ensure_capacity();
+    }
+    throw Error(4, "[error] step could not complete after repeated list rebuilds");
+}
+
+void PlainContext::set_list_options(int32_t interval, double sk) {
+    if (interval < 0 || sk < 0) throw Error(1, "[error] invalid list options");
+    if (interval > 0) rebuild_interval = interval;
+    if (sk > 0) skin = sk;
+    clear_graphs();
+}
+
+void PlainContext::list_pairs(int64_t* out, int64_t cap, int64_t* n_out) {
+    OCM_CK(cudaSetDevice(device));
+    check_positions_set();
+    ensure_capacity();
+    DevBuf<long long> buf;
+    buf.alloc(std::max<int64_t>(1, 2 * cap));
+    DevBuf<unsigned long long> cnt;
+    cnt.alloc(1);
+    OCM_CK(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), stream_));
+    const int wblocks = div_up(nc * 32, 128);
+    if (cs.periodic)
+        k_list_pairs<true><<<wblocks, 128, 0, stream_>>>((int)nc, xs_.p, perm_.p, tile_start_.p,
+                                                        tile_j_.p, box_, inv_box_, cs.pc.list_rc2,
+                                                        buf.p, cap, cnt.p, tile_cap_);
+    else
+        k_list_pairs<false><<<wblocks, 128, 0, stream_>>>((int)nc, xs_.p, perm_.p, tile_start_.p,
+                                                         tile_j_.p, box_, inv_box_, cs.pc.list_rc2,
+                                                         buf.p, cap, cnt.p, tile_cap_);
+    OCM_CK(cudaGetLastError());
+    unsigned long long c = 0;
+    OCM_CK(cudaMemcpyAsync(&c, cnt.p, sizeof(c), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaStreamSynchronize(stream_));
+    *n_out = (int64_t)c;
+    if ((int64_t)c > cap) throw Error(1, "[error] output capacity too small");
+    OCM_CK(cudaMemcpy(out, buf.p, 2 * c * sizeof(long long), cudaMemcpyDeviceToHost));
+}
+
+void PlainContext::cluster_order(int64_t* out, int64_t cap, int64_t* n_out) {
+    OCM_CK(cudaSetDevice(device));
+    check_positions_set();
+    ensure_capacity();
+    *n_out = np;
+    if (cap < np) throw Error(1, "[error] output capacity too small");
+    std::vector<int32_t> p(np);
+    OCM_CK(cudaMemcpy(p.data(), perm_.p, np * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    for (int64_t k = 0; k < np; ++k) out[k] = p[k];
+}
+
+}  // namespace ocm

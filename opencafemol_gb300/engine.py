@@ -1,0 +1,187 @@
+"""Device engines behind the C ABI.
+
+``Context`` is the plain single-system path: the part of an OpenMM
+``Context`` + ``LangevinIntegrator`` that the reference's ``Simulator``
+drives (src/Simulator.cpp:17-76).  ``Batch`` is the batched / served path:
+many independent systems advanced by one persistent kernel per chunk.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import OCM_MAX_GROUPS, ContextStats, OCMError, as_f64, check, dptr, i64ptr, lib
+from .forcefield import LangevinIntegrator, System
+
+__all__ = ["Context", "Batch", "ALL_GROUPS"]
+
+ALL_GROUPS = 0xFFFFFFFF
+
+
+class Context:
+    def __init__(self, system: System, integrator: LangevinIntegrator, device: int = 0):
+        self.system = system  # keeps the system alive
+        self.n = system.n
+        h = C.c_void_p()
+        check(lib.ocm_context_create(system.handle, integrator.temperature, integrator.friction,
+                                     integrator.step_size, integrator.seed, int(device), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.ocm_context_destroy(h)
+            self._h = None
+
+    def setPositions(self, xyz) -> None:
+        a = as_f64(xyz).reshape(self.n, 3)
+        check(lib.ocm_context_set_positions(self._h, dptr(a)))
+
+    def getPositions(self) -> np.ndarray:
+        a = np.zeros((self.n, 3))
+        check(lib.ocm_context_get_positions(self._h, dptr(a)))
+        return a
+
+    def setVelocities(self, v) -> None:
+        a = as_f64(v).reshape(self.n, 3)
+        check(lib.ocm_context_set_velocities(self._h, dptr(a)))
+
+    def getVelocities(self) -> np.ndarray:
+        a = np.zeros((self.n, 3))
+        check(lib.ocm_context_get_velocities(self._h, dptr(a)))
+        return a
+
+    def setVelocitiesToTemperature(self, temperature: float, seed: int) -> None:
+        check(lib.ocm_context_set_velocities_to_temperature(self._h, float(temperature), int(seed)))
+
+    def getState(self, forces: bool = True, energy: bool = True, groups: int = ALL_GROUPS):
+        """Return (forces [n,3] kJ/mol/nm or None, potential energy kJ/mol or None)."""
+        f = np.zeros((self.n, 3)) if forces else None
+        e = C.c_double()
+        check(lib.ocm_context_get_state(self._h, C.c_uint32(groups), dptr(f),
+                                        C.byref(e) if energy else None))
+        return f, (e.value if energy else None)
+
+    def getGroupEnergies(self) -> np.ndarray:
+        e = np.zeros(OCM_MAX_GROUPS)
+        check(lib.ocm_context_get_group_energies(self._h, dptr(e)))
+        return e
+
+    def getKineticEnergy(self) -> float:
+        e = C.c_double()
+        check(lib.ocm_context_get_kinetic_energy(self._h, C.byref(e)))
+        return e.value
+
+    def step(self, steps: int) -> None:
+        check(lib.ocm_context_step(self._h, int(steps)))
+
+    def stats(self) -> dict:
+        s = ContextStats()
+        check(lib.ocm_context_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in ContextStats._fields_}
+
+    def set_list_options(self, rebuild_interval: int = 0, skin: float = 0.0) -> None:
+        check(lib.ocm_context_set_list_options(self._h, int(rebuild_interval), float(skin)))
+
+    def list_pairs(self) -> np.ndarray:
+        n = C.c_int64()
+        cap = max(1024, self.n * 64)
+        while True:
+            out = np.zeros((cap, 2), np.int64)
+            try:
+                check(lib.ocm_context_list_pairs(self._h, i64ptr(out), cap, C.byref(n)))
+                return out[: n.value].copy()
+            except OCMError:
+                if n.value > cap:
+                    cap = n.value
+                    continue
+                raise
+
+    def cluster_order(self) -> np.ndarray:
+        n = C.c_int64()
+        cap = self.n + 64
+        out = np.zeros(cap, np.int64)
+        check(lib.ocm_context_cluster_order(self._h, i64ptr(out), cap, C.byref(n)))
+        return out[: n.value].copy()
+
+
+class Batch:
+    """Device-resident ensemble of independent systems."""
+
+    def __init__(self, max_systems: int, max_total_beads: int, max_beads_per_system: int,
+                 device: int = 0):
+        h = C.c_void_p()
+        check(lib.ocm_batch_create(int(device), int(max_systems), int(max_total_beads),
+                                   int(max_beads_per_system), C.byref(h)))
+        self._h = h
+        self._n: dict[int, int] = {}
+        self._systems: dict[int, System] = {}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.ocm_batch_destroy(h)
+            self._h = None
+
+    @staticmethod
+    def footprint(system: System) -> int:
+        return system.footprint()
+
+    def admit(self, system: System, positions, velocities=None, temperature: float = 300.0,
+              friction: float = 0.1, step_size: float = 0.01, seed: int = 0, n_steps: int = 0) -> int:
+        pos = as_f64(positions).reshape(system.n, 3)
+        vel = None if velocities is None else as_f64(velocities).reshape(system.n, 3)
+        slot = C.c_int64()
+        check(lib.ocm_batch_admit(self._h, system.handle, dptr(pos), dptr(vel), float(temperature),
+                                  float(friction), float(step_size), int(seed), int(n_steps),
+                                  C.byref(slot)))
+        self._n[slot.value] = system.n
+        self._systems[slot.value] = system
+        return slot.value
+
+    def run(self, steps_per_launch: int, sync: bool = False) -> None:
+        check(lib.ocm_batch_run(self._h, int(steps_per_launch), int(sync)))
+
+    def finished(self) -> list[int]:
+        n = C.c_int64()
+        cap = max(1, len(self._n))
+        out = np.zeros(cap, np.int64)
+        check(lib.ocm_batch_finished(self._h, i64ptr(out), cap, C.byref(n)))
+        return [int(v) for v in out[: min(n.value, cap)]]
+
+    def positions(self, slot: int) -> np.ndarray:
+        a = np.zeros((self._n[slot], 3))
+        check(lib.ocm_batch_get_positions(self._h, int(slot), dptr(a)))
+        return a
+
+    def velocities(self, slot: int) -> np.ndarray:
+        a = np.zeros((self._n[slot], 3))
+        check(lib.ocm_batch_get_velocities(self._h, int(slot), dptr(a)))
+        return a
+
+    def steps_done(self, slot: int) -> int:
+        s = C.c_int64()
+        check(lib.ocm_batch_steps_done(self._h, int(slot), C.byref(s)))
+        return s.value
+
+    def state(self, slot: int, groups: int = ALL_GROUPS):
+        f = np.zeros((self._n[slot], 3))
+        e = np.zeros(OCM_MAX_GROUPS)
+        check(lib.ocm_batch_get_state(self._h, int(slot), C.c_uint32(groups), dptr(f), dptr(e)))
+        return f, e
+
+    def retire(self, slot: int) -> None:
+        check(lib.ocm_batch_retire(self._h, int(slot)))
+        self._n.pop(slot, None)
+        self._systems.pop(slot, None)
+
+    def active(self) -> tuple[int, int]:
+        a, b = C.c_int64(), C.c_int64()
+        check(lib.ocm_batch_active(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def last_run_ms(self) -> float:
+        ms = C.c_double()
+        check(lib.ocm_batch_last_run_ms(self._h, C.byref(ms)))
+        return ms.value

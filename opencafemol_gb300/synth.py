@@ -1,0 +1,354 @@
+"""Seeded synthetic coarse-grained systems with the shapes of the benchmark
+configurations, and their assembly through the reference-named generators.
+
+No public dataset is involved: every system here is generated from a seed.
+* Go-model protein: one chain of N beads from a self-avoiding random walk
+  with 0.38 nm bonds; Go contacts on native pairs within 0.65 nm with
+  |i-j| > 3 (eps ~ U[0.2, 1.0] kcal/mol); FLA/FLD from a random amino-acid
+  sequence; EXV radius ~ U[0.2, 0.4] nm with a 2.0 nm cutoff; charges +-1 on
+  25 % of beads with a 2.0 nm Debye-Hueckel cutoff; residue masses.
+* HPS condensate slab: chains of 20 bead types (sigma ~ U[0.45, 0.75] nm,
+  lambda ~ U[0, 1]) packed into the central slab of a periodic box; HPS
+  Lennard-Jones with a 2.0 nm cutoff, Debye-Hueckel with 3.5 nm on 20 %
+  charged beads, k = 10 kcal/mol/A^2 bonds.
+Positions are rounded to FP32-representable values so the FP64 oracle and
+the FP32 kernels see identical coordinates.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .forcefield import (AMINO_ACIDS, DebyeHuckelForceFieldGenerator,
+                         ExcludedVolumeForceFieldGenerator, FlexibleLocalAngleForceFieldGenerator,
+                         FlexibleLocalDihedralForceFieldGenerator, GoContactForceFieldGenerator,
+                         HarmonicBondForceFieldGenerator, LennardJonesAttractiveForceFieldGenerator,
+                         LennardJonesRepulsiveForceFieldGenerator, System, SystemGenerator,
+                         Topology, fla_spline_table, fld_fourier_table, fld_table_keys)
+
+KJ_PER_KCAL = 4.184
+ANGSTROM_PER_NM = 10.0
+BOLTZ = 0.00831446261815324  # kJ/mol/K
+
+# Average residue masses (amu) of the 20 amino acids, AMINO_ACIDS order.
+RESIDUE_MASS = np.array([71.08, 156.19, 114.10, 115.09, 103.14, 128.13, 129.12, 57.05, 137.14,
+                         113.16, 113.16, 128.17, 131.19, 147.18, 97.12, 87.08, 101.10, 186.21,
+                         163.18, 99.13])
+
+
+@dataclass
+class PairTerm:
+    ratio: float
+    p0: np.ndarray                     # radius / charge / epsilon (NaN = absent)
+    p1: np.ndarray | None = None       # sigma for LJ terms
+    eps: float = 0.0                   # EXV epsilon (kJ/mol)
+    ionic_strength: float = 0.15
+    temperature: float = 300.0
+    ign_bond: int = -1                 # exclusions within this many bonds (-1: none)
+    ign_contact: int = -1              # exclusions within this many contacts
+
+
+@dataclass
+class CGSpec:
+    n: int
+    pos: np.ndarray
+    masses: np.ndarray
+    periodic: bool = False
+    box: tuple | None = None
+    bonds: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int64))
+    bond_v0: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    bond_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    contacts: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int64))
+    go_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    go_r0: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    fla_idx: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int64))
+    fla_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    fla_aa: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    fld_idx: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.int64))
+    fld_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    fld_aa1: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    fld_aa2: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    exv: PairTerm | None = None
+    dh: PairTerm | None = None
+    ljr: PairTerm | None = None
+    lja: PairTerm | None = None
+    temperature: float = 300.0
+    friction: float = 0.1
+    dt: float = 0.01
+
+
+def debye_length(temperature: float, ionic_strength: float) -> float:
+    """Debye length (nm) by the reference's formula (DebyeHuckelForceFieldGenerator.cpp:22-43)."""
+    eps_r = DebyeHuckelForceFieldGenerator.dielectric_water(temperature, ionic_strength)
+    na, kb, e = 6.02214076e23, 1.380649e-23, 1.6021766208e-19
+    eps0 = 8.854187817e-12 * 1.0e3 * 1.0e-9 / na / e / e
+    return math.sqrt((eps0 * eps_r * kb * 1.0e-3 * temperature) / (2.0 * ionic_strength * 1.0e-24))
+
+
+def _f32(a: np.ndarray) -> np.ndarray:
+    return np.asarray(a, np.float32).astype(np.float64)
+
+
+def _orthonormal(b: np.ndarray):
+    t = np.array([1.0, 0.0, 0.0]) if abs(b[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+    u = np.cross(b, t)
+    u /= np.linalg.norm(u)
+    return u, np.cross(b, u)
+
+
+def saw_chain(n: int, rng: np.random.Generator, bond: float = 0.38, min_dist: float = 0.45,
+              theta=(1.75, 2.6)) -> np.ndarray:
+    """Self-avoiding random walk: bond angles in `theta` (rad), beads at least
+    `min_dist` from every earlier non-adjacent bead."""
+    for _attempt in range(100):
+        x = np.zeros((n, 3))
+        if n > 1:
+            d = rng.normal(size=3)
+            x[1] = bond * d / np.linalg.norm(d)
+        ok = True
+        for i in range(2, n):
+            b = x[i - 1] - x[i - 2]
+            b /= np.linalg.norm(b)
+            u, w = _orthonormal(b)
+            placed = False
+            for _try in range(200):
+                th = rng.uniform(*theta)
+                ph = rng.uniform(-math.pi, math.pi)
+                dvec = -math.cos(th) * b + math.sin(th) * (math.cos(ph) * u + math.sin(ph) * w)
+                cand = x[i - 1] + bond * dvec
+                if i >= 3:
+                    dd = np.min(np.sum((x[: i - 1] - cand) ** 2, axis=1))
+                    if dd < min_dist * min_dist:
+                        continue
+                x[i] = cand
+                placed = True
+                break
+            if not placed:
+                ok = False
+                break
+        if ok:
+            return x
+    raise RuntimeError("could not grow a self-avoiding chain")
+
+
+def go_protein(n: int, seed: int, temperature: float = 300.0, cutoff: float = 2.0,
+               charge_fraction: float = 0.25, ionic_strength: float = 0.15,
+               exv_eps_kcal: float = 0.6, contact_cutoff: float = 0.65) -> CGSpec:
+    rng = np.random.default_rng(seed)
+    seq = rng.integers(0, 20, n).astype(np.int32)
+    pos = _f32(saw_chain(n, rng))
+    s = CGSpec(n=n, pos=pos, masses=RESIDUE_MASS[seq].copy(), temperature=temperature)
+    s.bonds = np.stack([np.arange(n - 1), np.arange(1, n)], 1).astype(np.int64)
+    s.bond_v0 = np.linalg.norm(pos[1:] - pos[:-1], axis=1)
+    s.bond_k = np.full(n - 1, 110.0 * KJ_PER_KCAL * ANGSTROM_PER_NM ** 2 * 2.0)
+    d = np.linalg.norm(pos[:, None, :] - pos[None, :, :], axis=2)
+    ii, jj = np.nonzero(np.triu(d < contact_cutoff, k=4))
+    s.contacts = np.stack([ii, jj], 1).astype(np.int64)
+    s.go_k = rng.uniform(0.2, 1.0, len(ii)) * KJ_PER_KCAL
+    s.go_r0 = d[ii, jj]
+    if n >= 3:
+        c = np.arange(1, n - 1)
+        s.fla_idx = np.stack([c - 1, c, c + 1], 1).astype(np.int64)
+        s.fla_k = np.full(n - 2, 1.0 * KJ_PER_KCAL)
+        s.fla_aa = seq[c]
+    if n >= 4:
+        c = np.arange(1, n - 2)
+        s.fld_idx = np.stack([c - 1, c, c + 1, c + 2], 1).astype(np.int64)
+        s.fld_k = np.full(n - 3, 1.0 * KJ_PER_KCAL)
+        s.fld_aa1 = seq[c]
+        s.fld_aa2 = seq[c + 1]
+    radius = rng.uniform(0.2, 0.4, n)
+    top = np.sort(radius)[::-1]
+    s.exv = PairTerm(ratio=cutoff / (top[0] + top[1]), p0=radius, eps=exv_eps_kcal * KJ_PER_KCAL,
+                     ign_bond=3, ign_contact=1)
+    q = np.full(n, np.nan)
+    nq = max(2, int(round(charge_fraction * n)))
+    pick = rng.choice(n, nq, replace=False)
+    q[pick] = rng.choice([-1.0, 1.0], nq)
+    s.dh = PairTerm(ratio=cutoff / debye_length(temperature, ionic_strength), p0=q,
+                    ionic_strength=ionic_strength, temperature=temperature, ign_bond=3)
+    return s
+
+
+def hps_slab(n_chains: int, chain_len: int, box, slab_width: float, seed: int,
+             hps_cutoff: float = 2.0, dh_cutoff: float = 3.5, charge_fraction: float = 0.2,
+             ionic_strength: float = 0.15, temperature: float = 300.0,
+             min_dist: float = 0.5) -> CGSpec:
+    rng = np.random.default_rng(seed)
+    box = tuple(float(b) for b in box)
+    sig_t = rng.uniform(0.45, 0.75, 20)
+    lam_t = rng.uniform(0.0, 1.0, 20)
+    n = n_chains * chain_len
+    types = rng.integers(0, 20, n).astype(np.int32)
+    pos = np.zeros((n, 3))
+    # hash grid of placed beads for the overlap test
+    cell = min_dist
+    grid: dict[tuple, list[int]] = {}
+    L = np.array(box)
+    zlo, zhi = 0.5 * box[2] - 0.5 * slab_width, 0.5 * box[2] + 0.5 * slab_width
+
+    def key(p):
+        w = p - L * np.floor(p / L)
+        return tuple((w // cell).astype(int))
+
+    def clash(p):
+        k = key(p)
+        nc = np.maximum(1, (L // cell).astype(int))
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    kk = ((k[0] + dx) % nc[0], (k[1] + dy) % nc[1], (k[2] + dz) % nc[2])
+                    for j in grid.get(kk, ()):
+                        d = pos[j] - p
+                        d -= L * np.round(d / L)
+                        if d @ d < min_dist * min_dist:
+                            return True
+        return False
+
+    def put(i, p):
+        nc = np.maximum(1, (L // cell).astype(int))
+        k = key(p)
+        grid.setdefault((k[0] % nc[0], k[1] % nc[1], k[2] % nc[2]), []).append(i)
+        pos[i] = p
+
+    i = 0
+    for _c in range(n_chains):
+        for _try in range(1000):
+            p0 = np.array([rng.uniform(0, box[0]), rng.uniform(0, box[1]), rng.uniform(zlo, zhi)])
+            if not clash(p0):
+                break
+        put(i, p0)
+        i += 1
+        prev_b = None
+        for _k in range(1, chain_len):
+            placed = False
+            for _try in range(400):
+                if prev_b is None:
+                    dvec = rng.normal(size=3)
+                    dvec /= np.linalg.norm(dvec)
+                else:
+                    u, w = _orthonormal(prev_b)
+                    th = rng.uniform(1.75, 2.6)
+                    ph = rng.uniform(-math.pi, math.pi)
+                    dvec = -math.cos(th) * prev_b + math.sin(th) * (math.cos(ph) * u + math.sin(ph) * w)
+                cand = pos[i - 1] + 0.38 * dvec
+                if cand[2] < zlo or cand[2] > zhi:
+                    continue
+                if not clash(cand):
+                    placed = True
+                    break
+            if not placed:
+                cand = pos[i - 1] + 0.38 * dvec
+            put(i, cand)
+            prev_b = dvec
+            i += 1
+    pos = pos - L * np.floor(pos / L)
+    pos = _f32(pos)
+    pos = np.where(pos >= L, pos - L, pos)  # FP32 rounding may land exactly on L
+    s = CGSpec(n=n, pos=pos, masses=RESIDUE_MASS[types].copy(), periodic=True, box=box,
+               temperature=temperature)
+    starts = np.arange(n_chains) * chain_len
+    b0 = (starts[:, None] + np.arange(chain_len - 1)[None, :]).ravel()
+    s.bonds = np.stack([b0, b0 + 1], 1).astype(np.int64)
+    dv = pos[s.bonds[:, 1]] - pos[s.bonds[:, 0]]
+    dv -= L * np.round(dv / L)
+    s.bond_v0 = np.linalg.norm(dv, axis=1)
+    s.bond_k = np.full(len(b0), 10.0 * KJ_PER_KCAL * ANGSTROM_PER_NM ** 2 * 2.0)
+    sig = sig_t[types]
+    lj_ratio = hps_cutoff / (0.5 * (np.sort(sig)[-1] + np.sort(sig)[-2]))
+    s.ljr = PairTerm(ratio=lj_ratio, p0=np.full(n, 0.2 * KJ_PER_KCAL), p1=sig, ign_bond=1)
+    s.lja = PairTerm(ratio=lj_ratio, p0=0.2 * lam_t[types] * KJ_PER_KCAL, p1=sig, ign_bond=1)
+    q = np.full(n, np.nan)
+    nq = max(2, int(round(charge_fraction * n)))
+    pick = rng.choice(n, nq, replace=False)
+    q[pick] = rng.choice([-1.0, 1.0], nq)
+    s.dh = PairTerm(ratio=dh_cutoff / debye_length(temperature, ionic_strength), p0=q,
+                    ionic_strength=ionic_strength, temperature=temperature, ign_bond=3)
+    return s
+
+
+def ensemble_sizes(count: int, lo: int, hi: int, seed: int) -> np.ndarray:
+    """Bead counts log-uniform in [lo, hi] (seeded)."""
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi + 1), count))).astype(int).clip(lo, hi)
+
+
+def ensemble_temperatures(count: int, seed: int, lo: float = 280.0, hi: float = 360.0) -> np.ndarray:
+    return np.random.default_rng(seed + 7919).uniform(lo, hi, count)
+
+
+# ---------------------------------------------------------------------------
+def fld_selects(key: str, a1: str, a2: str) -> bool:
+    """Whether the reader assigns dihedral class `key` to a "a1-a2" coef
+    (ReadTOMLForceFieldGenerator.cpp:637-744)."""
+    first, second = key.split("-")
+    if second == "GLY":
+        return a2 == "GLY"
+    if second == "PRO":
+        return (a1 == "GLY" and a2 == "PRO") if first == "GLY" else a2 == "PRO"
+    return a2 not in ("GLY", "PRO") and a1 == first
+
+
+def _ignore(topo: Topology, bond: int, contact: int) -> np.ndarray:
+    parts = []
+    if bond >= 0:
+        parts.append(topo.ignore_list_within_edge(bond, "bond"))
+    if contact >= 0:
+        parts.append(topo.ignore_list_within_edge(contact, "contact"))
+    if not parts:
+        return np.zeros((0, 2), np.int64)
+    allp = np.concatenate(parts)
+    return np.unique(allp, axis=0) if len(allp) else allp
+
+
+def build_generator(spec: CGSpec) -> SystemGenerator:
+    """Assemble the spec in the order the TOML reader would (local forces,
+    then global pair forces), through the reference-named generators."""
+    per = spec.periodic
+    topo = Topology(spec.n)
+    if len(spec.bonds):
+        topo.add_edges(spec.bonds, "bond")
+    if len(spec.contacts):
+        topo.add_edges(spec.contacts, "contact")
+    sg = SystemGenerator(spec.masses)
+    if per:
+        sg.set_pbc(*spec.box)
+    if len(spec.bonds):
+        sg.add_ff_generator(HarmonicBondForceFieldGenerator(spec.bonds, spec.bond_v0, spec.bond_k, per))
+    if len(spec.contacts):
+        sg.add_ff_generator(GoContactForceFieldGenerator(spec.contacts, spec.go_k, spec.go_r0, per))
+    if len(spec.fla_idx):
+        for a, aa in enumerate(AMINO_ACIDS):
+            sel = spec.fla_aa == a
+            sg.add_ff_generator(FlexibleLocalAngleForceFieldGenerator(
+                spec.fla_idx[sel], spec.fla_k[sel], fla_spline_table(aa), aa, per))
+    if len(spec.fld_idx):
+        a1 = [AMINO_ACIDS[v] for v in spec.fld_aa1]
+        a2 = [AMINO_ACIDS[v] for v in spec.fld_aa2]
+        for key in fld_table_keys():
+            sel = np.array([fld_selects(key, x, y) for x, y in zip(a1, a2)], bool)
+            sg.add_ff_generator(FlexibleLocalDihedralForceFieldGenerator(
+                spec.fld_idx[sel], spec.fld_k[sel], fld_fourier_table(key), key, per))
+    if spec.exv is not None:
+        t = spec.exv
+        sg.add_ff_generator(ExcludedVolumeForceFieldGenerator(
+            t.eps, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact), per))
+    if spec.ljr is not None:
+        t = spec.ljr
+        sg.add_ff_generator(LennardJonesRepulsiveForceFieldGenerator(
+            t.ratio, t.p0, t.p1, _ignore(topo, t.ign_bond, t.ign_contact), per))
+    if spec.lja is not None:
+        t = spec.lja
+        sg.add_ff_generator(LennardJonesAttractiveForceFieldGenerator(
+            t.ratio, t.p0, t.p1, _ignore(topo, t.ign_bond, t.ign_contact), per))
+    if spec.dh is not None:
+        t = spec.dh
+        sg.add_ff_generator(DebyeHuckelForceFieldGenerator(
+            t.ionic_strength, t.temperature, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact), per))
+    return sg
+
+
+def build_system(spec: CGSpec) -> System:
+    return build_generator(spec).generate()

@@ -1,0 +1,214 @@
+"""TEST INFRASTRUCTURE - ctypes front end of the FP64 CPU oracle
+(oracle/ocm_oracle.cpp).  Only tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py use it, as the checker.  Parity unpinned: the
+reference ships no golden vectors; the oracle is pinned by analytic
+known-answer tests.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_D = C.POINTER(C.c_double)
+_I64 = C.POINTER(C.c_int64)
+_I32 = C.POINTER(C.c_int32)
+
+
+class OracleSystem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64), ("pos", _D), ("periodic", C.c_int), ("box", C.c_double * 3),
+        ("n_bonds", C.c_int64), ("bond_idx", _I64), ("bond_v0", _D), ("bond_k", _D),
+        ("bond_periodic", C.c_int),
+        ("n_go", C.c_int64), ("go_idx", _I64), ("go_k", _D), ("go_r0", _D), ("go_periodic", C.c_int),
+        ("n_fla", C.c_int64), ("fla_idx", _I64), ("fla_k", _D), ("fla_aa", _I32),
+        ("n_fld", C.c_int64), ("fld_idx", _I64), ("fld_k", _D), ("fld_aa1", _I32), ("fld_aa2", _I32),
+        ("exv_on", C.c_int), ("exv_eps", C.c_double), ("exv_ratio", C.c_double), ("exv_radius", _D),
+        ("exv_ign_bond", C.c_int), ("exv_ign_contact", C.c_int),
+        ("dh_on", C.c_int), ("dh_I", C.c_double), ("dh_T", C.c_double), ("dh_ratio", C.c_double),
+        ("dh_q", _D), ("dh_ign_bond", C.c_int), ("dh_ign_contact", C.c_int),
+        ("ljr_on", C.c_int), ("ljr_ratio", C.c_double), ("ljr_eps", _D), ("ljr_sigma", _D),
+        ("ljr_ign_bond", C.c_int), ("ljr_ign_contact", C.c_int),
+        ("lja_on", C.c_int), ("lja_ratio", C.c_double), ("lja_eps", _D), ("lja_sigma", _D),
+        ("lja_ign_bond", C.c_int), ("lja_ign_contact", C.c_int),
+        ("fp32_cutoff", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        L.oracle_evaluate.argtypes = [C.POINTER(OracleSystem), _D, _D]
+        L.oracle_evaluate.restype = C.c_int
+        L.oracle_dh_params.argtypes = [C.c_double, C.c_double, C.c_double, _D]
+        L.oracle_fla_min_energy.argtypes = [C.c_int]
+        L.oracle_fla_min_energy.restype = C.c_double
+        L.oracle_fld_min_energy.argtypes = [C.c_int]
+        L.oracle_fld_min_energy.restype = C.c_double
+        L.oracle_natural_spline.argtypes = [_D, C.c_double, _D]
+        L.oracle_fld_classes.argtypes = [C.c_int, C.c_int, _I32, C.c_int]
+        L.oracle_fld_classes.restype = C.c_int
+        L.oracle_ignore_within.argtypes = [C.c_int64, C.c_int64, _I64, C.c_int64, _I64, C.c_int,
+                                           C.c_int, _I64, C.c_int64, _I64]
+        L.oracle_langevin_step.argtypes = [C.c_int64, _D, _D, _D, _D, C.c_double, C.c_double,
+                                           C.c_double, C.c_uint32, C.c_uint32, C.c_uint64]
+        L.oracle_simulate.argtypes = [C.POINTER(OracleSystem), _D, _D, _D, C.c_double, C.c_double,
+                                      C.c_double, C.c_uint32, C.c_uint64, C.c_int64]
+        L.oracle_gaussian3.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, _D]
+        L.oracle_gaussian3.restype = None
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return None if a is None else np.ascontiguousarray(a, np.float64)
+
+
+class _Keep:
+    """Holds the numpy buffers an OracleSystem points into."""
+
+    def __init__(self):
+        self.items = []
+
+    def d(self, a):
+        if a is None:
+            return None
+        arr = np.ascontiguousarray(a, np.float64)
+        self.items.append(arr)
+        return arr.ctypes.data_as(_D)
+
+    def i64(self, a):
+        arr = np.ascontiguousarray(a, np.int64)
+        self.items.append(arr)
+        return arr.ctypes.data_as(_I64)
+
+    def i32(self, a):
+        arr = np.ascontiguousarray(a, np.int32)
+        self.items.append(arr)
+        return arr.ctypes.data_as(_I32)
+
+
+def make_system(spec, fp32_cutoff: bool = True, pos=None):
+    """Translate a synth.CGSpec into the oracle's flat description."""
+    k = _Keep()
+    s = OracleSystem()
+    s.n = spec.n
+    s.pos = k.d(spec.pos if pos is None else pos)
+    s.periodic = int(spec.periodic)
+    if spec.box is not None:
+        for c in range(3):
+            s.box[c] = spec.box[c]
+    s.n_bonds = len(spec.bonds)
+    s.bond_idx, s.bond_v0, s.bond_k = k.i64(spec.bonds), k.d(spec.bond_v0), k.d(spec.bond_k)
+    s.bond_periodic = int(spec.periodic)
+    s.n_go = len(spec.contacts)
+    s.go_idx, s.go_k, s.go_r0 = k.i64(spec.contacts), k.d(spec.go_k), k.d(spec.go_r0)
+    s.go_periodic = int(spec.periodic)
+    s.n_fla = len(spec.fla_idx)
+    s.fla_idx, s.fla_k, s.fla_aa = k.i64(spec.fla_idx), k.d(spec.fla_k), k.i32(spec.fla_aa)
+    s.n_fld = len(spec.fld_idx)
+    s.fld_idx, s.fld_k = k.i64(spec.fld_idx), k.d(spec.fld_k)
+    s.fld_aa1, s.fld_aa2 = k.i32(spec.fld_aa1), k.i32(spec.fld_aa2)
+    if spec.exv is not None:
+        t = spec.exv
+        s.exv_on, s.exv_eps, s.exv_ratio, s.exv_radius = 1, t.eps, t.ratio, k.d(t.p0)
+        s.exv_ign_bond, s.exv_ign_contact = t.ign_bond, t.ign_contact
+    if spec.dh is not None:
+        t = spec.dh
+        s.dh_on, s.dh_I, s.dh_T, s.dh_ratio, s.dh_q = 1, t.ionic_strength, t.temperature, t.ratio, k.d(t.p0)
+        s.dh_ign_bond, s.dh_ign_contact = t.ign_bond, t.ign_contact
+    if spec.ljr is not None:
+        t = spec.ljr
+        s.ljr_on, s.ljr_ratio, s.ljr_eps, s.ljr_sigma = 1, t.ratio, k.d(t.p0), k.d(t.p1)
+        s.ljr_ign_bond, s.ljr_ign_contact = t.ign_bond, t.ign_contact
+    if spec.lja is not None:
+        t = spec.lja
+        s.lja_on, s.lja_ratio, s.lja_eps, s.lja_sigma = 1, t.ratio, k.d(t.p0), k.d(t.p1)
+        s.lja_ign_bond, s.lja_ign_contact = t.ign_bond, t.ign_contact
+    s.fp32_cutoff = int(fp32_cutoff)
+    return s, k
+
+
+SLOTS = ("ExcludedVolume", "DebyeHuckel", "LennardJonesRepulsive", "LennardJonesAttractive",
+         "HarmonicBond", "GoContact", "FlexibleLocalAngle", "FlexibleLocalDihedral")
+
+
+def evaluate(spec, fp32_cutoff: bool = True, pos=None):
+    """FP64 forces (n, 3) and per-term energies {name: kJ/mol}."""
+    s, keep = make_system(spec, fp32_cutoff, pos)
+    f = np.zeros((spec.n, 3))
+    e = np.zeros(8)
+    lib().oracle_evaluate(C.byref(s), f.ctypes.data_as(_D), e.ctypes.data_as(_D))
+    del keep
+    return f, dict(zip(SLOTS, e))
+
+
+def dh_params(ionic_strength, temperature, ratio):
+    out = np.zeros(5)
+    lib().oracle_dh_params(ionic_strength, temperature, ratio, out.ctypes.data_as(_D))
+    return dict(zip(("k_e", "debye_length", "cutoff", "cutoff_correction", "eps_r"), out))
+
+
+def fla_min_energy(aa: int) -> float:
+    return lib().oracle_fla_min_energy(int(aa))
+
+
+def fld_min_energy(cls: int) -> float:
+    return lib().oracle_fld_min_energy(int(cls))
+
+
+def natural_spline(y, h):
+    y = np.ascontiguousarray(y, np.float64)
+    M = np.zeros(10)
+    lib().oracle_natural_spline(y.ctypes.data_as(_D), h, M.ctypes.data_as(_D))
+    return M
+
+
+def fld_classes(aa1: int, aa2: int) -> list[int]:
+    out = np.zeros(4, np.int32)
+    c = lib().oracle_fld_classes(aa1, aa2, out.ctypes.data_as(_I32), 4)
+    return [int(v) for v in out[:c]]
+
+
+def ignore_within(n, bonds, contacts, ign_bond, ign_contact):
+    b = np.ascontiguousarray(bonds, np.int64).reshape(-1, 2)
+    c = np.ascontiguousarray(contacts, np.int64).reshape(-1, 2)
+    cap = max(16, 64 * n)
+    out = np.zeros((cap, 2), np.int64)
+    nout = C.c_int64()
+    lib().oracle_ignore_within(n, len(b), b.ctypes.data_as(_I64), len(c), c.ctypes.data_as(_I64),
+                               ign_bond, ign_contact, out.ctypes.data_as(_I64), cap, C.byref(nout))
+    return out[: nout.value].copy()
+
+
+def langevin_step(x, v, f, masses, T, gamma, dt, seed, step, stream=0):
+    x = np.ascontiguousarray(x, np.float64).copy()
+    v = np.ascontiguousarray(v, np.float64).copy()
+    f = np.ascontiguousarray(f, np.float64)
+    m = np.ascontiguousarray(masses, np.float64)
+    lib().oracle_langevin_step(len(m), x.ctypes.data_as(_D), v.ctypes.data_as(_D), f.ctypes.data_as(_D),
+                               m.ctypes.data_as(_D), T, gamma, dt, seed, stream, step)
+    return x, v
+
+
+def simulate(spec, x, v, steps, seed, step0=0):
+    """CPU baseline: `steps` oracle steps of one system (in place)."""
+    s, keep = make_system(spec, fp32_cutoff=False, pos=x)
+    m = np.ascontiguousarray(spec.masses, np.float64)
+    lib().oracle_simulate(C.byref(s), x.ctypes.data_as(_D), v.ctypes.data_as(_D), m.ctypes.data_as(_D),
+                          spec.temperature, spec.friction, spec.dt, seed, step0, steps)
+    del keep
+
+
+def gaussian3(seed, stream, bead, step, purpose=0):
+    g = np.zeros(3)
+    lib().oracle_gaussian3(seed, stream, bead, step, purpose, g.ctypes.data_as(_D))
+    return g

@@ -1,0 +1,132 @@
+"""Batched / served path on the GPU: parity with the FP64 oracle, identical
+results alone and in a mix, continuous admission and retirement."""
+import numpy as np
+import pytest
+
+from conftest import rel_force_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _systems(sizes, seed0=100, temps=None):
+    from opencafemol_gb300 import synth
+    specs = []
+    for k, n in enumerate(sizes):
+        T = 300.0 if temps is None else float(temps[k])
+        specs.append(synth.go_protein(int(n), seed0 + k, temperature=T))
+    return specs
+
+
+def test_batch_forces_match_oracle(gpu):
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    specs = _systems([50, 97, 256, 333, 800], temps=[280, 300, 320, 340, 360])
+    batch = gpu.Batch(max_systems=8, max_total_beads=4096, max_beads_per_system=800)
+    slots = []
+    for s in specs:
+        system = synth.build_system(s)
+        slots.append((batch.admit(system, s.pos, temperature=s.temperature, n_steps=10), system, s))
+    for slot, system, s in slots:
+        f, e32 = batch.state(slot)
+        f_ref, e_ref = oracle.evaluate(s)
+        assert rel_force_err(f, f_ref) <= 1e-4
+        names = system.group_names()
+        for g, name in enumerate(names):
+            assert abs(e32[g] - e_ref[name]) <= 1e-5 * max(1.0, abs(e_ref[name])), name
+
+
+def test_same_alone_and_in_mix(gpu):
+    """A system's trajectory does not depend on what else is in the batch."""
+    from opencafemol_gb300 import synth
+    specs = _systems([64, 300, 150, 700, 90], seed0=200)
+    target = specs[1]
+    sys_t = synth.build_system(target)
+    alone = gpu.Batch(max_systems=2, max_total_beads=1024, max_beads_per_system=800)
+    a = alone.admit(sys_t, target.pos, seed=42, n_steps=300)
+    for _ in range(3):
+        alone.run(100)
+    xa = alone.positions(a)
+
+    mix = gpu.Batch(max_systems=8, max_total_beads=4096, max_beads_per_system=800)
+    slots = [mix.admit(synth.build_system(s), s.pos, seed=7 + k, n_steps=300) for k, s in enumerate(specs)]
+    mix.retire(slots[0])  # leave a hole in the bead arena
+    m = mix.admit(sys_t, target.pos, seed=42, n_steps=300)
+    for _ in range(3):
+        mix.run(100)
+    xm = mix.positions(m)
+    assert np.array_equal(xa, xm)
+
+
+def test_chunking_does_not_change_results(gpu):
+    from opencafemol_gb300 import synth
+    s = _systems([400], seed0=300)[0]
+    system = synth.build_system(s)
+    out = []
+    for chunks in ([240], [100, 100, 40], [7] * 34 + [2]):
+        b = gpu.Batch(max_systems=1, max_total_beads=512, max_beads_per_system=512)
+        slot = b.admit(system, s.pos, seed=9, n_steps=240)
+        for c in chunks:
+            b.run(c)
+        assert b.steps_done(slot) == 240
+        out.append(b.positions(slot))
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+
+
+def test_batch_matches_plain_after_one_step(gpu):
+    """The batched and the plain engine evaluate the same physics: after one
+    step from identical state they agree to FP32 accumulation error."""
+    from opencafemol_gb300 import synth
+    s = _systems([256], seed0=400)[0]
+    system = synth.build_system(s)
+    v0 = np.random.default_rng(1).normal(scale=0.1, size=(s.n, 3)).astype(np.float32).astype(np.float64)
+    b = gpu.Batch(max_systems=1, max_total_beads=512, max_beads_per_system=512)
+    slot = b.admit(system, s.pos, velocities=v0, temperature=s.temperature, seed=77, n_steps=1)
+    b.run(1)
+    ctx = gpu.Context(system, gpu.LangevinIntegrator(s.temperature, s.friction, s.dt, 77))
+    ctx.setPositions(s.pos)
+    ctx.setVelocities(v0)
+    ctx.step(1)
+    assert np.max(np.abs(b.positions(slot) - ctx.getPositions())) < 1e-7
+    assert np.max(np.abs(b.velocities(slot) - ctx.getVelocities())) < 1e-4
+
+
+def test_continuous_admission(gpu):
+    """Requests admitted while others run; finished ones retire and free
+    capacity for new ones; every request completes its step count."""
+    from opencafemol_gb300 import synth
+    specs = _systems([40, 120, 500, 60, 250, 80, 700, 33], seed0=500)
+    steps = [30, 200, 120, 50, 90, 10, 150, 70]
+    batch = gpu.Batch(max_systems=3, max_total_beads=1300, max_beads_per_system=800)
+    pending = list(range(len(specs)))
+    running = {}
+    done = {}
+    rounds = 0
+    while pending or running:
+        while pending:
+            k = pending[0]
+            try:
+                slot = batch.admit(synth.build_system(specs[k]), specs[k].pos, seed=k, n_steps=steps[k])
+            except gpu.OCMError as e:
+                assert e.code == 3  # out of capacity: wait for a retirement
+                break
+            running[slot] = k
+            pending.pop(0)
+        batch.run(25)
+        for slot in batch.finished():
+            k = running.pop(slot)
+            assert batch.steps_done(slot) == steps[k]
+            done[k] = batch.positions(slot)
+            batch.retire(slot)
+        rounds += 1
+        assert rounds < 200
+    assert sorted(done) == list(range(len(specs)))
+    assert all(np.all(np.isfinite(x)) for x in done.values())
+
+
+def test_oversize_system_rejected(gpu):
+    from opencafemol_gb300 import synth
+    s = _systems([300], seed0=600)[0]
+    b = gpu.Batch(max_systems=2, max_total_beads=1024, max_beads_per_system=256)
+    with pytest.raises(gpu.OCMError) as ei:
+        b.admit(synth.build_system(s), s.pos, n_steps=1)
+    assert ei.value.code == 3

@@ -1,0 +1,189 @@
+"""Plain single-system path on the GPU against the FP64 oracle.
+
+Tolerances: per-bead force error max_i |dF_i| / max(|F_i|, 1e-3 F_rms)
+<= 1e-4 (FP32 pair arithmetic, 64-bit fixed-point accumulation); per-term
+energies within 1e-5 relative (or 1e-5 kJ/mol absolute for near-zero sums).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_force_err, rms_rel_err
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-4
+ENERGY_TOL = 1e-5
+
+
+def _ctx(ocm, spec, seed=7):
+    from opencafemol_gb300 import synth
+    system = synth.build_system(spec)
+    ctx = ocm.Context(system, ocm.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, seed))
+    ctx.setPositions(spec.pos)
+    return system, ctx
+
+
+def _group_energy_map(system, e32):
+    return {name: e32[g] for g, name in enumerate(system.group_names())}
+
+
+def _check_energies(e_ref, got):
+    for name, ref in e_ref.items():
+        if name not in got:
+            assert abs(ref) < 1e-12, name
+            continue
+        tol = ENERGY_TOL * max(1.0, abs(ref))
+        assert abs(got[name] - ref) <= tol, (name, got[name], ref)
+
+
+@pytest.mark.parametrize("n,seed", [(60, 1), (300, 2), (800, 3)])
+def test_go_protein_forces_energies(gpu, n, seed):
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    spec = synth.go_protein(n, seed)
+    system, ctx = _ctx(gpu, spec)
+    f, etot = ctx.getState()
+    f_ref, e_ref = oracle.evaluate(spec)
+    assert rel_force_err(f, f_ref) <= FORCE_TOL
+    assert rms_rel_err(f, f_ref) <= 1e-5
+    _check_energies(e_ref, _group_energy_map(system, ctx.getGroupEnergies()))
+    assert abs(etot - sum(e_ref.values())) <= ENERGY_TOL * max(1.0, abs(sum(e_ref.values())))
+
+
+@pytest.mark.parametrize("chains,length,box,seed", [(6, 50, (12.0, 12.0, 30.0), 4),
+                                                    (30, 100, (15.0, 15.0, 60.0), 5)])
+def test_hps_slab_forces_energies(gpu, chains, length, box, seed):
+    """Periodic HPS + DH system; the second case has > 2048 beads and runs
+    the Morton-ordered cluster layout."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    spec = synth.hps_slab(chains, length, box, slab_width=box[2] / 3, seed=seed)
+    system, ctx = _ctx(gpu, spec)
+    f, _ = ctx.getState(energy=False)
+    f_ref, e_ref = oracle.evaluate(spec)
+    assert rel_force_err(f, f_ref) <= FORCE_TOL
+    _check_energies(e_ref, _group_energy_map(system, ctx.getGroupEnergies()))
+    assert ctx.stats()["reordered"] == int(spec.n > 2048)
+
+
+def test_group_masks(gpu):
+    """getState(groups=1<<g) returns exactly that group's forces and energy
+    (Observer.cpp:339-341 queries one group at a time)."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    spec = synth.go_protein(200, 9)
+    system, ctx = _ctx(gpu, spec)
+    _, e_ref = oracle.evaluate(spec)
+    total_f = np.zeros((spec.n, 3))
+    for g, name in enumerate(system.group_names()):
+        f, e = ctx.getState(groups=1 << g)
+        total_f += f
+        assert abs(e - e_ref[name]) <= ENERGY_TOL * max(1.0, abs(e_ref[name])), name
+    f_all, _ = ctx.getState()
+    assert np.allclose(total_f, f_all, rtol=0, atol=1e-6 * np.abs(f_all).max())
+
+
+def test_pair_set_bit_exact(gpu):
+    """The pairs the tile list makes the kernel test within the largest
+    cutoff equal a brute-force FP32 enumeration with the same r^2 formula."""
+    from opencafemol_gb300 import synth
+    spec = synth.hps_slab(30, 100, (15.0, 15.0, 60.0), slab_width=20.0, seed=6)
+    system, ctx = _ctx(gpu, spec)
+    pairs = ctx.list_pairs()
+    got = set(map(tuple, pairs.tolist()))
+    assert len(got) == len(pairs), "a pair was evaluated twice"
+    rc = ctx.stats()["max_cutoff"]
+    ref = brute_force_pairs(spec.pos, spec.box, rc)
+    assert got == ref
+
+
+def brute_force_pairs(pos, box, rc):
+    L = np.asarray(box, np.float64)
+    x = np.asarray(pos, np.float64)
+    w = x - L * np.floor(x * (1.0 / L))
+    xf = w.astype(np.float32)
+    Lf, iLf = L.astype(np.float32), (1.0 / L).astype(np.float32)
+    rc2 = np.float32(rc * rc)
+    out = set()
+    n = len(xf)
+    for i in range(n - 1):
+        d = xf[i + 1:] - xf[i]
+        d = (d - Lf * np.rint(d * iLf)).astype(np.float32)  # separate rounding, equals the fma result
+        # emulate fmaf(dz,dz,fmaf(dy,dy,dx*dx)) exactly in float64 then round once per fma
+        dx2 = (d[:, 0] * d[:, 0]).astype(np.float32)
+        s1 = (d[:, 1].astype(np.float64) * d[:, 1] + dx2).astype(np.float32)
+        r2 = (d[:, 2].astype(np.float64) * d[:, 2] + s1).astype(np.float32)
+        for j in np.nonzero(r2 < rc2)[0]:
+            out.add((i, i + 1 + int(j)))
+    return out
+
+
+def test_morton_order_deterministic(gpu):
+    from opencafemol_gb300 import synth
+    spec = synth.hps_slab(30, 100, (15.0, 15.0, 60.0), slab_width=20.0, seed=6)
+    _, c1 = _ctx(gpu, spec)
+    _, c2 = _ctx(gpu, spec)
+    o1, o2 = c1.cluster_order(), c2.cluster_order()
+    assert np.array_equal(o1, o2)
+    real = o1[o1 >= 0]
+    assert np.array_equal(np.sort(real), np.arange(spec.n))
+
+
+def test_langevin_one_step(gpu):
+    """x(t+dt), v(t+dt/2) after one step against the oracle's Langevin
+    update fed with the oracle's forces and the same Philox stream."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    spec = synth.go_protein(120, 11)
+    system, ctx = _ctx(gpu, spec, seed=1234)
+    rng = np.random.default_rng(0)
+    v0 = rng.normal(scale=0.1, size=(spec.n, 3)).astype(np.float32).astype(np.float64)
+    ctx.setVelocities(v0)
+    ctx.step(1)
+    x1, v1 = ctx.getPositions(), ctx.getVelocities()
+    f_ref, _ = oracle.evaluate(spec)
+    xr, vr = oracle.langevin_step(spec.pos, v0, f_ref, spec.masses, spec.temperature, spec.friction,
+                                  spec.dt, 1234, 0)
+    assert np.max(np.abs(v1 - vr)) <= 1e-4 * np.max(np.abs(vr))
+    assert np.max(np.abs(x1 - xr)) <= 1e-6
+
+
+def test_trajectory_deterministic(gpu):
+    from opencafemol_gb300 import synth
+    spec = synth.go_protein(150, 12)
+    runs = []
+    for _ in range(2):
+        _, ctx = _ctx(gpu, spec, seed=99)
+        ctx.setVelocitiesToTemperature(spec.temperature, 5)
+        ctx.step(200)
+        runs.append(ctx.getPositions())
+    assert np.array_equal(runs[0], runs[1])
+
+
+def test_temperature_equilibrates(gpu):
+    """<KE> -> 3N/2 kT for Langevin dynamics at the bath temperature."""
+    from opencafemol_gb300 import synth
+    spec = synth.go_protein(200, 13)
+    spec.friction = 1.0
+    _, ctx = _ctx(gpu, spec, seed=3)
+    ctx.setVelocitiesToTemperature(spec.temperature, 4)
+    ctx.step(2000)
+    kes = []
+    for _ in range(60):
+        ctx.step(50)
+        kes.append(ctx.getKineticEnergy())
+    kT = 0.00831446261815324 * spec.temperature
+    expect = 1.5 * spec.n * kT
+    assert abs(np.mean(kes) / expect - 1.0) < 0.05
+
+
+def test_long_run_stays_finite_and_rebuilds(gpu):
+    from opencafemol_gb300 import synth
+    spec = synth.hps_slab(30, 100, (15.0, 15.0, 60.0), slab_width=20.0, seed=8)
+    _, ctx = _ctx(gpu, spec, seed=21)
+    ctx.setVelocitiesToTemperature(spec.temperature, 22)
+    ctx.step(500)
+    x = ctx.getPositions()
+    assert np.all(np.isfinite(x))
+    st = ctx.stats()
+    assert st["steps_done"] == 500 and st["list_builds"] >= 500 // max(1, st["rebuild_interval"])
