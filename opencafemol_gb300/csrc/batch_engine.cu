@@ -60,9 +60,25 @@ __device__ __forceinline__ void sadd(unsigned long long* F, int nmax, int b, flo
     atomicAdd(&F[2 * nmax + b], to_fixed(f.z));
 }
 
-__device__ __forceinline__ float3 dsep(const double* sxd, int nmax, int i, int j) {
-    return make_float3((float)(sxd[j] - sxd[i]), (float)(sxd[nmax + j] - sxd[nmax + i]),
-                       (float)(sxd[2 * nmax + j] - sxd[2 * nmax + i]));
+__device__ __forceinline__ float3 lo3(const float* sxl, int nmax, int i) {
+    return make_float3(sxl[i], sxl[nmax + i], sxl[2 * nmax + i]);
+}
+
+// x_j - x_i of float-float positions, rounded once to FP32.
+__device__ __forceinline__ float3 ffsep(const float4* sx, const float* sxl, int nmax, int i, int j) {
+    float3 dh, dl;
+    ff_sep(sx[i], lo3(sxl, nmax, i), sx[j], lo3(sxl, nmax, j), dh, dl);
+    return make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
+}
+
+// (hi, lo) += d, renormalised so hi is the FP32 rounding of the sum.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
+    float e;
+    const float s = two_sum(hi, d, e);
+    const float l = __fadd_rn(lo, e);
+    const float h = __fadd_rn(s, l);
+    lo = __fsub_rn(l, __fsub_rn(h, s));
+    hi = h;
 }
 
 template <int TERMS, bool LABELS, bool ENERGY>
@@ -185,13 +201,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
     constexpr int NW = THREADS / 32;
     extern __shared__ __align__(16) unsigned char smem[];
     const int nmax = a.nmax;
-    double* sxd = reinterpret_cast<double*>(smem);
-    unsigned long long* sF = reinterpret_cast<unsigned long long*>(smem + 24 * (size_t)nmax);
-    float4* sx = reinterpret_cast<float4*>(smem + 48 * (size_t)nmax);
-    float4* sp0 = reinterpret_cast<float4*>(smem + 64 * (size_t)nmax);
-    float* sv = reinterpret_cast<float*>(smem + 80 * (size_t)nmax);
-    float* sim = reinterpret_cast<float*>(smem + 92 * (size_t)nmax);
-    size_t off = 96 * (size_t)nmax;
+    // Positions are float-float: hi parts in sx (used by the pair tiles),
+    // lo parts in sxl; x = hi + lo carries ~48 significant bits.
+    unsigned long long* sF = reinterpret_cast<unsigned long long*>(smem);
+    float4* sx = reinterpret_cast<float4*>(smem + 24 * (size_t)nmax);
+    float4* sp0 = reinterpret_cast<float4*>(smem + 40 * (size_t)nmax);
+    float* sxl = reinterpret_cast<float*>(smem + 56 * (size_t)nmax);
+    float* sv = reinterpret_cast<float*>(smem + 68 * (size_t)nmax);
+    float* sim = reinterpret_cast<float*>(smem + 80 * (size_t)nmax);
+    size_t off = 84 * (size_t)nmax;
     float4* sp1 = nullptr;
     uint32_t* slab = nullptr;
     if ((TERMS & kTermLJA) || LABELS) {
@@ -251,11 +269,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
             sF[2 * nmax + b] = 0ull;
             if (b < n) {
                 const double px = a.x[boff + b], py = a.y[boff + b], pz = a.z[boff + b];
-                sxd[b] = px;
-                sxd[nmax + b] = py;
-                sxd[2 * nmax + b] = pz;
-                sx[b] = make_float4(__double2float_rn(px), __double2float_rn(py),
-                                    __double2float_rn(pz), 0.f);
+                const float hx = __double2float_rn(px), hy = __double2float_rn(py),
+                            hz = __double2float_rn(pz);
+                sx[b] = make_float4(hx, hy, hz, 0.f);
+                sxl[b] = __double2float_rn(px - (double)hx);
+                sxl[nmax + b] = __double2float_rn(py - (double)hy);
+                sxl[2 * nmax + b] = __double2float_rn(pz - (double)hz);
                 sp0[b] = gp0[b];
                 sv[b] = a.vx[boff + b];
                 sv[nmax + b] = a.vy[boff + b];
@@ -303,9 +322,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                 const BondTerm bt = bonds[b];
                 const int sl = bt.kind == kBondHarmonic ? kSlotHB : kSlotGO;
                 if (!(slots_en & (1u << sl))) continue;
-                const float3 d = dsep(sxd, nmax, bt.i, bt.j);
+                float3 dh, dl;
+                ff_sep(sx[bt.i], lo3(sxl, nmax, bt.i), sx[bt.j], lo3(sxl, nmax, bt.j), dh, dl);
+                const float3 d = make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
+                const float delta = ff_bond_delta(dh, dl, bt.r0sq_hi, bt.r0sq_lo);
                 float en;
-                const float s = bond_scalar(bt.kind, norm2(d), bt.p0, bt.p1, en);
+                const float s = bond_scalar(bt.kind, norm2(d), delta, bt.p0, bt.p1, en);
                 sadd(sF, nmax, bt.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
                 sadd(sF, nmax, bt.j, make_float3(s * d.x, s * d.y, s * d.z));
                 if (ENERGY) eacc[sl] += en;
@@ -313,8 +335,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
             if (slots_en & (1u << kSlotFLA)) {
                 for (int b = tid; b < R.n_angles; b += THREADS) {
                     const AngleTerm g = angles[b];
-                    const float3 u = dsep(sxd, nmax, g.j, g.i);
-                    const float3 v = dsep(sxd, nmax, g.j, g.k);
+                    const float3 u = ffsep(sx, sxl, nmax, g.j, g.i);
+                    const float3 v = ffsep(sx, sxl, nmax, g.j, g.k);
                     float3 f1, f3;
                     float en;
                     fla_forces(u, v, g.kk, fla[g.table], f1, f3, en);
@@ -327,9 +349,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
             if (slots_en & (1u << kSlotFLD)) {
                 for (int b = tid; b < R.n_dih; b += THREADS) {
                     const DihedralTerm qd = dih[b];
-                    const float3 F = dsep(sxd, nmax, qd.j, qd.i);
-                    const float3 G = dsep(sxd, nmax, qd.k, qd.j);
-                    const float3 H = dsep(sxd, nmax, qd.k, qd.l);
+                    const float3 F = ffsep(sx, sxl, nmax, qd.j, qd.i);
+                    const float3 G = ffsep(sx, sxl, nmax, qd.k, qd.j);
+                    const float3 H = ffsep(sx, sxl, nmax, qd.k, qd.l);
                     float3 f1, f2, f3, f4;
                     float en;
                     fld_forces(F, G, H, qd.kk, fld[qd.table], f1, f2, f3, f4, en);
@@ -364,14 +386,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                         sv[b] = vx;
                         sv[nmax + b] = vy;
                         sv[2 * nmax + b] = vz;
-                        const double px = sxd[b] + (double)vx * (double)lc.dt;
-                        const double py = sxd[nmax + b] + (double)vy * (double)lc.dt;
-                        const double pz = sxd[2 * nmax + b] + (double)vz * (double)lc.dt;
-                        sxd[b] = px;
-                        sxd[nmax + b] = py;
-                        sxd[2 * nmax + b] = pz;
-                        sx[b] = make_float4(__double2float_rn(px), __double2float_rn(py),
-                                            __double2float_rn(pz), 0.f);
+                        float4 h = sx[b];
+                        ff_add(h.x, sxl[b], vx * lc.dt);
+                        ff_add(h.y, sxl[nmax + b], vy * lc.dt);
+                        ff_add(h.z, sxl[2 * nmax + b], vz * lc.dt);
+                        sx[b] = h;
                     }
                 }
                 __syncwarp();
@@ -383,9 +402,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         // ---- write back ----
         if (INTEGRATE) {
             for (int b = tid; b < n; b += THREADS) {
-                a.x[boff + b] = sxd[b];
-                a.y[boff + b] = sxd[nmax + b];
-                a.z[boff + b] = sxd[2 * nmax + b];
+                const float4 h = sx[b];
+                a.x[boff + b] = (double)h.x + (double)sxl[b];
+                a.y[boff + b] = (double)h.y + (double)sxl[nmax + b];
+                a.z[boff + b] = (double)h.z + (double)sxl[2 * nmax + b];
                 a.vx[boff + b] = sv[b];
                 a.vy[boff + b] = sv[nmax + b];
                 a.vz[boff + b] = sv[2 * nmax + b];
@@ -616,7 +636,7 @@ BatchEngine::~BatchEngine() {
 }
 
 size_t BatchEngine::smem_bytes(int nmax, bool general) const {
-    return (size_t)nmax * (general ? 116 : 96) + 2 * kMaxClusters * sizeof(float4);
+    return (size_t)nmax * (general ? 104 : 84) + 2 * kMaxClusters * sizeof(float4);
 }
 
 int64_t BatchEngine::footprint(const SystemDesc& d) {

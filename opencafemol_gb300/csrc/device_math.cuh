@@ -144,21 +144,54 @@ __device__ __forceinline__ float pair_scalar(float r2, float4 pi, float4 pj, flo
 // ---------------------------------------------------------------------------
 // Harmonic bond 1/2 k (r - r0)^2 (HarmonicBondForceFieldGenerator.cpp:5-10).
 // Go 10-12: k (5 (r0/r)^12 - 6 (r0/r)^10) (GoContactForceFieldGenerator.cpp:5-7).
-// Returns s with F_a = s * (x_a - x_b).
-__device__ __forceinline__ float bond_scalar(int kind, float r2, float p0, float p1, float& energy) {
+// `delta` = r^2 - r0^2 evaluated without cancellation by the caller: both
+// forces are proportional to it near the native length, where an FP32
+// r - r0 would lose all its digits.  Returns s with F_a = s * (x_a - x_b).
+__device__ __forceinline__ float bond_scalar(int kind, float r2, float delta, float p0, float p1,
+                                             float& energy) {
     if (kind == kBondHarmonic) {  // p0 = r0, p1 = k
         const float r = sqrtf(r2);
-        const float dr = r - p0;
+        const float dr = delta / (r + p0);
         energy = 0.5f * p1 * dr * dr;
         return -p1 * dr / r;
-    } else {  // Go: p0 = k, p1 = r0
+    } else {  // Go: p0 = k, p1 = r0;  t^2 - 1 = -delta / r^2
         const float inv = 1.f / r2;
         const float t2 = p1 * p1 * inv;
         const float t10 = t2 * t2 * t2 * t2 * t2;
-        const float t12 = t10 * t2;
-        energy = p0 * (5.f * t12 - 6.f * t10);
-        return 60.f * p0 * (t12 - t10) * inv;
+        energy = p0 * t10 * (5.f * t2 - 6.f);
+        return -60.f * p0 * t10 * delta * inv * inv;
     }
+}
+
+// Error-free transforms for float-float ("unevaluated sum") arithmetic.
+__device__ __forceinline__ float two_sum(float a, float b, float& err) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+// r^2 - r0^2 for a separation given as dh + dl (|dl| << |dh|), with r0^2 =
+// r0sq_hi + r0sq_lo: products split exactly by FMA, sums by TwoSum.
+__device__ __forceinline__ float ff_bond_delta(float3 dh, float3 dl, float r0sq_hi, float r0sq_lo) {
+    const float px = __fmul_rn(dh.x, dh.x), py = __fmul_rn(dh.y, dh.y), pz = __fmul_rn(dh.z, dh.z);
+    const float ex = __fmaf_rn(dh.x, dh.x, -px), ey = __fmaf_rn(dh.y, dh.y, -py),
+                ez = __fmaf_rn(dh.z, dh.z, -pz);
+    float t1, t2;
+    const float s1 = two_sum(px, py, t1);
+    const float s2 = two_sum(s1, pz, t2);
+    const float lo = t1 + t2 + ex + ey + ez + 2.f * (dh.x * dl.x + dh.y * dl.y + dh.z * dl.z);
+    return __fsub_rn(s2, r0sq_hi) + (lo - r0sq_lo);
+}
+// Separation x_j - x_i of float-float positions: hi part exact by TwoSum.
+__device__ __forceinline__ void ff_sep(float4 hi_i, float3 lo_i, float4 hi_j, float3 lo_j,
+                                       float3& dh, float3& dl) {
+    float e;
+    dh.x = two_sum(hi_j.x, -hi_i.x, e);
+    dl.x = e + (lo_j.x - lo_i.x);
+    dh.y = two_sum(hi_j.y, -hi_i.y, e);
+    dl.y = e + (lo_j.y - lo_i.y);
+    dh.z = two_sum(hi_j.z, -hi_i.z, e);
+    dl.z = e + (lo_j.z - lo_i.z);
 }
 
 // Flexible-local angle (FlexibleLocalAngleForceFieldGenerator.cpp:21-25):

@@ -73,6 +73,7 @@ struct BondTerm {
     int32_t kind;      // kBondHarmonic / kBondGo
     int32_t periodic;  // minimum image when nonzero
     float p0, p1;      // (r0, k) harmonic; (k, r0) Go
+    float r0sq_hi, r0sq_lo;  // r0^2 as an unevaluated float sum
 };
 struct AngleTerm {
     int32_t i, j, k, table;

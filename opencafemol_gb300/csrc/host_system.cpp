@@ -692,6 +692,10 @@ CompiledSystem compile_system(const SystemDesc& d) {
                 b.periodic = f.periodic ? 1 : 0;
                 b.p0 = (float)f.par[t][0];
                 b.p1 = (float)f.par[t][1];
+                const double r0 = f.kind == ForceKind::HarmonicBond ? f.par[t][0] : f.par[t][1];
+                const double r0sq = r0 * r0;
+                b.r0sq_hi = (float)r0sq;
+                b.r0sq_lo = (float)(r0sq - (double)b.r0sq_hi);
                 if (b.i < 0 || b.j < 0) throw Error(1, "[error] negative particle index");
                 c.bonds.push_back(b);
             }

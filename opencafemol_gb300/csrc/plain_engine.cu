@@ -439,9 +439,17 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
             const BondTerm b = a.bonds[t];
             const int slot = b.kind == kBondHarmonic ? kSlotHB : kSlotGO;
             if (a.slots_enabled & (1u << slot)) {
-                const float3 d = bonded_sep(a, b.i, b.j, b.periodic);
+                double dx = a.x[b.j] - a.x[b.i], dy = a.y[b.j] - a.y[b.i], dz = a.z[b.j] - a.z[b.i];
+                if (b.periodic) {
+                    dx -= (double)a.box.x * rint(dx * (double)a.inv_box.x);
+                    dy -= (double)a.box.y * rint(dy * (double)a.inv_box.y);
+                    dz -= (double)a.box.z * rint(dz * (double)a.inv_box.z);
+                }
+                const double r2d = dx * dx + dy * dy + dz * dz;
+                const float delta = (float)(r2d - ((double)b.r0sq_hi + (double)b.r0sq_lo));
+                const float3 d = make_float3((float)dx, (float)dy, (float)dz);
                 float en;
-                const float s = bond_scalar(b.kind, norm2(d), b.p0, b.p1, en);
+                const float s = bond_scalar(b.kind, norm2(d), delta, b.p0, b.p1, en);
                 add_force(a.F, a.n, b.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
                 add_force(a.F, a.n, b.j, make_float3(s * d.x, s * d.y, s * d.z));
                 if (b.kind == kBondHarmonic) eh = en;

@@ -126,6 +126,10 @@ class HarmonicBondForceFieldGenerator(_Generator):
         self.indices = _pairs_arg(indices_vec, 2)
         self.v0s, self.ks = as_f64(v0s), as_f64(ks)
         self.use_periodic = bool(use_periodic)
+        if not (len(self.indices) == len(self.v0s) == len(self.ks)):
+            raise OCMError(1, "[error] HarmonicBondForceFieldGenerator: parameter number of "
+                              f"indices_vec ({len(self.indices)}), v0 ({len(self.v0s)}) and "
+                              f"k ({len(self.ks)}) is not matched.The number os these parameters must be same.")
 
     def name(self) -> str:
         return "HarmonicBond"
@@ -144,6 +148,10 @@ class GoContactForceFieldGenerator(_Generator):
         self.indices = _pairs_arg(indices_vec, 2)
         self.ks, self.r0s = as_f64(ks), as_f64(r0s)
         self.use_periodic = bool(use_periodic)
+        if not (len(self.indices) == len(self.ks) == len(self.r0s)):
+            raise OCMError(1, "[error] GoContactForceFieldGenerator : parameter number of "
+                              f"indices_vec ({len(self.indices)}), k ({len(self.ks)}) and "
+                              f"r0 ({len(self.r0s)}) is not matched.The number of these parameters must be same.")
 
     def name(self) -> str:
         return "GoContact"
@@ -164,6 +172,10 @@ class FlexibleLocalAngleForceFieldGenerator(_Generator):
             raise OCMError(1, "spline_table must have 10 values")
         self.aa = aa_name
         self.use_periodic = bool(use_periodic)
+        if len(self.indices) != len(self.ks):
+            raise OCMError(1, "[error] FlexibleLocalAngleForceFieldGenerator : parameter number of"
+                              f"indices_vec ({len(self.indices)}) and k ({len(self.ks)}) is not matched."
+                              "The number of these parameters must be same.")
 
     def name(self) -> str:
         return f"FlexibleLocalAngle ({self.aa})"
@@ -185,6 +197,10 @@ class FlexibleLocalDihedralForceFieldGenerator(_Generator):
             raise OCMError(1, "fourier_table must have 7 values")
         self.pair = aa_pair_name
         self.use_periodic = bool(use_periodic)
+        if len(self.indices) != len(self.ks):
+            raise OCMError(1, "[error] FlexibleLocalDihedralForceFieldGenerator : parameter number of "
+                              f"indices_vec ({len(self.indices)}) and k ({len(self.ks)}) is not matched."
+                              "The number of these parameters must be same.")
 
     def name(self) -> str:
         return f"FlexibleLocalDihedral ({self.pair})"

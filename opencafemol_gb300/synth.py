@@ -193,7 +193,7 @@ def hps_slab(n_chains: int, chain_len: int, box, slab_width: float, seed: int,
         w = p - L * np.floor(p / L)
         return tuple((w // cell).astype(int))
 
-    def clash(p):
+    def clash(p, skip=()):
         k = key(p)
         nc = np.maximum(1, (L // cell).astype(int))
         for dx in (-1, 0, 1):
@@ -201,6 +201,8 @@ def hps_slab(n_chains: int, chain_len: int, box, slab_width: float, seed: int,
                 for dz in (-1, 0, 1):
                     kk = ((k[0] + dx) % nc[0], (k[1] + dy) % nc[1], (k[2] + dz) % nc[2])
                     for j in grid.get(kk, ()):
+                        if j in skip:
+                            continue
                         d = pos[j] - p
                         d -= L * np.round(d / L)
                         if d @ d < min_dist * min_dist:
@@ -213,37 +215,54 @@ def hps_slab(n_chains: int, chain_len: int, box, slab_width: float, seed: int,
         grid.setdefault((k[0] % nc[0], k[1] % nc[1], k[2] % nc[2]), []).append(i)
         pos[i] = p
 
+    def unput(i):
+        nc = np.maximum(1, (L // cell).astype(int))
+        k = key(pos[i])
+        grid[(k[0] % nc[0], k[1] % nc[1], k[2] % nc[2])].remove(i)
+
     i = 0
     for _c in range(n_chains):
-        for _try in range(1000):
-            p0 = np.array([rng.uniform(0, box[0]), rng.uniform(0, box[1]), rng.uniform(zlo, zhi)])
-            if not clash(p0):
-                break
-        put(i, p0)
-        i += 1
-        prev_b = None
-        for _k in range(1, chain_len):
-            placed = False
-            for _try in range(400):
-                if prev_b is None:
-                    dvec = rng.normal(size=3)
-                    dvec /= np.linalg.norm(dvec)
-                else:
-                    u, w = _orthonormal(prev_b)
-                    th = rng.uniform(1.75, 2.6)
-                    ph = rng.uniform(-math.pi, math.pi)
-                    dvec = -math.cos(th) * prev_b + math.sin(th) * (math.cos(ph) * u + math.sin(ph) * w)
-                cand = pos[i - 1] + 0.38 * dvec
-                if cand[2] < zlo or cand[2] > zhi:
-                    continue
-                if not clash(cand):
-                    placed = True
+        start = i
+        for _restart in range(50):
+            i = start
+            for _try in range(1000):
+                p0 = np.array([rng.uniform(0, box[0]), rng.uniform(0, box[1]), rng.uniform(zlo, zhi)])
+                if not clash(p0):
                     break
-            if not placed:
-                cand = pos[i - 1] + 0.38 * dvec
-            put(i, cand)
-            prev_b = dvec
+            put(i, p0)
             i += 1
+            prev_b = None
+            ok = True
+            for _k in range(1, chain_len):
+                placed = False
+                # bond angle in [1.75, 2.6] rad first; free direction when stuck at a wall
+                for _try in range(800):
+                    if prev_b is None or _try >= 400:
+                        dvec = rng.normal(size=3)
+                        dvec /= np.linalg.norm(dvec)
+                    else:
+                        u, w = _orthonormal(prev_b)
+                        th = rng.uniform(1.75, 2.6)
+                        ph = rng.uniform(-math.pi, math.pi)
+                        dvec = -math.cos(th) * prev_b + math.sin(th) * (math.cos(ph) * u + math.sin(ph) * w)
+                    cand = pos[i - 1] + 0.38 * dvec
+                    if cand[2] < zlo or cand[2] > zhi:
+                        continue
+                    if not clash(cand, skip=(i - 1, i - 2)):
+                        placed = True
+                        break
+                if not placed:
+                    ok = False
+                    break
+                put(i, cand)
+                prev_b = dvec
+                i += 1
+            if ok:
+                break
+            for k in range(start, i):
+                unput(k)
+        else:
+            raise RuntimeError("could not place a chain in the slab")
     pos = pos - L * np.floor(pos / L)
     pos = _f32(pos)
     pos = np.where(pos >= L, pos - L, pos)  # FP32 rounding may land exactly on L
