@@ -267,6 +267,19 @@ int ocm_batch_retire(ocm_batch* batch, int64_t slot);
 int ocm_batch_active(ocm_batch* batch, int64_t* n_active, int64_t* beads_active);
 /* Device milliseconds of the last ocm_batch_run (CUDA events on its stream). */
 int ocm_batch_last_run_ms(ocm_batch* batch, double* ms);
+/* Launch shape of the persistent kernel: threads per CTA (256, 512 or
+ * 1024); the number of resident CTAs per SM follows from occupancy.  Set
+ * by the autotuner; results do not depend on it. */
+int ocm_batch_set_threads(ocm_batch* batch, int32_t threads_per_cta);
+/* Shared memory per CTA given to neighbour lists, in KiB (the rest of the
+ * SM's unified memory stays L1 cache for the static parameters); -1 = all
+ * that fits.  Set by the autotuner; results do not depend on it. */
+int ocm_batch_set_list_smem(ocm_batch* batch, int32_t kib);
+int ocm_batch_get_threads(ocm_batch* batch, int32_t* threads_per_cta);
+/* Neighbour-list statistics of a slot: list builds during its last chunk
+ * and the list capacity (entries per bead). */
+int ocm_batch_slot_stats(ocm_batch* batch, int64_t slot, int32_t* list_builds,
+                         int32_t* list_capacity);
 
 #ifdef __cplusplus
 }

@@ -105,6 +105,10 @@ SIGNATURES = {
     "ocm_batch_retire": (C.c_int, [_P, C.c_int64]),
     "ocm_batch_active": (C.c_int, [_P, _I64P, _I64P]),
     "ocm_batch_last_run_ms": (C.c_int, [_P, _DP]),
+    "ocm_batch_set_threads": (C.c_int, [_P, C.c_int32]),
+    "ocm_batch_get_threads": (C.c_int, [_P, _I32P]),
+    "ocm_batch_set_list_smem": (C.c_int, [_P, C.c_int32]),
+    "ocm_batch_slot_stats": (C.c_int, [_P, C.c_int64, _I32P, _I32P]),
 }
 
 

@@ -45,7 +45,9 @@ struct BatchArgs {
     int nmax;
     double* energy;              // [slot][kNumSlots]
     unsigned long long* forces;  // eval output [3][nmax]
+    uint16_t* lists;             // neighbour-list arena
     uint32_t slots_enabled;
+    size_t smem_bytes;           // dynamic shared memory of the launch
 };
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -196,20 +198,141 @@ __device__ __forceinline__ bool bbox_close(float4 ci, float4 hi, float4 cj, floa
     return gx * gx + gy * gy + gz * gz < cut2;
 }
 
+// Neighbour list of every bead of the claimed system, built by one thread
+// per bead: all j != i whose FP32 r^2 (canonical form) is below cut2, in
+// increasing j, so the list and every FP32 sum over it are deterministic.
+// Entry = j | (excluded-term bits << 11); pairs excluded for every present
+// term are dropped.  Entry k of bead i lives in shared memory at
+// slist[k * npad + i] for k < cap_s and in global memory at
+// glist[k * npad + i] for cap_s <= k < maxn.  Sets *overflow when a list
+// exceeds maxn.
+template <bool LABELS>
+__device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, int cap_s, float cut2,
+                                            const float4* sx, const uint32_t* slab,
+                                            const float4* bc, const float4* bh,
+                                            const int32_t* __restrict__ ex_start,
+                                            const int32_t* __restrict__ ex,
+                                            const PairConsts& pc, uint16_t* slist,
+                                            uint16_t* __restrict__ glist, uint16_t* scnt,
+                                            float* sref, int nmax, int tid, int threads,
+                                            int* overflow) {
+    const float3 nobox = make_float3(0.f, 0.f, 0.f);
+    const uint32_t present = (uint32_t)pc.terms;
+    for (int i = tid; i < n; i += threads) {
+        const float4 xi = sx[i];
+        const uint32_t labi = LABELS ? slab[i] : 0u;
+        int cnt = 0;
+        int ep = ex_start[i];
+        const int e1 = ex_start[i + 1];
+        int ej = ep < e1 ? (ex[ep] & 0xFFFFFF) : 0x7FFFFFFF;
+        for (int J = 0; J < nt; ++J) {
+            const float4 c = bc[J], h = bh[J];
+            const float gx = fmaxf(0.f, fabsf(xi.x - c.x) - h.x);
+            const float gy = fmaxf(0.f, fabsf(xi.y - c.y) - h.y);
+            const float gz = fmaxf(0.f, fabsf(xi.z - c.z) - h.z);
+            if (gx * gx + gy * gy + gz * gz >= cut2) continue;
+            const int j1 = min(n, J * 32 + 32);
+            for (int j = J * 32; j < j1; ++j) {
+                if (j == i) continue;
+                const float r2 = norm2(separation<false>(xi, sx[j], nobox, nobox));
+                if (!(r2 < cut2)) continue;
+                while (ej < j) {
+                    ++ep;
+                    ej = ep < e1 ? (ex[ep] & 0xFFFFFF) : 0x7FFFFFFF;
+                }
+                uint32_t bits = ej == j ? ((uint32_t)ex[ep] >> 24) : 0u;
+                if (LABELS) {
+                    const uint32_t labj = slab[j];
+#pragma unroll
+                    for (int term = 0; term < 4; ++term)
+                        if ((pc.uses_labels & (1 << term)) && !labels_allow(labi, labj, term, pc.allow[term]))
+                            bits |= 1u << term;
+                }
+                if ((bits & present) == present) continue;
+                const uint16_t e = (uint16_t)(j | (bits << 11));
+                if (cnt < cap_s) slist[cnt * npad + i] = e;
+                else if (cnt < maxn) glist[(size_t)cnt * npad + i] = e;
+                ++cnt;
+            }
+        }
+        if (cnt > maxn) {
+            atomicOr(overflow, 1);
+            cnt = maxn;
+        }
+        scnt[i] = (uint16_t)cnt;
+        sref[i] = xi.x;
+        sref[nmax + i] = xi.y;
+        sref[2 * nmax + i] = xi.z;
+    }
+}
+
+// Pair forces on bead i from its list, four entries per iteration so their
+// loads and arithmetic overlap.  One accumulator, in list (= increasing j)
+// order: entries outside the cutoff contribute nothing, so the FP32 sum does
+// not depend on when the list was built.
+template <int TERMS, bool ENERGY>
+__device__ __forceinline__ float3 list_forces(int i, int cnt, int cap_s, int npad,
+                                              const uint16_t* slist,
+                                              const uint16_t* __restrict__ glist,
+                                              const float4* sx, const float4* sp0,
+                                              const float4* sp1, uint32_t excl_all,
+                                              const PairConsts& pc, PairEnergy& e) {
+    const float3 nobox = make_float3(0.f, 0.f, 0.f);
+    const float4 xi = sx[i];
+    const float4 p0i = sp0[i];
+    const float4 p1i = (TERMS & kTermLJA) ? sp1[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float3 fa = make_float3(0.f, 0.f, 0.f);
+    for (int k = 0; k < cnt; k += 4) {
+        uint32_t ent[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int kk = k + u;
+            ent[u] = kk < cnt ? (kk < cap_s ? (uint32_t)slist[kk * npad + i]
+                                            : (uint32_t)glist[(size_t)kk * npad + i])
+                              : 0xFFFFFFFFu;
+        }
+        float4 xj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xj[u] = sx[ent[u] != 0xFFFFFFFFu ? (int)(ent[u] & 2047u) : i];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (ent[u] == 0xFFFFFFFFu) continue;
+            const int j = (int)(ent[u] & 2047u);
+            const float3 d = separation<false>(xi, xj[u], nobox, nobox);
+            const float r2 = norm2(d);
+            if (r2 < pc.list_rc2) {
+                const float4 p0j = sp0[j];
+                const float4 p1j = (TERMS & kTermLJA) ? sp1[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float s = pair_scalar<TERMS, ENERGY>(r2, p0i, p0j, p1i, p1j,
+                                                           (ent[u] >> 11) | excl_all, pc, e);
+                fa.x -= s * d.x;
+                fa.y -= s * d.y;
+                fa.z -= s * d.z;
+            }
+        }
+    }
+    return fa;
+}
+
+constexpr int kMaxBeadsPerThread = 8;  // 2048 beads / 256 threads
+
 template <int THREADS, int TERMS, bool LABELS, bool ENERGY, bool INTEGRATE>
 __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
     constexpr int NW = THREADS / 32;
+    constexpr int BPT = (32 * kMaxClusters + THREADS - 1) / THREADS;  // beads per thread
     extern __shared__ __align__(16) unsigned char smem[];
     const int nmax = a.nmax;
-    // Positions are float-float: hi parts in sx (used by the pair tiles),
-    // lo parts in sxl; x = hi + lo carries ~48 significant bits.
+    // Positions are float-float: hi parts in sx (pair arithmetic), lo parts
+    // in sxl; x = hi + lo carries ~48 significant bits.
     unsigned long long* sF = reinterpret_cast<unsigned long long*>(smem);
     float4* sx = reinterpret_cast<float4*>(smem + 24 * (size_t)nmax);
     float4* sp0 = reinterpret_cast<float4*>(smem + 40 * (size_t)nmax);
     float* sxl = reinterpret_cast<float*>(smem + 56 * (size_t)nmax);
     float* sv = reinterpret_cast<float*>(smem + 68 * (size_t)nmax);
     float* sim = reinterpret_cast<float*>(smem + 80 * (size_t)nmax);
-    size_t off = 84 * (size_t)nmax;
+    float* sref = reinterpret_cast<float*>(smem + 84 * (size_t)nmax);
+    uint16_t* scnt = reinterpret_cast<uint16_t*>(smem + 96 * (size_t)nmax);
+    size_t off = 98 * (size_t)nmax;
     float4* sp1 = nullptr;
     uint32_t* slab = nullptr;
     if ((TERMS & kTermLJA) || LABELS) {
@@ -219,14 +342,24 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
     }
     float4* bc = reinterpret_cast<float4*>(smem + off);
     float4* bh = bc + kMaxClusters;
+    off += 2 * kMaxClusters * sizeof(float4);
+    uint16_t* slist = reinterpret_cast<uint16_t*>(smem + off);
+    const size_t list_bytes = a.smem_bytes > off ? a.smem_bytes - off : 0;
     __shared__ int s_claim;
+    __shared__ int s_move[2];
+    __shared__ int s_overflow;
     __shared__ double s_energy[kNumSlots];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float nan = __int_as_float(0x7fc00000);
 
     while (true) {
-        if (tid == 0) s_claim = atomicAdd(a.head, 1);
+        if (tid == 0) {
+            s_claim = atomicAdd(a.head, 1);
+            s_move[0] = 0;
+            s_move[1] = 0;
+            s_overflow = 0;
+        }
         if (ENERGY && tid < kNumSlots) s_energy[tid] = 0.0;
         __syncthreads();
         const int q = s_claim;
@@ -249,6 +382,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         const FldTable* fld = reinterpret_cast<const FldTable*>(blob + R.off_fld);
         const int32_t* tmask = reinterpret_cast<const int32_t*>(blob + R.off_tmask);
         const uint32_t* masks = reinterpret_cast<const uint32_t*>(blob + R.off_masks);
+        const int32_t* ex_start = reinterpret_cast<const int32_t*>(blob + R.off_ex_start);
+        const int32_t* exl = reinterpret_cast<const int32_t*>(blob + R.off_ex);
+        uint16_t* glist = a.lists + R.list_off;
+        const int maxn = R.maxn;
+        // entries per bead kept in shared memory (multiple of 4)
+        const int cap_s = min(maxn, (int)(list_bytes / (2 * (size_t)npad)) & ~3);
+        const int n_bonds = R.n_bonds, n_angles = R.n_angles, n_dih = R.n_dih;
         const unsigned long long step0 = R.steps_done;
         int K = 1;
         if (INTEGRATE) {
@@ -261,6 +401,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         if (!(slots_en & (1u << kSlotDH))) excl_all |= kTermDH;
         if (!(slots_en & (1u << kSlotLJR))) excl_all |= kTermLJR;
         if (!(slots_en & (1u << kSlotLJA))) excl_all |= kTermLJA;
+        const bool pairs_on = (pc.terms & ~excl_all) != 0;
 
         // ---- load ----
         for (int b = tid; b < npad; b += THREADS) {
@@ -298,43 +439,114 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         for (int I = warp; I < nt; I += NW) cluster_bbox(I, n, sx, bc, bh, lane);
         __syncthreads();
 
-        const float cut = sqrtf(pc.list_rc2) * 1.0001f + 1e-4f;
-        const float cut2 = cut * cut;
+        // list cutoff = largest pair cutoff + skin; tiles use the cutoff alone
+        const float rc = sqrtf(pc.list_rc2);
+        const float lcut = (rc + R.skin) * 1.0001f;
+        const float lcut2 = lcut * lcut;
+        const float tcut = rc * 1.0001f + 1e-4f;
+        const float tcut2 = tcut * tcut;
+        const float half_skin2 = 0.25f * R.skin * R.skin;
+        bool use_tiles = false;
+        bool need_build = pairs_on;
+        int builds = 0;
         float eacc[kNumSlots];
 #pragma unroll
         for (int k = 0; k < kNumSlots; ++k) eacc[k] = 0.f;
 
         for (int st = 0; st < K; ++st) {
-            // ---- pair tiles (bounding-box culled) ----
-            if ((pc.terms & ~excl_all) != 0) {
+            if (need_build && !use_tiles) {
+                build_lists<LABELS>(n, nt, npad, maxn, cap_s, lcut2, sx, slab, bc, bh, ex_start, exl,
+                                    pc, slist, glist, scnt, sref, nmax, tid, THREADS, &s_overflow);
+                ++builds;
+                __syncthreads();
+                use_tiles = s_overflow != 0;
+            }
+            const unsigned long long step = step0 + (unsigned long long)st;
+            // Langevin noise for this thread's beads, drawn before the force
+            // work so its latency overlaps the pair loop.
+            float3 noise[BPT];
+            if (INTEGRATE) {
+#pragma unroll
+                for (int c = 0; c < BPT; ++c) {
+                    const int b = tid + c * THREADS;
+                    noise[c] = b < n ? gaussian3(lc.seed, lc.stream, (uint32_t)b, step, kPurposeLangevin)
+                                     : make_float3(0.f, 0.f, 0.f);
+                }
+            }
+            // ---- bonded parameters: issue every load before any math ----
+            BondTerm bt[2];
+            AngleTerm at;
+            DihedralTerm dt;
+            const bool has_b0 = tid < n_bonds, has_b1 = tid + THREADS < n_bonds;
+            if (has_b0) bt[0] = bonds[tid];
+            if (has_b1) bt[1] = bonds[tid + THREADS];
+            const bool has_a = tid < n_angles, has_d = tid < n_dih;
+            if (has_a) at = angles[tid];
+            if (has_d) dt = dih[tid];
+            // ---- pair terms ----
+            if (pairs_on && !use_tiles) {
+#pragma unroll
+                for (int c = 0; c < BPT; ++c) {
+                    const int i = tid + c * THREADS;
+                    if (i >= n) break;
+                    PairEnergy e;
+                    e.zero();
+                    const float3 fi = list_forces<TERMS, ENERGY>(i, scnt[i], cap_s, npad, slist, glist,
+                                                                 sx, sp0, sp1, excl_all, pc, e);
+                    sadd(sF, nmax, i, fi);
+                    if (ENERGY) {
+                        // every pair appears in both lists
+                        eacc[kSlotEXV] += 0.5f * e.exv;
+                        eacc[kSlotDH] += 0.5f * e.dh;
+                        eacc[kSlotLJR] += 0.5f * e.ljr;
+                        eacc[kSlotLJA] += 0.5f * e.lja;
+                    }
+                }
+            } else if (pairs_on) {
                 for (int t = warp; t < R.n_tiles; t += NW) {
                     int J = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
                     while ((J + 1) * (J + 2) / 2 <= t) ++J;
                     while (J * (J + 1) / 2 > t) --J;
                     const int I = t - J * (J + 1) / 2;
-                    if (!bbox_close(bc[I], bh[I], bc[J], bh[J], cut2)) continue;
+                    if (!bbox_close(bc[I], bh[I], bc[J], bh[J], tcut2)) continue;
                     batch_tile<TERMS, LABELS, ENERGY>(I, J, tmask[t], masks, sx, sp0, sp1, slab, sF,
                                                       nmax, pc, excl_all, lane, eacc);
                 }
             }
             // ---- bonded ----
-            for (int b = tid; b < R.n_bonds; b += THREADS) {
-                const BondTerm bt = bonds[b];
-                const int sl = bt.kind == kBondHarmonic ? kSlotHB : kSlotGO;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (!(u == 0 ? has_b0 : has_b1)) continue;
+                const BondTerm& bb = bt[u];
+                const int sl = bb.kind == kBondHarmonic ? kSlotHB : kSlotGO;
                 if (!(slots_en & (1u << sl))) continue;
                 float3 dh, dl;
-                ff_sep(sx[bt.i], lo3(sxl, nmax, bt.i), sx[bt.j], lo3(sxl, nmax, bt.j), dh, dl);
+                ff_sep(sx[bb.i], lo3(sxl, nmax, bb.i), sx[bb.j], lo3(sxl, nmax, bb.j), dh, dl);
                 const float3 d = make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
-                const float delta = ff_bond_delta(dh, dl, bt.r0sq_hi, bt.r0sq_lo);
+                const float delta = ff_bond_delta(dh, dl, bb.r0sq_hi, bb.r0sq_lo);
                 float en;
-                const float s = bond_scalar(bt.kind, norm2(d), delta, bt.p0, bt.p1, en);
-                sadd(sF, nmax, bt.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
-                sadd(sF, nmax, bt.j, make_float3(s * d.x, s * d.y, s * d.z));
+                const float s = bond_scalar(bb.kind, norm2(d), delta, bb.p0, bb.p1, en);
+                sadd(sF, nmax, bb.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
+                sadd(sF, nmax, bb.j, make_float3(s * d.x, s * d.y, s * d.z));
+                if (ENERGY) eacc[sl] += en;
+            }
+            for (int b = tid + 2 * THREADS; b < n_bonds; b += THREADS) {
+                const BondTerm bb = bonds[b];
+                const int sl = bb.kind == kBondHarmonic ? kSlotHB : kSlotGO;
+                if (!(slots_en & (1u << sl))) continue;
+                float3 dh, dl;
+                ff_sep(sx[bb.i], lo3(sxl, nmax, bb.i), sx[bb.j], lo3(sxl, nmax, bb.j), dh, dl);
+                const float3 d = make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
+                const float delta = ff_bond_delta(dh, dl, bb.r0sq_hi, bb.r0sq_lo);
+                float en;
+                const float s = bond_scalar(bb.kind, norm2(d), delta, bb.p0, bb.p1, en);
+                sadd(sF, nmax, bb.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
+                sadd(sF, nmax, bb.j, make_float3(s * d.x, s * d.y, s * d.z));
                 if (ENERGY) eacc[sl] += en;
             }
             if (slots_en & (1u << kSlotFLA)) {
-                for (int b = tid; b < R.n_angles; b += THREADS) {
-                    const AngleTerm g = angles[b];
+                for (int b = tid; b < n_angles; b += THREADS) {
+                    const AngleTerm g = b == tid ? at : angles[b];
                     const float3 u = ffsep(sx, sxl, nmax, g.j, g.i);
                     const float3 v = ffsep(sx, sxl, nmax, g.j, g.k);
                     float3 f1, f3;
@@ -347,8 +559,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                 }
             }
             if (slots_en & (1u << kSlotFLD)) {
-                for (int b = tid; b < R.n_dih; b += THREADS) {
-                    const DihedralTerm qd = dih[b];
+                for (int b = tid; b < n_dih; b += THREADS) {
+                    const DihedralTerm qd = b == tid ? dt : dih[b];
                     const float3 F = ffsep(sx, sxl, nmax, qd.j, qd.i);
                     const float3 G = ffsep(sx, sxl, nmax, qd.k, qd.j);
                     const float3 H = ffsep(sx, sxl, nmax, qd.k, qd.l);
@@ -362,12 +574,19 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                     if (ENERGY) eacc[kSlotFLD] += en;
                 }
             }
+            (void)has_a;
+            (void)has_d;
             __syncthreads();
             if (!INTEGRATE) break;
-            // ---- Langevin update + bounding boxes ----
-            const unsigned long long step = step0 + (unsigned long long)st;
-            for (int I = warp; I < nt; I += NW) {
+            // ---- Langevin update, bounding boxes, displacement check ----
+            // Bead b = tid + c * THREADS is cluster b / 32 handled by this warp.
+            const int mv = st & 1;
+#pragma unroll
+            for (int c = 0; c < BPT; ++c) {
+                const int I = warp + c * NW;
+                if (I >= nt) break;
                 const int b = I * 32 + lane;
+                bool moved = false;
                 if (b < n) {
                     const float fx = (float)((double)(long long)sF[b] * kFixedInv);
                     const float fy = (float)((double)(long long)sF[nmax + b] * kFixedInv);
@@ -377,7 +596,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                     sF[2 * nmax + b] = 0ull;
                     const float im = sim[b];
                     if (im > 0.f) {
-                        const float3 g = gaussian3(lc.seed, lc.stream, (uint32_t)b, step, kPurposeLangevin);
+                        const float3 g = noise[c];
                         const float sq = sqrtf(im) * lc.noise;
                         const float fs = lc.fscale * im;
                         const float vx = lc.vscale * sv[b] + fs * fx + sq * g.x;
@@ -391,12 +610,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                         ff_add(h.y, sxl[nmax + b], vy * lc.dt);
                         ff_add(h.z, sxl[2 * nmax + b], vz * lc.dt);
                         sx[b] = h;
+                        const float dx = h.x - sref[b], dy = h.y - sref[nmax + b], dz = h.z - sref[2 * nmax + b];
+                        moved = dx * dx + dy * dy + dz * dz > half_skin2;
                     }
                 }
+                if (__any_sync(kFull, moved) && lane == 0) atomicOr(&s_move[mv], 1);
                 __syncwarp();
                 cluster_bbox(I, n, sx, bc, bh, lane);
             }
             __syncthreads();
+            need_build = s_move[mv] != 0;
+            if (tid == 0) s_move[mv ^ 1] = 0;
         }
 
         // ---- write back ----
@@ -410,13 +634,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                 a.vy[boff + b] = sv[nmax + b];
                 a.vz[boff + b] = sv[2 * nmax + b];
             }
-            if (tid == 0) a.sys[slot].steps_done = step0 + (unsigned long long)K;
+            if (tid == 0) {
+                a.sys[slot].steps_done = step0 + (unsigned long long)K;
+                a.sys[slot].builds = builds;
+                if (s_overflow) a.sys[slot].overflow = 1;
+            }
         } else {
             for (int b = tid; b < n; b += THREADS) {
                 a.forces[b] = sF[b];
                 a.forces[nmax + b] = sF[nmax + b];
                 a.forces[2 * nmax + b] = sF[2 * nmax + b];
             }
+            if (tid == 0 && s_overflow) a.sys[slot].overflow = 1;
         }
         if (ENERGY) {
 #pragma unroll
@@ -443,36 +672,52 @@ __global__ void k_batch_velocity_init(int n, long long off, const float* __restr
     vz[off + i] = s * g.z;
 }
 
+// Persistent launch: as many CTAs as fit, each given an equal share of the
+// SM's shared memory (the state needs `smem`; the rest holds neighbour
+// lists).
 template <typename Fn>
-void launch_persistent(Fn fn, int threads, const BatchArgs& a, int max_grid, size_t smem,
-                       cudaStream_t s, int num_sms) {
-    OCM_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+void launch_persistent(Fn fn, int threads, BatchArgs a, int max_grid, size_t smem,
+                       cudaStream_t s, int num_sms, int list_smem_kib) {
+    int optin = 0, per_sm_smem = 0, dev = 0;
+    OCM_CK(cudaGetDevice(&dev));
+    OCM_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    OCM_CK(cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    cudaFuncAttributes fa{};
+    OCM_CK(cudaFuncGetAttributes(&fa, fn));
+    const int max_dyn = optin - (int)fa.sharedSizeBytes;
+    OCM_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn));
     int per_sm = 0;
     OCM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
     if (per_sm < 1) throw Error(6, "[error] batched kernel does not fit on an SM");
+    size_t share = (size_t)per_sm_smem / per_sm;
+    share = share > 2048 ? share - 2048 : share;  // static + reserved per block
+    share = std::min<size_t>(share, (size_t)max_dyn);
+    if (list_smem_kib >= 0) share = std::min(share, smem + (size_t)list_smem_kib * 1024);
+    share = std::max(share, smem) & ~(size_t)15;
+    a.smem_bytes = share;
     const int grid = std::max(1, std::min(max_grid, num_sms * per_sm));
-    fn<<<grid, threads, smem, s>>>(a);
+    fn<<<grid, threads, share, s>>>(a);
     OCM_CK(cudaGetLastError());
 }
 
 template <int THREADS, int TERMS, bool LABELS>
 void launch_batch_t(const BatchArgs& a, int max_grid, size_t smem, cudaStream_t s, bool integrate,
-                    bool energy, int num_sms) {
+                    bool energy, int num_sms, int lkib) {
     if (integrate)
-        launch_persistent(k_batch<THREADS, TERMS, LABELS, false, true>, THREADS, a, max_grid, smem, s, num_sms);
+        launch_persistent(k_batch<THREADS, TERMS, LABELS, false, true>, THREADS, a, max_grid, smem, s, num_sms, lkib);
     else if (energy)
-        launch_persistent(k_batch<THREADS, TERMS, LABELS, true, false>, THREADS, a, max_grid, smem, s, num_sms);
+        launch_persistent(k_batch<THREADS, TERMS, LABELS, true, false>, THREADS, a, max_grid, smem, s, num_sms, lkib);
     else
-        launch_persistent(k_batch<THREADS, TERMS, LABELS, false, false>, THREADS, a, max_grid, smem, s, num_sms);
+        launch_persistent(k_batch<THREADS, TERMS, LABELS, false, false>, THREADS, a, max_grid, smem, s, num_sms, lkib);
 }
 
 template <int TERMS, bool LABELS>
 void launch_batch_threads(int threads, const BatchArgs& a, int grid, size_t smem, cudaStream_t s,
-                          bool integrate, bool energy, int num_sms) {
+                          bool integrate, bool energy, int num_sms, int lkib) {
     switch (threads) {
-        case 256: launch_batch_t<256, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms); break;
-        case 512: launch_batch_t<512, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms); break;
-        default: launch_batch_t<1024, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms); break;
+        case 256: launch_batch_t<256, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms, lkib); break;
+        case 512: launch_batch_t<512, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms, lkib); break;
+        default: launch_batch_t<1024, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms, lkib); break;
     }
 }
 
@@ -481,7 +726,7 @@ int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 struct BlobLayout {
     int64_t size = 0;
     int off_p0, off_p1, off_lab, off_invm, off_bonds, off_angles, off_dih, off_fla, off_fld,
-        off_tmask, off_masks;
+        off_tmask, off_masks, off_ex_start, off_ex;
     int n_tiles, n_masks;
 };
 
@@ -508,6 +753,8 @@ BlobLayout blob_layout(const CompiledSystem& c, int n_masks) {
     L.off_fld = take((int64_t)sizeof(FldTable) * c.fld.size());
     L.off_tmask = take(4 * (int64_t)L.n_tiles);
     L.off_masks = take(4 * 128 * (int64_t)n_masks);
+    L.off_ex_start = take(4 * (n + 1));
+    L.off_ex = take(4 * (int64_t)c.ex_j.size());
     L.size = align_up(o, 256);
     return L;
 }
@@ -536,6 +783,30 @@ void build_masks(const CompiledSystem& c, std::vector<int32_t>& tmask, std::vect
             }
         }
     }
+}
+
+constexpr float kBatchSkin = 0.3f;  // nm
+
+// Entries per bead of a system's neighbour list: the largest count within
+// the list cutoff at admission, with head-room for compaction.
+int initial_list_capacity(const CompiledSystem& c, const double* pos) {
+    const int64_t n = c.n;
+    if (c.pc.terms == 0) return 1;
+    const double cut = std::sqrt((double)c.pc.list_rc2) + kBatchSkin;
+    const double cut2 = cut * cut;
+    int mx = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        int cnt = 0;
+        for (int64_t j = 0; j < n; ++j) {
+            if (j == i) continue;
+            const double dx = pos[3 * j] - pos[3 * i], dy = pos[3 * j + 1] - pos[3 * i + 1],
+                         dz = pos[3 * j + 2] - pos[3 * i + 2];
+            cnt += dx * dx + dy * dy + dz * dz < cut2;
+        }
+        mx = std::max(mx, cnt);
+    }
+    const int cap = (int)std::ceil(1.25 * mx) + 16;
+    return (int)std::min<int64_t>(std::max<int64_t>(1, n - 1), align_up(cap, 4));
 }
 
 void check_batchable(const CompiledSystem& c, int nmax) {
@@ -616,6 +887,11 @@ BatchEngine::BatchEngine(int device, int64_t max_systems, int64_t max_beads, int
     x_.alloc(max_beads); y_.alloc(max_beads); z_.alloc(max_beads);
     vx_.alloc(max_beads); vy_.alloc(max_beads); vz_.alloc(max_beads);
     blob_dev_.alloc(blob_cap);
+    const int64_t list_cap = max_beads * 256 + max_systems * 1024;
+    list_alloc_.reset(list_cap);
+    lists_.alloc(list_cap);
+    OCM_CK(cudaMallocHost(&h_overflow_, sizeof(int) * max_systems));
+    std::memset(h_overflow_, 0, sizeof(int) * max_systems);
     sys_.alloc(max_systems);
     OCM_CK(cudaMemset(sys_.p, 0, sizeof(BatchSys) * max_systems));
     order_.alloc(max_systems);
@@ -631,12 +907,13 @@ BatchEngine::~BatchEngine() {
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
     if (ev_copy_) cudaEventDestroy(ev_copy_);
+    if (h_overflow_) cudaFreeHost(h_overflow_);
     if (stream_) cudaStreamDestroy(stream_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
 }
 
 size_t BatchEngine::smem_bytes(int nmax, bool general) const {
-    return (size_t)nmax * (general ? 104 : 84) + 2 * kMaxClusters * sizeof(float4);
+    return (size_t)nmax * (general ? 118 : 98) + 2 * kMaxClusters * sizeof(float4);
 }
 
 int64_t BatchEngine::footprint(const SystemDesc& d) {
@@ -646,6 +923,11 @@ int64_t BatchEngine::footprint(const SystemDesc& d) {
     build_masks(c, tm, mk);
     const BlobLayout L = blob_layout(c, (int)(mk.size() / 128));
     return L.size + c.n * (3 * 8 + 3 * 4) + (int64_t)sizeof(BatchSys);
+}
+
+void BatchEngine::set_list_smem(int kib) {
+    if (kib < -1 || kib > 228) throw Error(1, "[error] list shared memory must be -1 or 0..228 KiB");
+    list_smem_kib_ = kib;
 }
 
 void BatchEngine::set_threads(int threads) {
@@ -675,12 +957,21 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     std::vector<uint32_t> masks;
     build_masks(c, tmask, masks);
     const BlobLayout L = blob_layout(c, (int)(masks.size() / 128));
+    const int npad = (int)align_up(n, 32);
+    const int maxn = initial_list_capacity(c, pos);
     const int64_t boff = beads_.alloc(n, 1);
     if (boff < 0) throw Error(3, "[error] batch bead capacity exhausted");
     const int64_t blob_off = blob_.alloc(L.size, 256);
     if (blob_off < 0) {
         beads_.release(boff, n);
         throw Error(3, "[error] batch parameter memory exhausted");
+    }
+    const int64_t list_size = (int64_t)maxn * npad;
+    const int64_t list_off = list_alloc_.alloc(list_size, 64);
+    if (list_off < 0) {
+        beads_.release(boff, n);
+        blob_.release(blob_off, L.size);
+        throw Error(3, "[error] batch neighbour-list memory exhausted");
     }
     // host blob
     std::vector<unsigned char> blob(L.size, 0);
@@ -698,6 +989,12 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     put(L.off_fld, c.fld.data(), sizeof(FldTable) * c.fld.size());
     put(L.off_tmask, tmask.data(), 4 * tmask.size());
     put(L.off_masks, masks.data(), 4 * masks.size());
+    {
+        std::vector<int32_t> ex(c.ex_j.size());
+        for (size_t e = 0; e < ex.size(); ++e) ex[e] = c.ex_j[e] | ((int32_t)c.ex_bits[e] << 24);
+        put(L.off_ex_start, c.ex_start.data(), 4 * c.ex_start.size());
+        put(L.off_ex, ex.data(), 4 * ex.size());
+    }
 
     BatchSys R{};
     R.bead_off = boff;
@@ -712,6 +1009,10 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     R.off_p0 = L.off_p0; R.off_p1 = L.off_p1; R.off_lab = L.off_lab; R.off_invm = L.off_invm;
     R.off_bonds = L.off_bonds; R.off_angles = L.off_angles; R.off_dih = L.off_dih;
     R.off_fla = L.off_fla; R.off_fld = L.off_fld; R.off_tmask = L.off_tmask; R.off_masks = L.off_masks;
+    R.off_ex_start = L.off_ex_start; R.off_ex = L.off_ex;
+    R.skin = kBatchSkin;
+    R.maxn = maxn;
+    R.list_off = list_off;
     R.active = 1;
     R.pc = c.pc;
     const double vscale = std::exp(-friction * dt);
@@ -767,6 +1068,9 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     S.blob_size = L.size;
     S.steps_target = (uint64_t)n_steps;
     S.steps_done = 0;
+    S.list_off = list_off;
+    S.list_size = list_size;
+    S.maxn = maxn;
     S.terms = c.pc.terms;
     S.labels = c.pc.uses_labels != 0;
     for (int k = 0; k < kNumSlots; ++k) S.slot_group[k] = c.slot_group[k];
@@ -806,12 +1110,14 @@ void BatchEngine::launch(bool integrate, bool energy, int k, const std::vector<i
     a.nmax = nmax_;
     a.energy = energy_.p;
     a.forces = forces_.p;
+    a.lists = lists_.p;
     a.slots_enabled = 0xffffffffu;
     const int grid = (int)order.size();
     if (general)
-        launch_batch_threads<15, true>(threads_, a, grid, smem, s, integrate, energy, num_sms_);
+        launch_batch_threads<15, true>(threads_, a, grid, smem, s, integrate, energy, num_sms_, list_smem_kib_);
     else
-        launch_batch_threads<kTermEXV | kTermDH, false>(threads_, a, grid, smem, s, integrate, energy, num_sms_);
+        launch_batch_threads<kTermEXV | kTermDH, false>(threads_, a, grid, smem, s, integrate, energy, num_sms_,
+                                                         list_smem_kib_);
 }
 
 void BatchEngine::run(int32_t k, bool sync) {
@@ -822,10 +1128,13 @@ void BatchEngine::run(int32_t k, bool sync) {
         if (slots_[s].used && slots_[s].steps_done < slots_[s].steps_target) order.push_back((int32_t)s);
     std::stable_sort(order.begin(), order.end(),
                      [&](int32_t a, int32_t b) { return slots_[a].cost > slots_[b].cost; });
+    grow_lists();
     OCM_CK(cudaStreamWaitEvent(stream_, ev_copy_, 0));
     OCM_CK(cudaEventRecord(ev0_, stream_));
     if (!order.empty()) launch(true, false, k, order, stream_);
     OCM_CK(cudaEventRecord(ev1_, stream_));
+    OCM_CK(cudaMemcpy2DAsync(h_overflow_, sizeof(int), &sys_.p[0].overflow, sizeof(BatchSys),
+                             sizeof(int), max_systems_, cudaMemcpyDeviceToHost, stream_));
     ran_ = true;
     for (int32_t q : order)
         slots_[q].steps_done = std::min<uint64_t>(slots_[q].steps_target, slots_[q].steps_done + k);
@@ -842,6 +1151,41 @@ double BatchEngine::last_run_ms() {
 }
 
 void BatchEngine::sync_steps() { OCM_CK(cudaStreamSynchronize(stream_)); }
+
+// A list that overflowed made its system fall back to the tile sweep for
+// the rest of that chunk (same results, more work); give it more room now.
+void BatchEngine::grow_lists() {
+    if (!ran_) return;
+    OCM_CK(cudaStreamSynchronize(stream_));
+    for (int64_t s = 0; s < max_systems_; ++s) {
+        if (!h_overflow_[s] || !slots_[s].used) continue;
+        h_overflow_[s] = 0;
+        Slot& S = slots_[s];
+        const int npad = (int)align_up(S.n, 32);
+        const int maxn = (int)std::min<int64_t>(std::max<int64_t>(1, S.n - 1), align_up(S.maxn * 3 / 2 + 8, 4));
+        const int64_t size = (int64_t)maxn * npad;
+        list_alloc_.release(S.list_off, S.list_size);
+        const int64_t off = list_alloc_.alloc(size, 64);
+        if (off < 0) {
+            const int64_t back = list_alloc_.alloc(S.list_size, 64);
+            (void)back;
+            throw Error(3, "[error] batch neighbour-list memory exhausted while growing a list");
+        }
+        S.list_off = off;
+        S.list_size = size;
+        S.maxn = maxn;
+        sys_host_[s].list_off = off;
+        sys_host_[s].maxn = maxn;
+        sys_host_[s].overflow = 0;
+        BatchSys* dst = sys_.p + s;
+        OCM_CK(cudaMemcpyAsync(&dst->list_off, &sys_host_[s].list_off, sizeof(long long),
+                               cudaMemcpyHostToDevice, stream_));
+        OCM_CK(cudaMemcpyAsync(&dst->maxn, &sys_host_[s].maxn, sizeof(int), cudaMemcpyHostToDevice, stream_));
+        OCM_CK(cudaMemcpyAsync(&dst->overflow, &sys_host_[s].overflow, sizeof(int),
+                               cudaMemcpyHostToDevice, stream_));
+        OCM_CK(cudaStreamSynchronize(stream_));
+    }
+}
 
 void BatchEngine::finished(int64_t* out, int64_t cap, int64_t* n_out) {
     OCM_CK(cudaSetDevice(device_));
@@ -913,9 +1257,11 @@ void BatchEngine::get_state(int64_t slot, uint32_t groups, double* forces, doubl
         a.sys = sys_.p; a.order = order_.p; a.n_order = 1; a.head = head_.p;
         a.x = x_.p; a.y = y_.p; a.z = z_.p; a.vx = vx_.p; a.vy = vy_.p; a.vz = vz_.p;
         a.blob = blob_dev_.p; a.k = 0; a.nmax = nmax_; a.energy = energy_.p; a.forces = forces_.p;
+        a.lists = lists_.p;
         a.slots_enabled = en;
-        if (general) launch_batch_threads<15, true>(threads_, a, 1, smem, stream_, false, true, num_sms_);
-        else launch_batch_threads<kTermEXV | kTermDH, false>(threads_, a, 1, smem, stream_, false, true, num_sms_);
+        if (general) launch_batch_threads<15, true>(threads_, a, 1, smem, stream_, false, true, num_sms_, list_smem_kib_);
+        else launch_batch_threads<kTermEXV | kTermDH, false>(threads_, a, 1, smem, stream_, false, true, num_sms_,
+                                                              list_smem_kib_);
     }
     std::vector<unsigned long long> f(3 * nmax_);
     double e[kNumSlots];
@@ -941,11 +1287,22 @@ void BatchEngine::retire(int64_t slot) {
     Slot& S = slots_[slot];
     beads_.release(S.bead_off, S.n);
     blob_.release(S.blob_off, S.blob_size);
+    list_alloc_.release(S.list_off, S.list_size);
     S = Slot();
     BatchSys R{};
     sys_host_[slot] = R;
     OCM_CK(cudaMemcpyAsync(sys_.p + slot, &sys_host_[slot], sizeof(BatchSys), cudaMemcpyHostToDevice, stream_));
     OCM_CK(cudaStreamSynchronize(stream_));
+}
+
+void BatchEngine::slot_stats(int64_t slot, int32_t* builds, int32_t* capacity) {
+    OCM_CK(cudaSetDevice(device_));
+    if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
+    sync_steps();
+    int b = 0;
+    OCM_CK(cudaMemcpy(&b, &sys_.p[slot].builds, sizeof(int), cudaMemcpyDeviceToHost));
+    *builds = b;
+    *capacity = slots_[slot].maxn;
 }
 
 void BatchEngine::active(int64_t* n_active, int64_t* beads) {

@@ -19,11 +19,17 @@ namespace ocm {
 struct BatchSys {
     long long bead_off;    // offset into the bead arena
     long long blob_off;    // byte offset of the static blob
+    long long list_off;    // offset (entries) of the neighbour-list region
     int n, nt, n_tiles;    // beads, 32-bead clusters, cluster pairs
     int n_bonds, n_angles, n_dih, n_masks;
     int off_p0, off_p1, off_lab, off_invm;   // byte offsets inside the blob
     int off_bonds, off_angles, off_dih, off_fla, off_fld, off_tmask, off_masks;
+    int off_ex_start, off_ex;                // exclusion CSR (j | bits << 24)
+    int maxn;              // neighbour-list entries per bead
     int active;
+    int overflow;          // set by the kernel when a list did not fit
+    int builds;            // list builds in the last chunk
+    float skin;
     PairConsts pc;
     LangevinConsts lc;
     unsigned long long steps_done, steps_target;
@@ -63,6 +69,8 @@ class BatchEngine {
     void active(int64_t* n_active, int64_t* beads);
     double last_run_ms();
     void set_threads(int threads);  // 256/512/1024 (autotuner)
+    void set_list_smem(int kib);    // -1 = all that fits (autotuner)
+    void slot_stats(int64_t slot, int32_t* builds, int32_t* capacity);
     int threads() const { return threads_; }
 
   private:
@@ -75,7 +83,10 @@ class BatchEngine {
         int terms = 0;
         bool labels = false;
         int slot_group[kNumSlots];
+        int64_t list_off = 0, list_size = 0;
+        int maxn = 0;
     };
+    void grow_lists();
     void sync_steps();
     void launch(bool integrate, bool energy, int k, const std::vector<int32_t>& order,
                 cudaStream_t s);
@@ -85,15 +96,18 @@ class BatchEngine {
     int64_t max_systems_, max_beads_;
     int nmax_;
     int threads_ = 1024;
+    int list_smem_kib_ = 0;
     int num_sms_ = 0;
     cudaStream_t stream_ = nullptr, copy_stream_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, ev_copy_ = nullptr;
     bool ran_ = false;
     std::vector<Slot> slots_;
-    RangeAllocator beads_, blob_;
+    RangeAllocator beads_, blob_, list_alloc_;
     DevBuf<double> x_, y_, z_;
     DevBuf<float> vx_, vy_, vz_;
     DevBuf<unsigned char> blob_dev_;
+    DevBuf<uint16_t> lists_;
+    int* h_overflow_ = nullptr;  // pinned copy of the records' overflow flags
     DevBuf<BatchSys> sys_;
     DevBuf<int32_t> order_, head_;
     DevBuf<double> energy_;

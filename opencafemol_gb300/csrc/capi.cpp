@@ -481,5 +481,18 @@ int ocm_batch_active(ocm_batch* batch, int64_t* n_active, int64_t* beads) {
 int ocm_batch_last_run_ms(ocm_batch* batch, double* ms) {
     BATCH_CALL(need(ms, "ms"); *ms = batch->b->last_run_ms());
 }
+int ocm_batch_set_threads(ocm_batch* batch, int32_t threads) {
+    BATCH_CALL(batch->b->set_threads(threads));
+}
+int ocm_batch_set_list_smem(ocm_batch* batch, int32_t kib) {
+    BATCH_CALL(batch->b->set_list_smem(kib));
+}
+int ocm_batch_get_threads(ocm_batch* batch, int32_t* threads) {
+    BATCH_CALL(need(threads, "threads"); *threads = batch->b->threads());
+}
+int ocm_batch_slot_stats(ocm_batch* batch, int64_t slot, int32_t* builds, int32_t* capacity) {
+    BATCH_CALL(need(builds, "builds"); need(capacity, "capacity");
+               batch->b->slot_stats(slot, builds, capacity));
+}
 
 }  // extern "C"

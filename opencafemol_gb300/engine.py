@@ -181,6 +181,22 @@ class Batch:
         check(lib.ocm_batch_active(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def set_threads(self, threads_per_cta: int) -> None:
+        check(lib.ocm_batch_set_threads(self._h, int(threads_per_cta)))
+
+    def set_list_smem(self, kib: int) -> None:
+        check(lib.ocm_batch_set_list_smem(self._h, int(kib)))
+
+    def threads(self) -> int:
+        t = C.c_int32()
+        check(lib.ocm_batch_get_threads(self._h, C.byref(t)))
+        return t.value
+
+    def slot_stats(self, slot: int) -> dict:
+        b, c = C.c_int32(), C.c_int32()
+        check(lib.ocm_batch_slot_stats(self._h, int(slot), C.byref(b), C.byref(c)))
+        return {"list_builds": b.value, "list_capacity": c.value}
+
     def last_run_ms(self) -> float:
         ms = C.c_double()
         check(lib.ocm_batch_last_run_ms(self._h, C.byref(ms)))
