@@ -35,6 +35,10 @@ SIZE_LO, SIZE_HI = 50, 800
 SEED = 2024
 
 
+def local_device() -> int:
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
 def ensemble_specs(count=N_SYSTEMS, seed=SEED):
     from opencafemol_gb300 import synth
     sizes = synth.ensemble_sizes(count, SIZE_LO, SIZE_HI, seed)
@@ -138,9 +142,9 @@ def run_ours(args, rank, world):
     total_steps = (args.warmup + args.steps + 2) * K
 
     batch = ocm.Batch(max_systems=len(specs), max_total_beads=beads + 1024,
-                      max_beads_per_system=SIZE_HI)
+                      max_beads_per_system=SIZE_HI, device=local_device())
     if args.threads:
-        pass
+        batch.set_threads(args.threads)
     slots = [batch.admit(sysobj, s.pos, temperature=s.temperature, friction=s.friction,
                          step_size=s.dt, seed=1000 + k, n_steps=10 ** 12)
              for k, (sysobj, s) in enumerate(zip(systems, specs))]
@@ -151,7 +155,7 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     dist_barrier(world)
     times = []
-    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+    with ClockSampler(local_device()) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             flush_l2()
@@ -170,6 +174,9 @@ def run_ours(args, rank, world):
 
     # ---- plain single-system path on a sample of the same mix ----
     plain = run_plain(ocm, specs, systems, args)
+
+    # ---- served stream (continuous batching), p50/p99 completion latency ----
+    serve = run_serving(ocm, args) if args.serve_requests > 0 and rank == 0 else None
 
     # ---- roofline of the batched kernel (FP32-issue bound) ----
     pc = pair_counts(specs)
@@ -199,6 +206,7 @@ def run_ours(args, rank, world):
                    "l2": "flushed (256 MiB write) between timed launches"},
         "e2e": e2e, "gpu_launches": args.steps, "roofline": roof, "cpu_baseline": cpu,
         "plain_path": plain,
+        "serving": serve,
         "batched_vs_plain": value / world / plain["value"] if plain and plain.get("value") else None,
         "clocks": clk.summary(), "wall_s": wall,
     }
@@ -206,36 +214,67 @@ def run_ours(args, rank, world):
 
 
 def run_e2e(ocm, synth, specs, systems, args, world):
-    """Each step: upload every replica's state from pinned host buffers
-    (admission), run K MD steps, read back every replica's positions."""
+    """End to end through the public API with host buffers: every step
+    uploads every replica's positions and velocities from pinned host memory
+    (one copy), runs K MD steps and reads every replica's positions back
+    (one copy)."""
     import torch
     K = args.md_steps
     beads = int(sum(s.n for s in specs))
     batch = ocm.Batch(max_systems=len(specs), max_total_beads=beads + 1024,
-                      max_beads_per_system=SIZE_HI)
-    host_pos = [torch.from_numpy(s.pos.copy()).pin_memory().numpy() for s in specs]
-    steps = max(1, min(args.steps, 3))
-    h2d = d2h = 0
-    t_total = 0.0
-    for it in range(steps + 1):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        slots = [batch.admit(sysobj, host_pos[k], temperature=s.temperature, step_size=s.dt,
-                             seed=17 + k, n_steps=K)
-                 for k, (sysobj, s) in enumerate(zip(systems, specs))]
+                      max_beads_per_system=SIZE_HI, device=local_device())
+    if args.threads:
+        batch.set_threads(args.threads)
+    slots = [batch.admit(sysobj, s.pos, temperature=s.temperature, step_size=s.dt,
+                         seed=17 + k, n_steps=10 ** 12)
+             for k, (sysobj, s) in enumerate(zip(systems, specs))]
+    pos_in = torch.from_numpy(np.concatenate([s.pos for s in specs])).pin_memory()
+    vel_in = torch.zeros_like(pos_in).pin_memory()
+    pos_out = torch.zeros_like(pos_in).pin_memory()
+    pin, vin, pout = pos_in.numpy(), vel_in.numpy(), pos_out.numpy()
+    for _ in range(2):  # warm-up
+        batch.set_positions_many(slots, pin, vin)
         batch.run(K, sync=True)
-        outs = [batch.positions(sl) for sl in slots]
-        for sl in slots:
-            batch.retire(sl)
-        dt = time.perf_counter() - t0
-        if it > 0:  # first pass warms up
-            t_total += dt
-            h2d = sum(p.nbytes for p in host_pos)
-            d2h = sum(o.nbytes for o in outs)
-    t_total = dist_max(t_total, world)
-    return {"value": beads * K * steps * world / t_total, "unit": "bead-steps/s",
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "what": "admit (positions H2D, topology upload) + K MD steps + positions D2H, per step"}
+        batch.get_positions_many(slots, pout)
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.set_positions_many(slots, pin, vin)
+        batch.run(K, sync=True)
+        batch.get_positions_many(slots, pout)
+    t = dist_max(time.perf_counter() - t0, world)
+    return {"value": beads * K * args.steps * world / t, "unit": "bead-steps/s",
+            "h2d_bytes_per_step": int(pin.nbytes + vin.nbytes), "d2h_bytes_per_step": int(pout.nbytes),
+            "what": "positions+velocities H2D (pinned) -> K MD steps -> positions D2H, per step"}
+
+
+def run_serving(ocm, args):
+    """Continuous batching on a scaled request stream with the serving
+    config's shapes: Go proteins of 30..2000 beads (log-uniform), T~U[280,360],
+    Poisson arrivals at 200 req/s; step counts log-uniform in
+    [1e4, 1e6] / scale."""
+    from opencafemol_gb300 import serving, synth
+    rng = np.random.default_rng(4242)
+    n = args.serve_requests
+    sizes = serving.log_uniform_int(rng, 30, 2001, n)
+    steps = np.maximum(100, serving.log_uniform_int(rng, 1e4, 1e6, n) // args.serve_step_scale)
+    temps = rng.uniform(280.0, 360.0, n)
+    arrivals = serving.poisson_arrivals(n, args.serve_rate, seed=4243)
+    reqs = []
+    for k in range(n):
+        spec = synth.go_protein(int(sizes[k]), 90000 + k, temperature=float(temps[k]))
+        reqs.append(serving.Request(rid=k, arrival=float(arrivals[k]), system=synth.build_system(spec),
+                                    positions=spec.pos, temperature=float(temps[k]),
+                                    n_steps=int(steps[k]), seed=k))
+    server = serving.Server(max_systems=512, max_total_beads=300_000, max_beads_per_system=2048,
+                            chunk_steps=args.serve_chunk, device=local_device())
+    st = server.serve(reqs, realtime=True).summary()
+    offered = float(np.sum(sizes * steps) / arrivals[-1]) if n > 1 else None
+    st.update({"offered_bead_steps_per_s": offered, "rate_req_per_s": args.serve_rate,
+               "step_scale": args.serve_step_scale, "chunk_steps": args.serve_chunk,
+               "sizes": "log-uniform [30, 2000]", "steps": f"log-uniform [1e4, 1e6] / {args.serve_step_scale}"})
+    return st
 
 
 def run_plain(ocm, specs, systems, args):
@@ -247,7 +286,8 @@ def run_plain(ocm, specs, systems, args):
     t = 0.0
     for k in idx:
         s = specs[k]
-        ctx = ocm.Context(systems[k], ocm.LangevinIntegrator(s.temperature, s.friction, s.dt, 31 + k))
+        ctx = ocm.Context(systems[k], ocm.LangevinIntegrator(s.temperature, s.friction, s.dt, 31 + k),
+                          device=local_device())
         ctx.setPositions(s.pos)
         ctx.setVelocitiesToTemperature(s.temperature, 5)
         ctx.step(K)  # warm: graph capture
@@ -343,6 +383,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=48)
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--serve-requests", type=int, default=96)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-step-scale", type=int, default=50)
+    ap.add_argument("--serve-chunk", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 

@@ -257,6 +257,14 @@ int ocm_batch_run(ocm_batch* batch, int32_t steps_per_launch, int sync);
 int ocm_batch_finished(ocm_batch* batch, int64_t* slots, int64_t capacity, int64_t* n_out);
 int ocm_batch_get_positions(ocm_batch* batch, int64_t slot, double* xyz);
 int ocm_batch_get_velocities(ocm_batch* batch, int64_t slot, double* v);
+/* Replace the positions (and, if v is not NULL, velocities) of n slots in
+ * one host->device copy; xyz (and v) hold the slots' beads back to back in
+ * the order of `slots`. */
+int ocm_batch_set_positions_many(ocm_batch* batch, int64_t n, const int64_t* slots,
+                                 const double* xyz, const double* v);
+/* Read the positions of n slots, back to back in the order of `slots`, in
+ * one device->host copy. */
+int ocm_batch_get_positions_many(ocm_batch* batch, int64_t n, const int64_t* slots, double* xyz);
 int ocm_batch_steps_done(ocm_batch* batch, int64_t slot, int64_t* steps);
 /* Forces (3*n) and per-group energies (OCM_MAX_GROUPS) of one slot at its
  * current positions, evaluated by the batched kernel. */

@@ -1305,6 +1305,123 @@ void BatchEngine::slot_stats(int64_t slot, int32_t* builds, int32_t* capacity) {
     *capacity = slots_[slot].maxn;
 }
 
+// Scatter / gather of many slots' states through one pinned staging buffer
+// and one kernel, so a whole ensemble moves host<->device in two copies.
+namespace {
+__global__ void k_scatter_state(int nseg, const long long* __restrict__ seg_bead,
+                                const long long* __restrict__ seg_src, const int* __restrict__ seg_n,
+                                const double* __restrict__ src, int with_v, double* x, double* y,
+                                double* z, float* vx, float* vy, float* vz, long long total) {
+    const int g = blockIdx.y;
+    if (g >= nseg) return;
+    const int n = seg_n[g];
+    const long long b0 = seg_bead[g], s0 = seg_src[g];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const double* p = src + 3 * (s0 + k);
+        x[b0 + k] = p[0];
+        y[b0 + k] = p[1];
+        z[b0 + k] = p[2];
+        if (with_v) {
+            const double* q = src + 3 * total + 3 * (s0 + k);
+            vx[b0 + k] = (float)q[0];
+            vy[b0 + k] = (float)q[1];
+            vz[b0 + k] = (float)q[2];
+        }
+    }
+}
+__global__ void k_gather_pos(int nseg, const long long* __restrict__ seg_bead,
+                             const long long* __restrict__ seg_dst, const int* __restrict__ seg_n,
+                             const double* x, const double* y, const double* z, double* __restrict__ dst) {
+    const int g = blockIdx.y;
+    if (g >= nseg) return;
+    const int n = seg_n[g];
+    const long long b0 = seg_bead[g], d0 = seg_dst[g];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        double* p = dst + 3 * (d0 + k);
+        p[0] = x[b0 + k];
+        p[1] = y[b0 + k];
+        p[2] = z[b0 + k];
+    }
+}
+}  // namespace
+
+void BatchEngine::set_positions_many(int64_t n, const int64_t* slots, const double* xyz,
+                                     const double* v) {
+    OCM_CK(cudaSetDevice(device_));
+    if (n <= 0) return;
+    std::vector<long long> bead(n), src(n);
+    std::vector<int> cnt(n);
+    long long total = 0;
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t sl = slots[k];
+        if (sl < 0 || sl >= max_systems_ || !slots_[sl].used) throw Error(1, "[error] invalid slot");
+        bead[k] = slots_[sl].bead_off;
+        src[k] = total;
+        cnt[k] = (int)slots_[sl].n;
+        total += slots_[sl].n;
+    }
+    for (long long k = 0; k < 3 * total; ++k)
+        if (!std::isfinite(xyz[k])) throw Error(7, "[error] non-finite position");
+    OCM_CK(cudaStreamSynchronize(stream_));
+    if ((int64_t)seg_n_.n < n) {
+        seg_bead_.alloc(n);
+        seg_off_.alloc(n);
+        seg_n_.alloc(n);
+    }
+    if ((int64_t)stage_.n < (v ? 6 : 3) * total) stage_.alloc((v ? 6 : 3) * total);
+    DevBuf<long long>& db = seg_bead_;
+    DevBuf<long long>& ds = seg_off_;
+    DevBuf<int>& dn = seg_n_;
+    DevBuf<double>& buf = stage_;
+    cudaStream_t s = stream_;
+    OCM_CK(cudaMemcpyAsync(db.p, bead.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(ds.p, src.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(dn.p, cnt.data(), n * sizeof(int), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(buf.p, xyz, 3 * total * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (v) OCM_CK(cudaMemcpyAsync(buf.p + 3 * total, v, 3 * total * sizeof(double), cudaMemcpyHostToDevice, s));
+    const dim3 grid(8, (unsigned)n);
+    k_scatter_state<<<grid, 128, 0, s>>>((int)n, db.p, ds.p, dn.p, buf.p, v ? 1 : 0, x_.p, y_.p, z_.p,
+                                         vx_.p, vy_.p, vz_.p, total);
+    OCM_CK(cudaGetLastError());
+    OCM_CK(cudaStreamSynchronize(s));
+}
+
+void BatchEngine::get_positions_many(int64_t n, const int64_t* slots, double* xyz) {
+    OCM_CK(cudaSetDevice(device_));
+    if (n <= 0) return;
+    std::vector<long long> bead(n), dst(n);
+    std::vector<int> cnt(n);
+    long long total = 0;
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t sl = slots[k];
+        if (sl < 0 || sl >= max_systems_ || !slots_[sl].used) throw Error(1, "[error] invalid slot");
+        bead[k] = slots_[sl].bead_off;
+        dst[k] = total;
+        cnt[k] = (int)slots_[sl].n;
+        total += slots_[sl].n;
+    }
+    OCM_CK(cudaStreamSynchronize(stream_));
+    if ((int64_t)seg_n_.n < n) {
+        seg_bead_.alloc(n);
+        seg_off_.alloc(n);
+        seg_n_.alloc(n);
+    }
+    if ((int64_t)stage_.n < 3 * total) stage_.alloc(3 * total);
+    DevBuf<long long>& db = seg_bead_;
+    DevBuf<long long>& dd = seg_off_;
+    DevBuf<int>& dn = seg_n_;
+    DevBuf<double>& buf = stage_;
+    cudaStream_t s = stream_;
+    OCM_CK(cudaMemcpyAsync(db.p, bead.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(dd.p, dst.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(dn.p, cnt.data(), n * sizeof(int), cudaMemcpyHostToDevice, s));
+    const dim3 grid(8, (unsigned)n);
+    k_gather_pos<<<grid, 128, 0, s>>>((int)n, db.p, dd.p, dn.p, x_.p, y_.p, z_.p, buf.p);
+    OCM_CK(cudaGetLastError());
+    OCM_CK(cudaMemcpyAsync(xyz, buf.p, 3 * total * sizeof(double), cudaMemcpyDeviceToHost, s));
+    OCM_CK(cudaStreamSynchronize(s));
+}
+
 void BatchEngine::active(int64_t* n_active, int64_t* beads) {
     int64_t a = 0, b = 0;
     for (const auto& s : slots_)

@@ -71,6 +71,8 @@ class BatchEngine {
     void set_threads(int threads);  // 256/512/1024 (autotuner)
     void set_list_smem(int kib);    // -1 = all that fits (autotuner)
     void slot_stats(int64_t slot, int32_t* builds, int32_t* capacity);
+    void set_positions_many(int64_t n, const int64_t* slots, const double* xyz, const double* v);
+    void get_positions_many(int64_t n, const int64_t* slots, double* xyz);
     int threads() const { return threads_; }
 
   private:
@@ -95,8 +97,8 @@ class BatchEngine {
     int device_;
     int64_t max_systems_, max_beads_;
     int nmax_;
-    int threads_ = 1024;
-    int list_smem_kib_ = 0;
+    int threads_ = 512;       // measured best on the 512-replica mix
+    int list_smem_kib_ = 96;
     int num_sms_ = 0;
     cudaStream_t stream_ = nullptr, copy_stream_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, ev_copy_ = nullptr;
@@ -112,6 +114,10 @@ class BatchEngine {
     DevBuf<int32_t> order_, head_;
     DevBuf<double> energy_;
     DevBuf<unsigned long long> forces_;
+    // staging of the many-slot state copies (grown on demand)
+    DevBuf<long long> seg_bead_, seg_off_;
+    DevBuf<int> seg_n_;
+    DevBuf<double> stage_;
     std::vector<BatchSys> sys_host_;
 };
 

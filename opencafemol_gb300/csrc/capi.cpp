@@ -466,6 +466,15 @@ int ocm_batch_get_positions(ocm_batch* batch, int64_t slot, double* xyz) {
 int ocm_batch_get_velocities(ocm_batch* batch, int64_t slot, double* v) {
     BATCH_CALL(need(v, "v"); batch->b->get_velocities(slot, v));
 }
+int ocm_batch_set_positions_many(ocm_batch* batch, int64_t n, const int64_t* slots,
+                                 const double* xyz, const double* v) {
+    BATCH_CALL(if (n) { need(slots, "slots"); need(xyz, "xyz"); }
+               batch->b->set_positions_many(n, slots, xyz, v));
+}
+int ocm_batch_get_positions_many(ocm_batch* batch, int64_t n, const int64_t* slots, double* xyz) {
+    BATCH_CALL(if (n) { need(slots, "slots"); need(xyz, "xyz"); }
+               batch->b->get_positions_many(n, slots, xyz));
+}
 int ocm_batch_steps_done(ocm_batch* batch, int64_t slot, int64_t* steps) {
     BATCH_CALL(need(steps, "steps"); *steps = batch->b->steps_done(slot));
 }

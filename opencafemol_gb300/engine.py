@@ -160,6 +160,21 @@ class Batch:
         check(lib.ocm_batch_get_velocities(self._h, int(slot), dptr(a)))
         return a
 
+    def set_positions_many(self, slots, xyz, velocities=None) -> None:
+        """Positions (and velocities) of many slots, beads back to back."""
+        sl = np.ascontiguousarray(slots, np.int64)
+        x = as_f64(xyz)
+        v = None if velocities is None else as_f64(velocities)
+        check(lib.ocm_batch_set_positions_many(self._h, len(sl), i64ptr(sl), dptr(x), dptr(v)))
+
+    def get_positions_many(self, slots, out=None) -> np.ndarray:
+        sl = np.ascontiguousarray(slots, np.int64)
+        total = sum(self._n[int(k)] for k in sl)
+        if out is None:
+            out = np.zeros((total, 3))
+        check(lib.ocm_batch_get_positions_many(self._h, len(sl), i64ptr(sl), dptr(out)))
+        return out
+
     def steps_done(self, slot: int) -> int:
         s = C.c_int64()
         check(lib.ocm_batch_steps_done(self._h, int(slot), C.byref(s)))

@@ -1,0 +1,139 @@
+"""Continuous-batching request loop over the batched engine.
+
+Requests (one coarse-grained system each, with its own temperature, seed
+and step count) arrive over time.  The loop admits waiting requests while
+their device footprint fits the batch's free bead capacity and free slots,
+advances every resident system by one chunk of steps with one launch,
+retires finished systems (freeing their capacity for the next admissions)
+and records each request's completion latency.  Admission happens between
+chunks while every other system stays resident on the device, so new work
+overlaps with work already running.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._lib import OCMError
+from .engine import Batch
+from .forcefield import System
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float          # seconds after the stream starts
+    system: System
+    positions: np.ndarray
+    temperature: float
+    n_steps: int
+    seed: int
+    friction: float = 0.1
+    step_size: float = 0.01
+    # filled in by the server
+    admitted_at: float = math.nan
+    finished_at: float = math.nan
+    result: np.ndarray | None = None
+
+    @property
+    def beads(self) -> int:
+        return self.system.n
+
+    @property
+    def latency(self) -> float:
+        return self.finished_at - self.arrival
+
+
+@dataclass
+class ServeStats:
+    requests: int
+    wall_s: float
+    bead_steps: float
+    latencies_s: list = field(default_factory=list)
+    chunks: int = 0
+    max_resident: int = 0
+
+    def summary(self) -> dict:
+        lat = np.array(self.latencies_s)
+        return {"requests": self.requests, "wall_s": self.wall_s,
+                "bead_steps_per_s": self.bead_steps / self.wall_s if self.wall_s > 0 else None,
+                "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
+                "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
+                "chunks": self.chunks, "max_resident": self.max_resident}
+
+
+class Server:
+    """Owns a Batch and runs a request stream through it."""
+
+    def __init__(self, max_systems: int, max_total_beads: int, max_beads_per_system: int,
+                 chunk_steps: int = 200, device: int = 0, keep_results: bool = False):
+        self.batch = Batch(max_systems, max_total_beads, max_beads_per_system, device=device)
+        self.chunk_steps = chunk_steps
+        self.max_systems = max_systems
+        self.keep_results = keep_results
+
+    def serve(self, requests: list[Request], realtime: bool = True) -> ServeStats:
+        """Run the stream.  With realtime=True requests become visible at
+        their arrival times on the wall clock; otherwise all arrive at once."""
+        queue = sorted(requests, key=lambda r: r.arrival)
+        waiting: list[Request] = []
+        resident: dict[int, Request] = {}
+        done = 0
+        nxt = 0
+        stats = ServeStats(requests=len(queue), wall_s=0.0, bead_steps=0.0)
+        t0 = time.perf_counter()
+        while done < len(queue):
+            now = time.perf_counter() - t0 if realtime else math.inf
+            while nxt < len(queue) and queue[nxt].arrival <= now:
+                waiting.append(queue[nxt])
+                nxt += 1
+            ran = False
+            if resident:
+                # launch the chunk first: the admissions below (host-side
+                # compile + uploads on the copy stream) overlap with it
+                self.batch.run(self.chunk_steps, sync=False)
+                stats.chunks += 1
+                ran = True
+            while waiting and len(resident) < self.max_systems:
+                r = waiting[0]
+                try:
+                    slot = self.batch.admit(r.system, r.positions, temperature=r.temperature,
+                                            friction=r.friction, step_size=r.step_size,
+                                            seed=r.seed, n_steps=r.n_steps)
+                except OCMError as e:
+                    if e.code == 3:  # no capacity now: retry after a retirement
+                        break
+                    raise
+                r.admitted_at = time.perf_counter() - t0
+                resident[slot] = r
+                waiting.pop(0)
+            stats.max_resident = max(stats.max_resident, len(resident))
+            if not ran:
+                if not resident and nxt < len(queue) and realtime:
+                    time.sleep(max(0.0, queue[nxt].arrival - (time.perf_counter() - t0)))
+                continue
+            for slot in self.batch.finished():
+                if slot not in resident:
+                    continue
+                r = resident.pop(slot)
+                r.finished_at = time.perf_counter() - t0
+                if self.keep_results:
+                    r.result = self.batch.positions(slot)
+                self.batch.retire(slot)
+                stats.latencies_s.append(r.latency if realtime else r.finished_at)
+                stats.bead_steps += r.beads * r.n_steps
+                done += 1
+        stats.wall_s = time.perf_counter() - t0
+        return stats
+
+
+def poisson_arrivals(n: int, rate_per_s: float, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate_per_s, n))
+
+
+def log_uniform_int(rng: np.random.Generator, lo: float, hi: float, n: int) -> np.ndarray:
+    return np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), n))).astype(np.int64)
