@@ -129,6 +129,52 @@ FLOPS_PER_BOND = 30
 FLOPS_PER_ANGLE = 110
 FLOPS_PER_DIHEDRAL = 160
 FLOPS_PER_BEAD = 40
+# integrator: read F (24), x (12), v (12), 1/m (4); write x (12), v (12),
+# zero F (24)
+BYTES_INTEGRATE_PER_BEAD = 100
+
+
+def measured_hbm_gbs():
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured (STREAM-style copy)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def batched_roofline(specs, K, launch_s, sm_max_mhz, traffic):
+    """Roofline object of one k_batch launch advancing every replica K steps.
+
+    HBM view: compulsory bytes per MD step of a design that streams the
+    state every step (positions + packed params in, 4 B per pair within the
+    cutoff, 64-bit force write, bonded index/param records, integrator
+    read/write of x, v, F, 1/m).  The persistent kernel keeps each system in
+    shared memory, so its DRAM traffic ("traffic") is far below this.
+    """
+    beads = int(sum(s.n for s in specs))
+    pc = pair_counts(specs)
+    n_bond = sum(len(s.bonds) for s in specs)
+    n_go = sum(len(s.contacts) for s in specs)
+    n_ang = sum(len(s.fla_idx) for s in specs)
+    n_dih = sum(len(s.fld_idx) for s in specs)
+    pairs = int(pc.sum())
+    bytes_step = int(beads * (16 + 24 + BYTES_INTEGRATE_PER_BEAD) + 4 * pairs
+                     + 16 * n_go + 16 * n_bond + 16 * n_ang + 20 * n_dih)
+    flops_step = int(pairs * FLOPS_PER_PAIR + (n_bond + n_go) * FLOPS_PER_BOND
+                     + n_ang * FLOPS_PER_ANGLE + n_dih * FLOPS_PER_DIHEDRAL + beads * FLOPS_PER_BEAD)
+    hbm_peak, hbm_src = measured_hbm_gbs()
+    achieved_gbs = bytes_step * K / launch_s / 1e9
+    achieved_tf = flops_step * K / launch_s / 1e12
+    fp32_peak = fp32_peak_tflops(sm_max_mhz)
+    return {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": hbm_src,
+            "kernel": "k_batch (persistent, shared-memory resident)",
+            "algorithmic_bytes_per_launch": bytes_step * K,
+            "bytes_per_bead_step": bytes_step / beads,
+            "pairs_within_cutoff_per_bead": pairs / beads,
+            "fp32": {"achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved_tf / fp32_peak, "flops_per_launch": flops_step * K,
+                     "peak_source": "nominal 152 SMs x 128 FP32 lanes x 2 flop x max SM clock"}}
 
 
 def run_ours(args, rank, world):
@@ -178,21 +224,12 @@ def run_ours(args, rank, world):
     # ---- served stream (continuous batching), p50/p99 completion latency ----
     serve = run_serving(ocm, args) if args.serve_requests > 0 and rank == 0 else None
 
-    # ---- roofline of the batched kernel (FP32-issue bound) ----
-    pc = pair_counts(specs)
-    flops_step = (pc.sum() * FLOPS_PER_PAIR
-                  + sum(len(s.bonds) + len(s.contacts) for s in specs) * FLOPS_PER_BOND
-                  + sum(len(s.fla_idx) for s in specs) * FLOPS_PER_ANGLE
-                  + sum(len(s.fld_idx) for s in specs) * FLOPS_PER_DIHEDRAL
-                  + beads * FLOPS_PER_BEAD)
-    achieved = flops_step * K / (dev_time / args.steps) / 1e12
-    peak = fp32_peak_tflops(clk.summary().get("sm_max_mhz"))
-    roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak if peak else None, "traffic": None,
-            "kernel": "k_batch (persistent, shared-memory resident)",
-            "peak_source": "nominal 152 SMs x 128 FP32 lanes x 2 flop x max SM clock"}
+    roof = batched_roofline(specs, K, dev_time / args.steps, clk.summary().get("sm_max_mhz"),
+                            args.traffic_bytes if args.traffic_bytes > 0 else None)
 
     cpu = run_cpu_baseline(specs, sample_systems=args.cpu_sample, md_steps=args.cpu_steps) if rank == 0 else None
+    if cpu:
+        cpu.pop("seconds", None)
 
     line = {
         "metric": METRIC, "value": value, "unit": "bead-steps/s", "n_gpus": world,
@@ -318,9 +355,9 @@ def run_cpu_baseline(specs, sample_systems=48, md_steps=20):
     with ThreadPoolExecutor(max_workers=cores) as ex:
         bs = sum(ex.map(one, idx))
     t = time.perf_counter() - t0
-    return {"value": bs / t, "unit": "bead-steps/s", "cores": cores, "kind": "port",
+    return {"value": bs / t, "unit": "bead-steps/s", "cores": min(cores, len(idx)), "kind": "port",
             "sample": f"{len(idx)} of the {len(specs)} replicas x {md_steps} steps, FP64 oracle "
-                      f"(all-pairs), one thread per replica"}
+                      f"(all-pairs), one thread per replica", "seconds": t}
 
 
 def fp32_peak_tflops(sm_max_mhz):
@@ -356,10 +393,12 @@ def run_reference(args, rank, world):
         r = run_cpu_baseline(specs, sample_systems=args.cpu_sample, md_steps=K)
         steps_cpu.append(r)
     value = float(np.median([r["value"] for r in steps_cpu]))
+    ms_per_step = float(np.median([r["seconds"] for r in steps_cpu])) * 1e3
     cpu = dict(steps_cpu[-1])
+    cpu.pop("seconds", None)
     cpu["value"] = value
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "bead-steps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Go-model proteins)",
             "config": {"workload": f"batched ensemble: {len(specs)} Go proteins, N log-uniform "
@@ -384,6 +423,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--serve-requests", type=int, default=96)
+    ap.add_argument("--traffic-bytes", type=float, default=0.0,
+                    help="DRAM bytes per k_batch launch from an ncu capture, reported as roofline.traffic")
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-step-scale", type=int, default=50)
     ap.add_argument("--serve-chunk", type=int, default=100)

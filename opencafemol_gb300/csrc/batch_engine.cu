@@ -32,6 +32,17 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxClusters = 64;  // 2048 beads per system
+// Pair work of a bead is split over S adjacent lanes (S = 1, 2, 4 or 8, the
+// largest with n * S <= threads per CTA); sub-lane s sums the list entries
+// whose j lies in [s*n/S, (s+1)*n/S).  kMaxUnits bounds n * S.
+constexpr int kMaxUnits = 1024;
+constexpr int kMaxSplit = 8;
+
+__host__ __device__ __forceinline__ int pair_split(int n, int threads) {
+    int S = 1;
+    while (S < kMaxSplit && n * S * 2 <= threads) S <<= 1;
+    return S;
+}
 
 struct BatchArgs {
     BatchSys* sys;
@@ -56,10 +67,38 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
-__device__ __forceinline__ void sadd(unsigned long long* F, int nmax, int b, float3 f) {
-    atomicAdd(&F[b], to_fixed(f.x));
-    atomicAdd(&F[nmax + b], to_fixed(f.y));
-    atomicAdd(&F[2 * nmax + b], to_fixed(f.z));
+// 64-bit fixed-point force accumulator in shared memory, kept as separate
+// low and high 32-bit words ([3][nmax] each).  An addition adds the low word
+// with a 32-bit atomic, takes the carry from the returned old value and adds
+// high + carry: the final 64-bit value is exact and independent of the order
+// of the additions, and two 32-bit shared atomics cost far less than one
+// 64-bit shared atomic.
+struct FixedAcc {
+    uint32_t* lo;
+    uint32_t* hi;
+};
+
+__device__ __forceinline__ void facc_add(const FixedAcc& F, int idx, float f) {
+    const unsigned long long v = to_fixed(f);
+    const uint32_t l = (uint32_t)v;
+    const uint32_t old = atomicAdd(&F.lo[idx], l);
+    const uint32_t h = (uint32_t)(v >> 32) + (old + l < old ? 1u : 0u);
+    if (h) atomicAdd(&F.hi[idx], h);
+}
+
+__device__ __forceinline__ long long facc_get(const FixedAcc& F, int idx) {
+    return (long long)(((unsigned long long)F.hi[idx] << 32) | F.lo[idx]);
+}
+
+__device__ __forceinline__ void facc_zero(const FixedAcc& F, int idx) {
+    F.lo[idx] = 0u;
+    F.hi[idx] = 0u;
+}
+
+__device__ __forceinline__ void sadd(const FixedAcc& F, int nmax, int b, float3 f) {
+    facc_add(F, b, f.x);
+    facc_add(F, nmax + b, f.y);
+    facc_add(F, 2 * nmax + b, f.z);
 }
 
 __device__ __forceinline__ float3 lo3(const float* sxl, int nmax, int i) {
@@ -86,7 +125,7 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
 template <int TERMS, bool LABELS, bool ENERGY>
 __device__ __forceinline__ void batch_tile(int I, int J, int mslot, const uint32_t* __restrict__ masks,
                                            const float4* sx, const float4* sp0, const float4* sp1,
-                                           const uint32_t* slab, unsigned long long* sF, int nmax,
+                                           const uint32_t* slab, const FixedAcc& sF, int nmax,
                                            const PairConsts& pc, uint32_t excl_all, int lane,
                                            float* eacc) {
     const int ki = I * 32 + lane, kj = J * 32 + lane;
@@ -215,13 +254,17 @@ __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, i
                                             const PairConsts& pc, uint16_t* slist,
                                             uint16_t* __restrict__ glist, uint16_t* scnt,
                                             float* sref, int nmax, int tid, int threads,
-                                            int* overflow) {
+                                            int S, uint16_t* sseg, int* overflow) {
     const float3 nobox = make_float3(0.f, 0.f, 0.f);
     const uint32_t present = (uint32_t)pc.terms;
     for (int i = tid; i < n; i += threads) {
         const float4 xi = sx[i];
         const uint32_t labi = LABELS ? slab[i] : 0u;
         int cnt = 0;
+        // list offset where each j-range of the pair split starts
+        int s_next = 1;
+        int jb = S > 1 ? n / S : 0x7FFFFFFF;
+        if (S > 1) sseg[i * S] = 0;
         int ep = ex_start[i];
         const int e1 = ex_start[i + 1];
         int ej = ep < e1 ? (ex[ep] & 0xFFFFFF) : 0x7FFFFFFF;
@@ -249,6 +292,11 @@ __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, i
                             bits |= 1u << term;
                 }
                 if ((bits & present) == present) continue;
+                while (j >= jb) {
+                    sseg[i * S + s_next] = (uint16_t)min(cnt, maxn);
+                    ++s_next;
+                    jb = s_next < S ? (s_next * n) / S : 0x7FFFFFFF;
+                }
                 const uint16_t e = (uint16_t)(j | (bits << 11));
                 if (cnt < cap_s) slist[cnt * npad + i] = e;
                 else if (cnt < maxn) glist[(size_t)cnt * npad + i] = e;
@@ -259,6 +307,7 @@ __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, i
             atomicOr(overflow, 1);
             cnt = maxn;
         }
+        for (; s_next < S; ++s_next) sseg[i * S + s_next] = (uint16_t)cnt;
         scnt[i] = (uint16_t)cnt;
         sref[i] = xi.x;
         sref[nmax + i] = xi.y;
@@ -266,12 +315,12 @@ __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, i
     }
 }
 
-// Pair forces on bead i from its list, four entries per iteration so their
-// loads and arithmetic overlap.  One accumulator, in list (= increasing j)
-// order: entries outside the cutoff contribute nothing, so the FP32 sum does
-// not depend on when the list was built.
+// Pair forces on bead i from list entries [k0, cnt), four entries per
+// iteration so their loads and arithmetic overlap.  One accumulator, in list
+// (= increasing j) order: entries outside the cutoff contribute nothing, so
+// the FP32 sum does not depend on when the list was built.
 template <int TERMS, bool ENERGY>
-__device__ __forceinline__ float3 list_forces(int i, int cnt, int cap_s, int npad,
+__device__ __forceinline__ float3 list_forces(int i, int k0, int cnt, int cap_s, int npad,
                                               const uint16_t* slist,
                                               const uint16_t* __restrict__ glist,
                                               const float4* sx, const float4* sp0,
@@ -282,7 +331,7 @@ __device__ __forceinline__ float3 list_forces(int i, int cnt, int cap_s, int npa
     const float4 p0i = sp0[i];
     const float4 p1i = (TERMS & kTermLJA) ? sp1[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     float3 fa = make_float3(0.f, 0.f, 0.f);
-    for (int k = 0; k < cnt; k += 4) {
+    for (int k = k0; k < cnt; k += 4) {
         uint32_t ent[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -324,7 +373,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
     const int nmax = a.nmax;
     // Positions are float-float: hi parts in sx (pair arithmetic), lo parts
     // in sxl; x = hi + lo carries ~48 significant bits.
-    unsigned long long* sF = reinterpret_cast<unsigned long long*>(smem);
+    const FixedAcc sF{reinterpret_cast<uint32_t*>(smem), reinterpret_cast<uint32_t*>(smem) + 3 * (size_t)nmax};
     float4* sx = reinterpret_cast<float4*>(smem + 24 * (size_t)nmax);
     float4* sp0 = reinterpret_cast<float4*>(smem + 40 * (size_t)nmax);
     float* sxl = reinterpret_cast<float*>(smem + 56 * (size_t)nmax);
@@ -343,6 +392,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
     float4* bc = reinterpret_cast<float4*>(smem + off);
     float4* bh = bc + kMaxClusters;
     off += 2 * kMaxClusters * sizeof(float4);
+    uint16_t* sseg = reinterpret_cast<uint16_t*>(smem + off);
+    off += 2 * kMaxUnits;
     uint16_t* slist = reinterpret_cast<uint16_t*>(smem + off);
     const size_t list_bytes = a.smem_bytes > off ? a.smem_bytes - off : 0;
     __shared__ int s_claim;
@@ -389,6 +440,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         // entries per bead kept in shared memory (multiple of 4)
         const int cap_s = min(maxn, (int)(list_bytes / (2 * (size_t)npad)) & ~3);
         const int n_bonds = R.n_bonds, n_angles = R.n_angles, n_dih = R.n_dih;
+        const int S = pair_split(n, THREADS);
         const unsigned long long step0 = R.steps_done;
         int K = 1;
         if (INTEGRATE) {
@@ -405,9 +457,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
 
         // ---- load ----
         for (int b = tid; b < npad; b += THREADS) {
-            sF[b] = 0ull;
-            sF[nmax + b] = 0ull;
-            sF[2 * nmax + b] = 0ull;
+            facc_zero(sF, b);
+            facc_zero(sF, nmax + b);
+            facc_zero(sF, 2 * nmax + b);
             if (b < n) {
                 const double px = a.x[boff + b], py = a.y[boff + b], pz = a.z[boff + b];
                 const float hx = __double2float_rn(px), hy = __double2float_rn(py),
@@ -456,7 +508,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         for (int st = 0; st < K; ++st) {
             if (need_build && !use_tiles) {
                 build_lists<LABELS>(n, nt, npad, maxn, cap_s, lcut2, sx, slab, bc, bh, ex_start, exl,
-                                    pc, slist, glist, scnt, sref, nmax, tid, THREADS, &s_overflow);
+                                    pc, slist, glist, scnt, sref, nmax, tid, THREADS, S, sseg,
+                                    &s_overflow);
                 ++builds;
                 __syncthreads();
                 use_tiles = s_overflow != 0;
@@ -484,14 +537,40 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
             if (has_a) at = angles[tid];
             if (has_d) dt = dih[tid];
             // ---- pair terms ----
-            if (pairs_on && !use_tiles) {
+            if (pairs_on && !use_tiles && S > 1) {
+                // n * S <= THREADS: one (bead, j-range) unit per thread; the
+                // S partial sums of a bead meet in a fixed butterfly
+                const int u = tid;
+                const int i = u / S, sr = u & (S - 1);
+                float3 fi = make_float3(0.f, 0.f, 0.f);
+                PairEnergy e;
+                e.zero();
+                if (i < n) {
+                    const int k0 = sseg[u];
+                    const int k1 = sr == S - 1 ? (int)scnt[i] : (int)sseg[u + 1];
+                    fi = list_forces<TERMS, ENERGY>(i, k0, k1, cap_s, npad, slist, glist, sx, sp0, sp1,
+                                                    excl_all, pc, e);
+                }
+                for (int o = 1; o < S; o <<= 1) {
+                    fi.x += __shfl_xor_sync(kFull, fi.x, o);
+                    fi.y += __shfl_xor_sync(kFull, fi.y, o);
+                    fi.z += __shfl_xor_sync(kFull, fi.z, o);
+                }
+                if (i < n && sr == 0) sadd(sF, nmax, i, fi);
+                if (ENERGY) {
+                    eacc[kSlotEXV] += 0.5f * e.exv;
+                    eacc[kSlotDH] += 0.5f * e.dh;
+                    eacc[kSlotLJR] += 0.5f * e.ljr;
+                    eacc[kSlotLJA] += 0.5f * e.lja;
+                }
+            } else if (pairs_on && !use_tiles) {
 #pragma unroll
                 for (int c = 0; c < BPT; ++c) {
                     const int i = tid + c * THREADS;
                     if (i >= n) break;
                     PairEnergy e;
                     e.zero();
-                    const float3 fi = list_forces<TERMS, ENERGY>(i, scnt[i], cap_s, npad, slist, glist,
+                    const float3 fi = list_forces<TERMS, ENERGY>(i, 0, scnt[i], cap_s, npad, slist, glist,
                                                                  sx, sp0, sp1, excl_all, pc, e);
                     sadd(sF, nmax, i, fi);
                     if (ENERGY) {
@@ -588,12 +667,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                 const int b = I * 32 + lane;
                 bool moved = false;
                 if (b < n) {
-                    const float fx = (float)((double)(long long)sF[b] * kFixedInv);
-                    const float fy = (float)((double)(long long)sF[nmax + b] * kFixedInv);
-                    const float fz = (float)((double)(long long)sF[2 * nmax + b] * kFixedInv);
-                    sF[b] = 0ull;
-                    sF[nmax + b] = 0ull;
-                    sF[2 * nmax + b] = 0ull;
+                    const float fx = fixed_to_float(facc_get(sF, b));
+                    const float fy = fixed_to_float(facc_get(sF, nmax + b));
+                    const float fz = fixed_to_float(facc_get(sF, 2 * nmax + b));
+                    facc_zero(sF, b);
+                    facc_zero(sF, nmax + b);
+                    facc_zero(sF, 2 * nmax + b);
                     const float im = sim[b];
                     if (im > 0.f) {
                         const float3 g = noise[c];
@@ -641,9 +720,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
             }
         } else {
             for (int b = tid; b < n; b += THREADS) {
-                a.forces[b] = sF[b];
-                a.forces[nmax + b] = sF[nmax + b];
-                a.forces[2 * nmax + b] = sF[2 * nmax + b];
+                a.forces[b] = (unsigned long long)facc_get(sF, b);
+                a.forces[nmax + b] = (unsigned long long)facc_get(sF, nmax + b);
+                a.forces[2 * nmax + b] = (unsigned long long)facc_get(sF, 2 * nmax + b);
             }
             if (tid == 0 && s_overflow) a.sys[slot].overflow = 1;
         }
@@ -913,7 +992,7 @@ BatchEngine::~BatchEngine() {
 }
 
 size_t BatchEngine::smem_bytes(int nmax, bool general) const {
-    return (size_t)nmax * (general ? 118 : 98) + 2 * kMaxClusters * sizeof(float4);
+    return (size_t)nmax * (general ? 118 : 98) + 2 * kMaxClusters * sizeof(float4) + 2 * kMaxUnits;
 }
 
 int64_t BatchEngine::footprint(const SystemDesc& d) {

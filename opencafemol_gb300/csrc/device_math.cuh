@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "engine_types.h"
+#include "fixed_point.h"
 
 namespace ocm {
 

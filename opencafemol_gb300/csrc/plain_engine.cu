@@ -541,9 +541,9 @@ __global__ void k_integrate(IntegrateArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const unsigned long long step = *a.step_base + (unsigned long long)a.r;
-    const float fx = (float)((double)(long long)a.F[i] * kFixedInv);
-    const float fy = (float)((double)(long long)a.F[a.n + i] * kFixedInv);
-    const float fz = (float)((double)(long long)a.F[2 * a.n + i] * kFixedInv);
+    const float fx = fixed_to_float((long long)a.F[i]);
+    const float fy = fixed_to_float((long long)a.F[a.n + i]);
+    const float fz = fixed_to_float((long long)a.F[2 * a.n + i]);
     a.F[i] = 0ull;
     a.F[a.n + i] = 0ull;
     a.F[2 * a.n + i] = 0ull;
