@@ -33,14 +33,17 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxClusters = 64;  // 2048 beads per system
 // Pair work of a bead is split over S adjacent lanes (S = 1, 2, 4 or 8, the
-// largest with n * S <= threads per CTA); sub-lane s sums the list entries
-// whose j lies in [s*n/S, (s+1)*n/S).  kMaxUnits bounds n * S.
-constexpr int kMaxUnits = 1024;
+// largest with n * S <= kSplitUnits); sub-lane s sums the list entries whose
+// j lies in [s*n/S, (s+1)*n/S).  S depends on n alone, so the FP32 sums, and
+// the results, do not depend on the threads per CTA (a CTA with fewer
+// threads walks the units in more passes).
+constexpr int kSplitUnits = 512;
+constexpr int kMaxUnits = kSplitUnits;
 constexpr int kMaxSplit = 8;
 
-__host__ __device__ __forceinline__ int pair_split(int n, int threads) {
+__host__ __device__ __forceinline__ int pair_split(int n) {
     int S = 1;
-    while (S < kMaxSplit && n * S * 2 <= threads) S <<= 1;
+    while (S < kMaxSplit && n * S * 2 <= kSplitUnits) S <<= 1;
     return S;
 }
 
@@ -370,32 +373,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
     constexpr int NW = THREADS / 32;
     constexpr int BPT = (32 * kMaxClusters + THREADS - 1) / THREADS;  // beads per thread
     extern __shared__ __align__(16) unsigned char smem[];
-    const int nmax = a.nmax;
-    // Positions are float-float: hi parts in sx (pair arithmetic), lo parts
-    // in sxl; x = hi + lo carries ~48 significant bits.
-    const FixedAcc sF{reinterpret_cast<uint32_t*>(smem), reinterpret_cast<uint32_t*>(smem) + 3 * (size_t)nmax};
-    float4* sx = reinterpret_cast<float4*>(smem + 24 * (size_t)nmax);
-    float4* sp0 = reinterpret_cast<float4*>(smem + 40 * (size_t)nmax);
-    float* sxl = reinterpret_cast<float*>(smem + 56 * (size_t)nmax);
-    float* sv = reinterpret_cast<float*>(smem + 68 * (size_t)nmax);
-    float* sim = reinterpret_cast<float*>(smem + 80 * (size_t)nmax);
-    float* sref = reinterpret_cast<float*>(smem + 84 * (size_t)nmax);
-    uint16_t* scnt = reinterpret_cast<uint16_t*>(smem + 96 * (size_t)nmax);
-    size_t off = 98 * (size_t)nmax;
-    float4* sp1 = nullptr;
-    uint32_t* slab = nullptr;
-    if ((TERMS & kTermLJA) || LABELS) {
-        sp1 = reinterpret_cast<float4*>(smem + off);
-        slab = reinterpret_cast<uint32_t*>(smem + off + 16 * (size_t)nmax);
-        off += 20 * (size_t)nmax;
-    }
-    float4* bc = reinterpret_cast<float4*>(smem + off);
-    float4* bh = bc + kMaxClusters;
-    off += 2 * kMaxClusters * sizeof(float4);
-    uint16_t* sseg = reinterpret_cast<uint16_t*>(smem + off);
-    off += 2 * kMaxUnits;
-    uint16_t* slist = reinterpret_cast<uint16_t*>(smem + off);
-    const size_t list_bytes = a.smem_bytes > off ? a.smem_bytes - off : 0;
+    const int nmax = a.nmax;  // stride of the global force output
     __shared__ int s_claim;
     __shared__ int s_move[2];
     __shared__ int s_overflow;
@@ -426,11 +404,47 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         const float4* gp1 = reinterpret_cast<const float4*>(blob + R.off_p1);
         const uint32_t* glab = reinterpret_cast<const uint32_t*>(blob + R.off_lab);
         const float* ginvm = reinterpret_cast<const float*>(blob + R.off_invm);
-        const BondTerm* bonds = reinterpret_cast<const BondTerm*>(blob + R.off_bonds);
-        const AngleTerm* angles = reinterpret_cast<const AngleTerm*>(blob + R.off_angles);
-        const DihedralTerm* dih = reinterpret_cast<const DihedralTerm*>(blob + R.off_dih);
-        const FlaTable* fla = reinterpret_cast<const FlaTable*>(blob + R.off_fla);
-        const FldTable* fld = reinterpret_cast<const FldTable*>(blob + R.off_fld);
+        // ---- shared-memory layout of this system, arrays of stride ns ----
+        // Positions are float-float: hi parts in sx (pair arithmetic), lo
+        // parts in sxl; x = hi + lo carries ~48 significant bits.
+        const int ns = npad;
+        const FixedAcc sF{reinterpret_cast<uint32_t*>(smem), reinterpret_cast<uint32_t*>(smem) + 3 * ns};
+        float4* sx = reinterpret_cast<float4*>(smem + 24 * (size_t)ns);
+        float4* sp0 = reinterpret_cast<float4*>(smem + 40 * (size_t)ns);
+        float* sxl = reinterpret_cast<float*>(smem + 56 * (size_t)ns);
+        float* sv = reinterpret_cast<float*>(smem + 68 * (size_t)ns);
+        float* sim = reinterpret_cast<float*>(smem + 80 * (size_t)ns);
+        float* sref = reinterpret_cast<float*>(smem + 84 * (size_t)ns);
+        uint16_t* scnt = reinterpret_cast<uint16_t*>(smem + 96 * (size_t)ns);
+        size_t off = 98 * (size_t)ns;
+        float4* sp1 = nullptr;
+        uint32_t* slab = nullptr;
+        if ((TERMS & kTermLJA) || LABELS) {
+            sp1 = reinterpret_cast<float4*>(smem + off);
+            slab = reinterpret_cast<uint32_t*>(smem + off + 16 * (size_t)ns);
+            off += 20 * (size_t)ns;
+        }
+        float4* bc = reinterpret_cast<float4*>(smem + off);
+        float4* bh = bc + nt;
+        off += 32 * (size_t)nt;
+        uint16_t* sseg = reinterpret_cast<uint16_t*>(smem + off);
+        off += 2 * kMaxUnits;
+        // bonded records and tables: staged in shared memory when they fit,
+        // read from the blob otherwise
+        const unsigned char* gbonded = blob + R.off_bonded;
+        const bool bonded_smem = off + (size_t)R.bonded_bytes <= a.smem_bytes;
+        unsigned char* sbonded = smem + off;
+        if (bonded_smem) off += (size_t)R.bonded_bytes;
+        const unsigned char* bsrc = bonded_smem ? sbonded : gbonded;
+        const float4* bpar = reinterpret_cast<const float4*>(bsrc + R.rb_p);
+        const uint32_t* bij = reinterpret_cast<const uint32_t*>(bsrc + R.rb_ij);
+        const uint2* aij = reinterpret_cast<const uint2*>(bsrc + R.ra_ij);
+        const float* ak = reinterpret_cast<const float*>(bsrc + R.ra_k);
+        const uint4* drec = reinterpret_cast<const uint4*>(bsrc + R.rd);
+        const FlaTable* fla = reinterpret_cast<const FlaTable*>(bsrc + R.rfla);
+        const FldTable* fld = reinterpret_cast<const FldTable*>(bsrc + R.rfld);
+        uint16_t* slist = reinterpret_cast<uint16_t*>(smem + off);
+        const size_t list_bytes = a.smem_bytes > off ? a.smem_bytes - off : 0;
         const int32_t* tmask = reinterpret_cast<const int32_t*>(blob + R.off_tmask);
         const uint32_t* masks = reinterpret_cast<const uint32_t*>(blob + R.off_masks);
         const int32_t* ex_start = reinterpret_cast<const int32_t*>(blob + R.off_ex_start);
@@ -440,7 +454,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         // entries per bead kept in shared memory (multiple of 4)
         const int cap_s = min(maxn, (int)(list_bytes / (2 * (size_t)npad)) & ~3);
         const int n_bonds = R.n_bonds, n_angles = R.n_angles, n_dih = R.n_dih;
-        const int S = pair_split(n, THREADS);
+        const int S = pair_split(n);
         const unsigned long long step0 = R.steps_done;
         int K = 1;
         if (INTEGRATE) {
@@ -458,20 +472,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         // ---- load ----
         for (int b = tid; b < npad; b += THREADS) {
             facc_zero(sF, b);
-            facc_zero(sF, nmax + b);
-            facc_zero(sF, 2 * nmax + b);
+            facc_zero(sF, ns + b);
+            facc_zero(sF, 2 * ns + b);
             if (b < n) {
                 const double px = a.x[boff + b], py = a.y[boff + b], pz = a.z[boff + b];
                 const float hx = __double2float_rn(px), hy = __double2float_rn(py),
                             hz = __double2float_rn(pz);
                 sx[b] = make_float4(hx, hy, hz, 0.f);
                 sxl[b] = __double2float_rn(px - (double)hx);
-                sxl[nmax + b] = __double2float_rn(py - (double)hy);
-                sxl[2 * nmax + b] = __double2float_rn(pz - (double)hz);
+                sxl[ns + b] = __double2float_rn(py - (double)hy);
+                sxl[2 * ns + b] = __double2float_rn(pz - (double)hz);
                 sp0[b] = gp0[b];
                 sv[b] = a.vx[boff + b];
-                sv[nmax + b] = a.vy[boff + b];
-                sv[2 * nmax + b] = a.vz[boff + b];
+                sv[ns + b] = a.vy[boff + b];
+                sv[2 * ns + b] = a.vz[boff + b];
                 sim[b] = ginvm[b];
                 if ((TERMS & kTermLJA) || LABELS) {
                     sp1[b] = gp1[b];
@@ -486,6 +500,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                     slab[b] = 0xffffffffu;
                 }
             }
+        }
+        if (bonded_smem) {
+            const uint4* src = reinterpret_cast<const uint4*>(gbonded);
+            uint4* dst = reinterpret_cast<uint4*>(sbonded);
+            for (int q = tid; q < R.bonded_bytes / 16; q += THREADS) dst[q] = src[q];
         }
         __syncthreads();
         for (int I = warp; I < nt; I += NW) cluster_bbox(I, n, sx, bc, bh, lane);
@@ -508,7 +527,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         for (int st = 0; st < K; ++st) {
             if (need_build && !use_tiles) {
                 build_lists<LABELS>(n, nt, npad, maxn, cap_s, lcut2, sx, slab, bc, bh, ex_start, exl,
-                                    pc, slist, glist, scnt, sref, nmax, tid, THREADS, S, sseg,
+                                    pc, slist, glist, scnt, sref, ns, tid, THREADS, S, sseg,
                                     &s_overflow);
                 ++builds;
                 __syncthreads();
@@ -526,42 +545,34 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                                      : make_float3(0.f, 0.f, 0.f);
                 }
             }
-            // ---- bonded parameters: issue every load before any math ----
-            BondTerm bt[2];
-            AngleTerm at;
-            DihedralTerm dt;
-            const bool has_b0 = tid < n_bonds, has_b1 = tid + THREADS < n_bonds;
-            if (has_b0) bt[0] = bonds[tid];
-            if (has_b1) bt[1] = bonds[tid + THREADS];
-            const bool has_a = tid < n_angles, has_d = tid < n_dih;
-            if (has_a) at = angles[tid];
-            if (has_d) dt = dih[tid];
             // ---- pair terms ----
             if (pairs_on && !use_tiles && S > 1) {
-                // n * S <= THREADS: one (bead, j-range) unit per thread; the
-                // S partial sums of a bead meet in a fixed butterfly
-                const int u = tid;
-                const int i = u / S, sr = u & (S - 1);
-                float3 fi = make_float3(0.f, 0.f, 0.f);
-                PairEnergy e;
-                e.zero();
-                if (i < n) {
-                    const int k0 = sseg[u];
-                    const int k1 = sr == S - 1 ? (int)scnt[i] : (int)sseg[u + 1];
-                    fi = list_forces<TERMS, ENERGY>(i, k0, k1, cap_s, npad, slist, glist, sx, sp0, sp1,
-                                                    excl_all, pc, e);
-                }
-                for (int o = 1; o < S; o <<= 1) {
-                    fi.x += __shfl_xor_sync(kFull, fi.x, o);
-                    fi.y += __shfl_xor_sync(kFull, fi.y, o);
-                    fi.z += __shfl_xor_sync(kFull, fi.z, o);
-                }
-                if (i < n && sr == 0) sadd(sF, nmax, i, fi);
-                if (ENERGY) {
-                    eacc[kSlotEXV] += 0.5f * e.exv;
-                    eacc[kSlotDH] += 0.5f * e.dh;
-                    eacc[kSlotLJR] += 0.5f * e.ljr;
-                    eacc[kSlotLJA] += 0.5f * e.lja;
+                // (bead, j-range) units u = i * S + s, 32 per warp; the S
+                // partial sums of a bead meet in a fixed butterfly
+                for (int base = warp * 32; base < n * S; base += THREADS) {
+                    const int u = base + lane;
+                    const int i = u / S, sr = u & (S - 1);
+                    float3 fi = make_float3(0.f, 0.f, 0.f);
+                    PairEnergy e;
+                    e.zero();
+                    if (i < n) {
+                        const int k0 = sseg[u];
+                        const int k1 = sr == S - 1 ? (int)scnt[i] : (int)sseg[u + 1];
+                        fi = list_forces<TERMS, ENERGY>(i, k0, k1, cap_s, npad, slist, glist, sx, sp0,
+                                                        sp1, excl_all, pc, e);
+                    }
+                    for (int o = 1; o < S; o <<= 1) {
+                        fi.x += __shfl_xor_sync(kFull, fi.x, o);
+                        fi.y += __shfl_xor_sync(kFull, fi.y, o);
+                        fi.z += __shfl_xor_sync(kFull, fi.z, o);
+                    }
+                    if (i < n && sr == 0) sadd(sF, ns, i, fi);
+                    if (ENERGY) {
+                        eacc[kSlotEXV] += 0.5f * e.exv;
+                        eacc[kSlotDH] += 0.5f * e.dh;
+                        eacc[kSlotLJR] += 0.5f * e.ljr;
+                        eacc[kSlotLJA] += 0.5f * e.lja;
+                    }
                 }
             } else if (pairs_on && !use_tiles) {
 #pragma unroll
@@ -572,7 +583,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                     e.zero();
                     const float3 fi = list_forces<TERMS, ENERGY>(i, 0, scnt[i], cap_s, npad, slist, glist,
                                                                  sx, sp0, sp1, excl_all, pc, e);
-                    sadd(sF, nmax, i, fi);
+                    sadd(sF, ns, i, fi);
                     if (ENERGY) {
                         // every pair appears in both lists
                         eacc[kSlotEXV] += 0.5f * e.exv;
@@ -589,72 +600,65 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                     const int I = t - J * (J + 1) / 2;
                     if (!bbox_close(bc[I], bh[I], bc[J], bh[J], tcut2)) continue;
                     batch_tile<TERMS, LABELS, ENERGY>(I, J, tmask[t], masks, sx, sp0, sp1, slab, sF,
-                                                      nmax, pc, excl_all, lane, eacc);
+                                                      ns, pc, excl_all, lane, eacc);
                 }
             }
-            // ---- bonded ----
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                if (!(u == 0 ? has_b0 : has_b1)) continue;
-                const BondTerm& bb = bt[u];
-                const int sl = bb.kind == kBondHarmonic ? kSlotHB : kSlotGO;
-                if (!(slots_en & (1u << sl))) continue;
-                float3 dh, dl;
-                ff_sep(sx[bb.i], lo3(sxl, nmax, bb.i), sx[bb.j], lo3(sxl, nmax, bb.j), dh, dl);
-                const float3 d = make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
-                const float delta = ff_bond_delta(dh, dl, bb.r0sq_hi, bb.r0sq_lo);
-                float en;
-                const float s = bond_scalar(bb.kind, norm2(d), delta, bb.p0, bb.p1, en);
-                sadd(sF, nmax, bb.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
-                sadd(sF, nmax, bb.j, make_float3(s * d.x, s * d.y, s * d.z));
-                if (ENERGY) eacc[sl] += en;
-            }
-            for (int b = tid + 2 * THREADS; b < n_bonds; b += THREADS) {
-                const BondTerm bb = bonds[b];
-                const int sl = bb.kind == kBondHarmonic ? kSlotHB : kSlotGO;
-                if (!(slots_en & (1u << sl))) continue;
-                float3 dh, dl;
-                ff_sep(sx[bb.i], lo3(sxl, nmax, bb.i), sx[bb.j], lo3(sxl, nmax, bb.j), dh, dl);
-                const float3 d = make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
-                const float delta = ff_bond_delta(dh, dl, bb.r0sq_hi, bb.r0sq_lo);
-                float en;
-                const float s = bond_scalar(bb.kind, norm2(d), delta, bb.p0, bb.p1, en);
-                sadd(sF, nmax, bb.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
-                sadd(sF, nmax, bb.j, make_float3(s * d.x, s * d.y, s * d.z));
-                if (ENERGY) eacc[sl] += en;
-            }
-            if (slots_en & (1u << kSlotFLA)) {
-                for (int b = tid; b < n_angles; b += THREADS) {
-                    const AngleTerm g = b == tid ? at : angles[b];
-                    const float3 u = ffsep(sx, sxl, nmax, g.j, g.i);
-                    const float3 v = ffsep(sx, sxl, nmax, g.j, g.k);
-                    float3 f1, f3;
-                    float en;
-                    fla_forces(u, v, g.kk, fla[g.table], f1, f3, en);
-                    sadd(sF, nmax, g.i, f1);
-                    sadd(sF, nmax, g.k, f3);
-                    sadd(sF, nmax, g.j, make_float3(-f1.x - f3.x, -f1.y - f3.y, -f1.z - f3.z));
-                    if (ENERGY) eacc[kSlotFLA] += en;
+            // ---- bonded: one flattened loop over dihedrals | angles |
+            // bonds, so the costliest terms spread over all threads ----
+            {
+                const int n_ad = n_dih + n_angles, n_all = n_ad + n_bonds;
+                const bool fld_on = (slots_en & (1u << kSlotFLD)) != 0;
+                const bool fla_on = (slots_en & (1u << kSlotFLA)) != 0;
+                for (int t = tid; t < n_all; t += THREADS) {
+                    if (t < n_dih) {
+                        if (!fld_on) continue;
+                        const uint4 qd = drec[t];
+                        const int qi = qd.x & 0xFFFF, qj = qd.x >> 16, qk = qd.y & 0xFFFF, ql = qd.y >> 16;
+                        const float3 F = ffsep(sx, sxl, ns, qj, qi);
+                        const float3 G = ffsep(sx, sxl, ns, qk, qj);
+                        const float3 H = ffsep(sx, sxl, ns, qk, ql);
+                        float3 f1, f2, f3, f4;
+                        float en;
+                        fld_forces(F, G, H, __uint_as_float(qd.w), fld[qd.z], f1, f2, f3, f4, en);
+                        sadd(sF, ns, qi, f1);
+                        sadd(sF, ns, qj, f2);
+                        sadd(sF, ns, qk, f3);
+                        sadd(sF, ns, ql, f4);
+                        if (ENERGY) eacc[kSlotFLD] += en;
+                    } else if (t < n_ad) {
+                        if (!fla_on) continue;
+                        const int b = t - n_dih;
+                        const uint2 g = aij[b];
+                        const int gi = g.x & 0xFFFF, gj = g.x >> 16, gk = g.y & 0xFFFF;
+                        const float3 u = ffsep(sx, sxl, ns, gj, gi);
+                        const float3 v = ffsep(sx, sxl, ns, gj, gk);
+                        float3 f1, f3;
+                        float en;
+                        fla_forces(u, v, ak[b], fla[g.y >> 16], f1, f3, en);
+                        sadd(sF, ns, gi, f1);
+                        sadd(sF, ns, gk, f3);
+                        sadd(sF, ns, gj, make_float3(-f1.x - f3.x, -f1.y - f3.y, -f1.z - f3.z));
+                        if (ENERGY) eacc[kSlotFLA] += en;
+                    } else {
+                        const int b = t - n_ad;
+                        const uint32_t ij = bij[b];
+                        const int kind = (ij >> 31) ? kBondGo : kBondHarmonic;
+                        const int sl = kind == kBondHarmonic ? kSlotHB : kSlotGO;
+                        if (!(slots_en & (1u << sl))) continue;
+                        const int bi = ij & 0xFFFF, bj = (ij >> 16) & 0x7FFF;
+                        const float4 bp = bpar[b];
+                        float3 dh, dl;
+                        ff_sep(sx[bi], lo3(sxl, ns, bi), sx[bj], lo3(sxl, ns, bj), dh, dl);
+                        const float3 d = make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
+                        const float delta = ff_bond_delta(dh, dl, bp.z, bp.w);
+                        float en;
+                        const float sc = bond_scalar(kind, norm2(d), delta, bp.x, bp.y, en);
+                        sadd(sF, ns, bi, make_float3(-sc * d.x, -sc * d.y, -sc * d.z));
+                        sadd(sF, ns, bj, make_float3(sc * d.x, sc * d.y, sc * d.z));
+                        if (ENERGY) eacc[sl] += en;
+                    }
                 }
             }
-            if (slots_en & (1u << kSlotFLD)) {
-                for (int b = tid; b < n_dih; b += THREADS) {
-                    const DihedralTerm qd = b == tid ? dt : dih[b];
-                    const float3 F = ffsep(sx, sxl, nmax, qd.j, qd.i);
-                    const float3 G = ffsep(sx, sxl, nmax, qd.k, qd.j);
-                    const float3 H = ffsep(sx, sxl, nmax, qd.k, qd.l);
-                    float3 f1, f2, f3, f4;
-                    float en;
-                    fld_forces(F, G, H, qd.kk, fld[qd.table], f1, f2, f3, f4, en);
-                    sadd(sF, nmax, qd.i, f1);
-                    sadd(sF, nmax, qd.j, f2);
-                    sadd(sF, nmax, qd.k, f3);
-                    sadd(sF, nmax, qd.l, f4);
-                    if (ENERGY) eacc[kSlotFLD] += en;
-                }
-            }
-            (void)has_a;
-            (void)has_d;
             __syncthreads();
             if (!INTEGRATE) break;
             // ---- Langevin update, bounding boxes, displacement check ----
@@ -668,28 +672,28 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                 bool moved = false;
                 if (b < n) {
                     const float fx = fixed_to_float(facc_get(sF, b));
-                    const float fy = fixed_to_float(facc_get(sF, nmax + b));
-                    const float fz = fixed_to_float(facc_get(sF, 2 * nmax + b));
+                    const float fy = fixed_to_float(facc_get(sF, ns + b));
+                    const float fz = fixed_to_float(facc_get(sF, 2 * ns + b));
                     facc_zero(sF, b);
-                    facc_zero(sF, nmax + b);
-                    facc_zero(sF, 2 * nmax + b);
+                    facc_zero(sF, ns + b);
+                    facc_zero(sF, 2 * ns + b);
                     const float im = sim[b];
                     if (im > 0.f) {
                         const float3 g = noise[c];
                         const float sq = sqrtf(im) * lc.noise;
                         const float fs = lc.fscale * im;
                         const float vx = lc.vscale * sv[b] + fs * fx + sq * g.x;
-                        const float vy = lc.vscale * sv[nmax + b] + fs * fy + sq * g.y;
-                        const float vz = lc.vscale * sv[2 * nmax + b] + fs * fz + sq * g.z;
+                        const float vy = lc.vscale * sv[ns + b] + fs * fy + sq * g.y;
+                        const float vz = lc.vscale * sv[2 * ns + b] + fs * fz + sq * g.z;
                         sv[b] = vx;
-                        sv[nmax + b] = vy;
-                        sv[2 * nmax + b] = vz;
+                        sv[ns + b] = vy;
+                        sv[2 * ns + b] = vz;
                         float4 h = sx[b];
                         ff_add(h.x, sxl[b], vx * lc.dt);
-                        ff_add(h.y, sxl[nmax + b], vy * lc.dt);
-                        ff_add(h.z, sxl[2 * nmax + b], vz * lc.dt);
+                        ff_add(h.y, sxl[ns + b], vy * lc.dt);
+                        ff_add(h.z, sxl[2 * ns + b], vz * lc.dt);
                         sx[b] = h;
-                        const float dx = h.x - sref[b], dy = h.y - sref[nmax + b], dz = h.z - sref[2 * nmax + b];
+                        const float dx = h.x - sref[b], dy = h.y - sref[ns + b], dz = h.z - sref[2 * ns + b];
                         moved = dx * dx + dy * dy + dz * dz > half_skin2;
                     }
                 }
@@ -707,11 +711,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
             for (int b = tid; b < n; b += THREADS) {
                 const float4 h = sx[b];
                 a.x[boff + b] = (double)h.x + (double)sxl[b];
-                a.y[boff + b] = (double)h.y + (double)sxl[nmax + b];
-                a.z[boff + b] = (double)h.z + (double)sxl[2 * nmax + b];
+                a.y[boff + b] = (double)h.y + (double)sxl[ns + b];
+                a.z[boff + b] = (double)h.z + (double)sxl[2 * ns + b];
                 a.vx[boff + b] = sv[b];
-                a.vy[boff + b] = sv[nmax + b];
-                a.vz[boff + b] = sv[2 * nmax + b];
+                a.vy[boff + b] = sv[ns + b];
+                a.vz[boff + b] = sv[2 * ns + b];
             }
             if (tid == 0) {
                 a.sys[slot].steps_done = step0 + (unsigned long long)K;
@@ -721,8 +725,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         } else {
             for (int b = tid; b < n; b += THREADS) {
                 a.forces[b] = (unsigned long long)facc_get(sF, b);
-                a.forces[nmax + b] = (unsigned long long)facc_get(sF, nmax + b);
-                a.forces[2 * nmax + b] = (unsigned long long)facc_get(sF, 2 * nmax + b);
+                a.forces[nmax + b] = (unsigned long long)facc_get(sF, ns + b);
+                a.forces[2 * nmax + b] = (unsigned long long)facc_get(sF, 2 * ns + b);
             }
             if (tid == 0 && s_overflow) a.sys[slot].overflow = 1;
         }
@@ -755,8 +759,10 @@ __global__ void k_batch_velocity_init(int n, long long off, const float* __restr
 // SM's shared memory (the state needs `smem`; the rest holds neighbour
 // lists).
 template <typename Fn>
+// smem: shared memory the largest system needs; want: the share to aim
+// for (state + bonded records + the list budget), 0 = all that fits.
 void launch_persistent(Fn fn, int threads, BatchArgs a, int max_grid, size_t smem,
-                       cudaStream_t s, int num_sms, int list_smem_kib) {
+                       cudaStream_t s, int num_sms, size_t want) {
     int optin = 0, per_sm_smem = 0, dev = 0;
     OCM_CK(cudaGetDevice(&dev));
     OCM_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -771,7 +777,7 @@ void launch_persistent(Fn fn, int threads, BatchArgs a, int max_grid, size_t sme
     size_t share = (size_t)per_sm_smem / per_sm;
     share = share > 2048 ? share - 2048 : share;  // static + reserved per block
     share = std::min<size_t>(share, (size_t)max_dyn);
-    if (list_smem_kib >= 0) share = std::min(share, smem + (size_t)list_smem_kib * 1024);
+    if (want > 0) share = std::min(share, want);
     share = std::max(share, smem) & ~(size_t)15;
     a.smem_bytes = share;
     const int grid = std::max(1, std::min(max_grid, num_sms * per_sm));
@@ -781,7 +787,7 @@ void launch_persistent(Fn fn, int threads, BatchArgs a, int max_grid, size_t sme
 
 template <int THREADS, int TERMS, bool LABELS>
 void launch_batch_t(const BatchArgs& a, int max_grid, size_t smem, cudaStream_t s, bool integrate,
-                    bool energy, int num_sms, int lkib) {
+                    bool energy, int num_sms, size_t lkib) {
     if (integrate)
         launch_persistent(k_batch<THREADS, TERMS, LABELS, false, true>, THREADS, a, max_grid, smem, s, num_sms, lkib);
     else if (energy)
@@ -792,7 +798,7 @@ void launch_batch_t(const BatchArgs& a, int max_grid, size_t smem, cudaStream_t 
 
 template <int TERMS, bool LABELS>
 void launch_batch_threads(int threads, const BatchArgs& a, int grid, size_t smem, cudaStream_t s,
-                          bool integrate, bool energy, int num_sms, int lkib) {
+                          bool integrate, bool energy, int num_sms, size_t lkib) {
     switch (threads) {
         case 256: launch_batch_t<256, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms, lkib); break;
         case 512: launch_batch_t<512, TERMS, LABELS>(a, grid, smem, s, integrate, energy, num_sms, lkib); break;
@@ -804,8 +810,8 @@ int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 
 struct BlobLayout {
     int64_t size = 0;
-    int off_p0, off_p1, off_lab, off_invm, off_bonds, off_angles, off_dih, off_fla, off_fld,
-        off_tmask, off_masks, off_ex_start, off_ex;
+    int off_p0, off_p1, off_lab, off_invm, off_tmask, off_masks, off_ex_start, off_ex;
+    int off_bonded, bonded_bytes, rb_p, rb_ij, ra_ij, ra_k, rd, rfla, rfld;
     int n_tiles, n_masks;
 };
 
@@ -825,11 +831,19 @@ BlobLayout blob_layout(const CompiledSystem& c, int n_masks) {
     L.off_p1 = take(16 * n);
     L.off_lab = take(4 * n);
     L.off_invm = take(4 * n);
-    L.off_bonds = take((int64_t)sizeof(BondTerm) * c.bonds.size());
-    L.off_angles = take((int64_t)sizeof(AngleTerm) * c.angles.size());
-    L.off_dih = take((int64_t)sizeof(DihedralTerm) * c.dihedrals.size());
-    L.off_fla = take((int64_t)sizeof(FlaTable) * c.fla.size());
-    L.off_fld = take((int64_t)sizeof(FldTable) * c.fld.size());
+    // bonded region: bond params (float4) | bond indices (u32) | angle
+    // indices (uint2) | angle k (f32) | dihedral records (uint4) | FLA | FLD
+    L.off_bonded = (int)o;
+    const int64_t nb = (int64_t)c.bonds.size(), na = (int64_t)c.angles.size(),
+                  nd = (int64_t)c.dihedrals.size();
+    L.rb_p = take(16 * nb) - L.off_bonded;
+    L.rb_ij = take(4 * nb) - L.off_bonded;
+    L.ra_ij = take(8 * na) - L.off_bonded;
+    L.ra_k = take(4 * na) - L.off_bonded;
+    L.rd = take(16 * nd) - L.off_bonded;
+    L.rfla = take((int64_t)sizeof(FlaTable) * c.fla.size()) - L.off_bonded;
+    L.rfld = take((int64_t)sizeof(FldTable) * c.fld.size()) - L.off_bonded;
+    L.bonded_bytes = (int)(o - L.off_bonded);
     L.off_tmask = take(4 * (int64_t)L.n_tiles);
     L.off_masks = take(4 * 128 * (int64_t)n_masks);
     L.off_ex_start = take(4 * (n + 1));
@@ -1061,11 +1075,39 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     put(L.off_p1, c.p1.data(), 16 * n);
     put(L.off_lab, c.labels.data(), 4 * n);
     put(L.off_invm, c.inv_mass.data(), 4 * n);
-    put(L.off_bonds, c.bonds.data(), sizeof(BondTerm) * c.bonds.size());
-    put(L.off_angles, c.angles.data(), sizeof(AngleTerm) * c.angles.size());
-    put(L.off_dih, c.dihedrals.data(), sizeof(DihedralTerm) * c.dihedrals.size());
-    put(L.off_fla, c.fla.data(), sizeof(FlaTable) * c.fla.size());
-    put(L.off_fld, c.fld.data(), sizeof(FldTable) * c.fld.size());
+    {
+        // compact bonded records (bead indices < 2048 fit 16 bits)
+        std::vector<float4> bp(c.bonds.size());
+        std::vector<uint32_t> bij(c.bonds.size());
+        for (size_t b = 0; b < c.bonds.size(); ++b) {
+            const BondTerm& t = c.bonds[b];
+            bp[b] = make_float4(t.p0, t.p1, t.r0sq_hi, t.r0sq_lo);
+            bij[b] = (uint32_t)t.i | ((uint32_t)t.j << 16) | (t.kind == kBondGo ? 0x80000000u : 0u);
+        }
+        std::vector<uint2> aij(c.angles.size());
+        std::vector<float> ak(c.angles.size());
+        for (size_t b = 0; b < c.angles.size(); ++b) {
+            const AngleTerm& t = c.angles[b];
+            aij[b] = make_uint2((uint32_t)t.i | ((uint32_t)t.j << 16), (uint32_t)t.k | ((uint32_t)t.table << 16));
+            ak[b] = t.kk;
+        }
+        std::vector<uint4> dr(c.dihedrals.size());
+        for (size_t b = 0; b < c.dihedrals.size(); ++b) {
+            const DihedralTerm& t = c.dihedrals[b];
+            uint32_t kb;
+            std::memcpy(&kb, &t.kk, 4);
+            dr[b] = make_uint4((uint32_t)t.i | ((uint32_t)t.j << 16), (uint32_t)t.k | ((uint32_t)t.l << 16),
+                               (uint32_t)t.table, kb);
+        }
+        const int ob = L.off_bonded;
+        put(ob + L.rb_p, bp.data(), 16 * bp.size());
+        put(ob + L.rb_ij, bij.data(), 4 * bij.size());
+        put(ob + L.ra_ij, aij.data(), 8 * aij.size());
+        put(ob + L.ra_k, ak.data(), 4 * ak.size());
+        put(ob + L.rd, dr.data(), 16 * dr.size());
+        put(ob + L.rfla, c.fla.data(), sizeof(FlaTable) * c.fla.size());
+        put(ob + L.rfld, c.fld.data(), sizeof(FldTable) * c.fld.size());
+    }
     put(L.off_tmask, tmask.data(), 4 * tmask.size());
     put(L.off_masks, masks.data(), 4 * masks.size());
     {
@@ -1086,8 +1128,10 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     R.n_dih = (int)c.dihedrals.size();
     R.n_masks = L.n_masks;
     R.off_p0 = L.off_p0; R.off_p1 = L.off_p1; R.off_lab = L.off_lab; R.off_invm = L.off_invm;
-    R.off_bonds = L.off_bonds; R.off_angles = L.off_angles; R.off_dih = L.off_dih;
-    R.off_fla = L.off_fla; R.off_fld = L.off_fld; R.off_tmask = L.off_tmask; R.off_masks = L.off_masks;
+    R.off_bonded = L.off_bonded; R.bonded_bytes = L.bonded_bytes;
+    R.rb_p = L.rb_p; R.rb_ij = L.rb_ij; R.ra_ij = L.ra_ij; R.ra_k = L.ra_k; R.rd = L.rd;
+    R.rfla = L.rfla; R.rfld = L.rfld;
+    R.off_tmask = L.off_tmask; R.off_masks = L.off_masks;
     R.off_ex_start = L.off_ex_start; R.off_ex = L.off_ex;
     R.skin = kBatchSkin;
     R.maxn = maxn;
@@ -1163,12 +1207,15 @@ void BatchEngine::launch(bool integrate, bool energy, int k, const std::vector<i
                          cudaStream_t s) {
     bool general = false;
     int terms = 0;
+    size_t bonded_max = 0;
     for (int32_t q : order) {
         terms |= slots_[q].terms;
         general = general || slots_[q].labels;
+        bonded_max = std::max(bonded_max, (size_t)sys_host_[q].bonded_bytes);
     }
     if (terms & ~(kTermEXV | kTermDH)) general = true;
     const size_t smem = smem_bytes(nmax_, general);
+    const size_t want = list_smem_kib_ >= 0 ? smem + bonded_max + (size_t)list_smem_kib_ * 1024 : 0;
     int optin = 0;
     OCM_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
     if ((int64_t)smem > optin)
@@ -1193,10 +1240,10 @@ void BatchEngine::launch(bool integrate, bool energy, int k, const std::vector<i
     a.slots_enabled = 0xffffffffu;
     const int grid = (int)order.size();
     if (general)
-        launch_batch_threads<15, true>(threads_, a, grid, smem, s, integrate, energy, num_sms_, list_smem_kib_);
+        launch_batch_threads<15, true>(threads_, a, grid, smem, s, integrate, energy, num_sms_, want);
     else
         launch_batch_threads<kTermEXV | kTermDH, false>(threads_, a, grid, smem, s, integrate, energy, num_sms_,
-                                                         list_smem_kib_);
+                                                         want);
 }
 
 void BatchEngine::run(int32_t k, bool sync) {
@@ -1338,9 +1385,12 @@ void BatchEngine::get_state(int64_t slot, uint32_t groups, double* forces, doubl
         a.blob = blob_dev_.p; a.k = 0; a.nmax = nmax_; a.energy = energy_.p; a.forces = forces_.p;
         a.lists = lists_.p;
         a.slots_enabled = en;
-        if (general) launch_batch_threads<15, true>(threads_, a, 1, smem, stream_, false, true, num_sms_, list_smem_kib_);
+        const size_t want = list_smem_kib_ >= 0
+                                ? smem + (size_t)sys_host_[slot].bonded_bytes + (size_t)list_smem_kib_ * 1024
+                                : 0;
+        if (general) launch_batch_threads<15, true>(threads_, a, 1, smem, stream_, false, true, num_sms_, want);
         else launch_batch_threads<kTermEXV | kTermDH, false>(threads_, a, 1, smem, stream_, false, true, num_sms_,
-                                                              list_smem_kib_);
+                                                              want);
     }
     std::vector<unsigned long long> f(3 * nmax_);
     double e[kNumSlots];

@@ -23,7 +23,12 @@ struct BatchSys {
     int n, nt, n_tiles;    // beads, 32-bead clusters, cluster pairs
     int n_bonds, n_angles, n_dih, n_masks;
     int off_p0, off_p1, off_lab, off_invm;   // byte offsets inside the blob
-    int off_bonds, off_angles, off_dih, off_fla, off_fld, off_tmask, off_masks;
+    // Compact bonded records and the FLA/FLD tables, one contiguous region
+    // [off_bonded, off_bonded + bonded_bytes) that the kernel stages into
+    // shared memory when it fits; section offsets are relative to it.
+    int off_bonded, bonded_bytes;
+    int rb_p, rb_ij, ra_ij, ra_k, rd, rfla, rfld;
+    int off_tmask, off_masks;
     int off_ex_start, off_ex;                // exclusion CSR (j | bits << 24)
     int maxn;              // neighbour-list entries per bead
     int active;

@@ -114,7 +114,9 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
     """Read a reference input file (path, bytes or an already-parsed dict).
 
     With ``fp32_positions`` the coordinates are rounded to FP32-representable
-    values, so the FP64 oracle and the FP32 kernels see the same input."""
+    values (periodic ones after wrapping into the box, whose lengths are
+    rounded to FP32 too), so the FP64 oracle and
+    the FP32 kernels see the same input."""
     if isinstance(source, dict):
         data = source
     elif isinstance(source, (bytes, bytearray)):
@@ -134,8 +136,6 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
     n = len(particles)
     masses = np.array([float(p["m"] if "m" in p else p["mass"]) for p in particles])
     pos = np.array([p["pos"] if "pos" in p else p["position"] for p in particles], float) * NM_PER_ANGSTROM
-    if fp32_positions:
-        pos = pos.astype(np.float32).astype(np.float64)
     vel = None
     if "vel" in particles[0] or "velocity" in particles[0]:
         vel = np.array([p["vel"] if "vel" in p else p["velocity"] for p in particles], float)
@@ -155,6 +155,17 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
         box = tuple((float(u) - float(lo)) * NM_PER_ANGSTROM for lo, u in zip(shape["lower"], shape["upper"]))
     elif sim["boundary_type"] != "Unlimited":
         raise ValueError(f"unknown boundary_type {sim['boundary_type']!r}")
+    if fp32_positions:
+        if periodic:
+            # the kernels hold the box and the wrapped coordinates in FP32:
+            # rounding the box and wrapping before rounding the coordinates
+            # makes these the values they use
+            box = tuple(float(np.float32(b)) for b in box)
+            L = np.array(box)
+            pos = pos - L * np.floor(pos / L)
+        pos = pos.astype(np.float32).astype(np.float64)
+        if periodic:
+            pos = np.where(pos >= L, pos - L, pos)
 
     spec = CGSpec(n=n, pos=pos, masses=masses, periodic=periodic, box=box, temperature=temperature,
                   friction=friction, dt=dt)

@@ -57,6 +57,24 @@ def test_same_alone_and_in_mix(gpu):
     assert np.array_equal(xa, xm)
 
 
+def test_threads_per_cta_do_not_change_results(gpu):
+    """The launch shape is a tuning knob only: 256, 512 and 1024 threads per
+    CTA give bit-identical trajectories (small systems split their pair
+    lists over lanes by a rule that depends on the bead count alone)."""
+    from opencafemol_gb300 import synth
+    specs = _systems([40, 100, 250, 600], seed0=900)
+    out = []
+    for th in (512, 256, 1024):
+        b = gpu.Batch(max_systems=4, max_total_beads=2048, max_beads_per_system=800)
+        b.set_threads(th)
+        slots = [b.admit(synth.build_system(s), s.pos, seed=3 + k, n_steps=150) for k, s in enumerate(specs)]
+        b.run(150)
+        out.append([b.positions(k) for k in slots])
+    for other in out[1:]:
+        for xa, xb in zip(out[0], other):
+            assert np.array_equal(xa, xb)
+
+
 def test_chunking_does_not_change_results(gpu):
     from opencafemol_gb300 import synth
     s = _systems([400], seed0=300)[0]

@@ -131,7 +131,7 @@ def test_periodic_box():
         "attributes.temperature = 310.0\nboundary_shape.lower = [0.0, 0.0, 0.0]\n"
         "boundary_shape.upper = [100.0, 120.0, 140.0]")
     s = _read(text).spec
-    assert s.periodic and s.box == pytest.approx((10.0, 12.0, 14.0))
+    assert s.periodic and s.box == pytest.approx((10.0, 12.0, 14.0), rel=1e-7)
 
 
 def test_unsupported_terms():
