@@ -265,6 +265,28 @@ int ocm_batch_set_positions_many(ocm_batch* batch, int64_t n, const int64_t* slo
 /* Read the positions of n slots, back to back in the order of `slots`, in
  * one device->host copy. */
 int ocm_batch_get_positions_many(ocm_batch* batch, int64_t n, const int64_t* slots, double* xyz);
+/* Same read-out as ocm_batch_get_positions_many, without allocating device
+ * memory: no counterpart in the reference.
+ *
+ * ocm_batch_get_positions_many grows its device staging buffers with
+ * cudaMalloc/cudaFree when a call needs more than any earlier one.  Callers
+ * that cannot allocate use this one instead: a serving loop that admits work
+ * against a fixed device-memory budget (an allocation there can fail or
+ * fragment the budget), and a host thread reading results while other
+ * streams of the device run (cudaMalloc/cudaFree may synchronise the
+ * device).  Its scratch is a fixed set of file-scope device arrays in the
+ * library (about 3 MiB per device), so it has fixed limits: at most 131072
+ * beads and 2048 slots per call; larger requests return
+ * OCM_ERR_INVALID_ARGUMENT with the limit in ocm_last_error().
+ *
+ * The first call on each device does a one-time set-up (it looks up the
+ * scratch addresses with that device current); make that first call before
+ * any stream capture.  Nothing in the scratch needs to start at zero: every
+ * call writes all of the scratch it reads.  The scratch is shared by every
+ * batch on the device, so calls that overlap in time (from several host
+ * threads) race on it and must be serialised by the caller. */
+int ocm_batch_get_positions_many_noalloc(ocm_batch* batch, int64_t n, const int64_t* slots,
+                                         double* xyz);
 int ocm_batch_steps_done(ocm_batch* batch, int64_t slot, int64_t* steps);
 /* Forces (3*n) and per-group energies (OCM_MAX_GROUPS) of one slot at its
  * current positions, evaluated by the batched kernel. */

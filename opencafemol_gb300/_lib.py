@@ -103,6 +103,7 @@ SIGNATURES = {
     "ocm_batch_steps_done": (C.c_int, [_P, C.c_int64, _I64P]),
     "ocm_batch_set_positions_many": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP]),
     "ocm_batch_get_positions_many": (C.c_int, [_P, C.c_int64, _I64P, _DP]),
+    "ocm_batch_get_positions_many_noalloc": (C.c_int, [_P, C.c_int64, _I64P, _DP]),
     "ocm_batch_get_state": (C.c_int, [_P, C.c_int64, C.c_uint32, _DP, _DP]),
     "ocm_batch_retire": (C.c_int, [_P, C.c_int64]),
     "ocm_batch_active": (C.c_int, [_P, _I64P, _I64P]),

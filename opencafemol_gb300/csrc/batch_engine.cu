@@ -19,6 +19,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -1472,6 +1474,18 @@ __global__ void k_gather_pos(int nseg, const long long* __restrict__ seg_bead,
         p[2] = z[b0 + k];
     }
 }
+
+// Scratch of ocm_batch_get_positions_many_noalloc: file-scope device arrays,
+// so that read-out never allocates device memory.  Their addresses are taken
+// once per device (noalloc_scratch).  Nothing in them needs to start at
+// zero: each call writes the segment table and every staged value it copies
+// back.  All batches of one device share them.
+constexpr int kNoAllocMaxBeads = 131072;  // 3 MiB of staged positions
+constexpr int kNoAllocMaxSlots = 2048;
+static __device__ __align__(256) double g_noalloc_stage[3 * kNoAllocMaxBeads];
+static __device__ __align__(256) long long g_noalloc_bead[kNoAllocMaxSlots];
+static __device__ __align__(256) long long g_noalloc_dst[kNoAllocMaxSlots];
+static __device__ __align__(256) int g_noalloc_n[kNoAllocMaxSlots];
 }  // namespace
 
 void BatchEngine::set_positions_many(int64_t n, const int64_t* slots, const double* xyz,
@@ -1548,6 +1562,68 @@ void BatchEngine::get_positions_many(int64_t n, const int64_t* slots, double* xy
     k_gather_pos<<<grid, 128, 0, s>>>((int)n, db.p, dd.p, dn.p, x_.p, y_.p, z_.p, buf.p);
     OCM_CK(cudaGetLastError());
     OCM_CK(cudaMemcpyAsync(xyz, buf.p, 3 * total * sizeof(double), cudaMemcpyDeviceToHost, s));
+    OCM_CK(cudaStreamSynchronize(s));
+}
+
+namespace {
+struct NoAllocScratch {
+    double* stage = nullptr;
+    long long* bead = nullptr;
+    long long* dst = nullptr;
+    int* n = nullptr;
+};
+
+// Device addresses of the no-alloc scratch for `device`, taken with that
+// device current on first use and cached (the one set-up step).
+NoAllocScratch noalloc_scratch(int device) {
+    static std::mutex mu;
+    static std::map<int, NoAllocScratch> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(device);
+    if (it != cache.end()) return it->second;
+    NoAllocScratch sc;
+    OCM_CK(cudaGetSymbolAddress(reinterpret_cast<void**>(&sc.stage), g_noalloc_stage));
+    OCM_CK(cudaGetSymbolAddress(reinterpret_cast<void**>(&sc.bead), g_noalloc_bead));
+    OCM_CK(cudaGetSymbolAddress(reinterpret_cast<void**>(&sc.dst), g_noalloc_dst));
+    OCM_CK(cudaGetSymbolAddress(reinterpret_cast<void**>(&sc.n), g_noalloc_n));
+    cache.emplace(device, sc);
+    return sc;
+}
+}  // namespace
+
+void BatchEngine::get_positions_many_noalloc(int64_t n, const int64_t* slots, double* xyz) {
+    OCM_CK(cudaSetDevice(device_));
+    if (n <= 0) return;
+    if (n > kNoAllocMaxSlots)
+        throw Error(1, "[error] ocm_batch_get_positions_many_noalloc reads at most " +
+                           std::to_string(kNoAllocMaxSlots) + " slots per call (asked for " +
+                           std::to_string(n) + "); use ocm_batch_get_positions_many");
+    // segment table in per-thread host storage: no heap allocation per call
+    thread_local long long h_bead[kNoAllocMaxSlots], h_dst[kNoAllocMaxSlots];
+    thread_local int h_n[kNoAllocMaxSlots];
+    long long total = 0;
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t sl = slots[k];
+        if (sl < 0 || sl >= max_systems_ || !slots_[sl].used) throw Error(1, "[error] invalid slot");
+        h_bead[k] = slots_[sl].bead_off;
+        h_dst[k] = total;
+        h_n[k] = (int)slots_[sl].n;
+        total += slots_[sl].n;
+    }
+    if (total > kNoAllocMaxBeads)
+        throw Error(1, "[error] ocm_batch_get_positions_many_noalloc reads at most " +
+                           std::to_string(kNoAllocMaxBeads) + " beads per call (asked for " +
+                           std::to_string(total) + "); use ocm_batch_get_positions_many");
+    const NoAllocScratch sc = noalloc_scratch(device_);
+    cudaStream_t s = stream_;
+    OCM_CK(cudaStreamSynchronize(s));
+    OCM_CK(cudaMemcpyAsync(sc.bead, h_bead, n * sizeof(long long), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(sc.dst, h_dst, n * sizeof(long long), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(sc.n, h_n, n * sizeof(int), cudaMemcpyHostToDevice, s));
+    const dim3 grid(8, (unsigned)n);
+    k_gather_pos<<<grid, 128, 0, s>>>((int)n, sc.bead, sc.dst, sc.n, x_.p, y_.p, z_.p, sc.stage);
+    OCM_CK(cudaGetLastError());
+    OCM_CK(cudaMemcpyAsync(xyz, sc.stage, 3 * total * sizeof(double), cudaMemcpyDeviceToHost, s));
     OCM_CK(cudaStreamSynchronize(s));
 }
 

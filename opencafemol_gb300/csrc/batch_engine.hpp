@@ -78,6 +78,8 @@ class BatchEngine {
     void slot_stats(int64_t slot, int32_t* builds, int32_t* capacity);
     void set_positions_many(int64_t n, const int64_t* slots, const double* xyz, const double* v);
     void get_positions_many(int64_t n, const int64_t* slots, double* xyz);
+    // Same result without allocating device memory (fixed per-device scratch).
+    void get_positions_many_noalloc(int64_t n, const int64_t* slots, double* xyz);
     int threads() const { return threads_; }
 
   private:

@@ -475,6 +475,11 @@ int ocm_batch_get_positions_many(ocm_batch* batch, int64_t n, const int64_t* slo
     BATCH_CALL(if (n) { need(slots, "slots"); need(xyz, "xyz"); }
                batch->b->get_positions_many(n, slots, xyz));
 }
+int ocm_batch_get_positions_many_noalloc(ocm_batch* batch, int64_t n, const int64_t* slots,
+                                         double* xyz) {
+    BATCH_CALL(if (n) { need(slots, "slots"); need(xyz, "xyz"); }
+               batch->b->get_positions_many_noalloc(n, slots, xyz));
+}
 int ocm_batch_steps_done(ocm_batch* batch, int64_t slot, int64_t* steps) {
     BATCH_CALL(need(steps, "steps"); *steps = batch->b->steps_done(slot));
 }

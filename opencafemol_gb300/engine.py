@@ -175,6 +175,16 @@ class Batch:
         check(lib.ocm_batch_get_positions_many(self._h, len(sl), i64ptr(sl), dptr(out)))
         return out
 
+    def get_positions_many_noalloc(self, slots, out=None) -> np.ndarray:
+        """``get_positions_many`` through fixed per-device scratch (no device
+        allocation; at most 131072 beads and 2048 slots per call)."""
+        sl = np.ascontiguousarray(slots, np.int64)
+        total = sum(self._n[int(k)] for k in sl)
+        if out is None:
+            out = np.zeros((total, 3))
+        check(lib.ocm_batch_get_positions_many_noalloc(self._h, len(sl), i64ptr(sl), dptr(out)))
+        return out
+
     def steps_done(self, slot: int) -> int:
         s = C.c_int64()
         check(lib.ocm_batch_steps_done(self._h, int(slot), C.byref(s)))
