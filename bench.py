@@ -63,13 +63,20 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            time.sleep(0.5)  # let the sampler start before the timed region
         except (FileNotFoundError, OSError):
             self.proc = None
+        self.first = len(self.lines)
+        self.last = None
         return self
+
+    def stop_marker(self):
+        """End of the timed region: later samples are not summarised."""
+        self.last = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -86,7 +93,7 @@ class ClockSampler:
     def summary(self) -> dict:
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for line in self.lines[self.first:self.last]:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 8:
                 continue
@@ -132,6 +139,10 @@ FLOPS_PER_BEAD = 40
 # integrator: read F (24), x (12), v (12), 1/m (4); write x (12), v (12),
 # zero F (24)
 BYTES_INTEGRATE_PER_BEAD = 100
+# dram__bytes_read.sum + dram__bytes_write.sum of one timed k_batch launch of
+# the default workload (100 MD steps of the 512-replica mix), from a
+# `ncu --set full --clock-control none` capture of this script
+K_BATCH_DRAM_BYTES = 20386304 + 256
 
 
 def measured_hbm_gbs():
@@ -209,6 +220,7 @@ def run_ours(args, rank, world):
             times.append(batch.last_run_ms() / 1e3)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        clk.stop_marker()
     dist_barrier(world)
     dev_time = float(np.sum(times))
     dev_time = dist_max(dev_time, world)
@@ -220,6 +232,7 @@ def run_ours(args, rank, world):
 
     # ---- plain single-system path on a sample of the same mix ----
     plain = run_plain(ocm, specs, systems, args)
+    plain_cfgs = run_plain_configs(ocm, args) if args.cfg1_steps > 0 else None
 
     # ---- served stream (continuous batching), p50/p99 completion latency ----
     serve = run_serving(ocm, args) if args.serve_requests > 0 and rank == 0 else None
@@ -243,6 +256,7 @@ def run_ours(args, rank, world):
                    "l2": "flushed (256 MiB write) between timed launches"},
         "e2e": e2e, "gpu_launches": args.steps, "roofline": roof, "cpu_baseline": cpu,
         "plain_path": plain,
+        "plain_single_system": plain_cfgs,
         "serving": serve,
         "batched_vs_plain": value / world / plain["value"] if plain and plain.get("value") else None,
         "clocks": clk.summary(), "wall_s": wall,
@@ -336,6 +350,47 @@ def run_plain(ocm, specs, systems, args):
             "what": "one Context per system, systems stepped sequentially"}
 
 
+def run_plain_configs(ocm, args):
+    """The plain single-system path on the two single-system shapes:
+    a 60-bead Go protein (10 fs steps, non-periodic) and a 20,000-bead HPS
+    condensate slab (100 chains x 200 beads, 15 x 15 x 150 nm periodic box,
+    HPS cutoff 2.0 nm, Debye-Hueckel 3.5 nm on 20% charged beads).  The slab
+    starts from a random packing, so it is relaxed first (untimed, strong
+    friction, 2 fs steps).  Wall-clock timing around synchronous steps."""
+    from opencafemol_gb300 import synth
+    out = {}
+    cases = [("go_protein_60", synth.go_protein(60, 11), 0, args.cfg0_steps),
+             ("hps_slab_20000", synth.hps_slab(100, 200, (15.0, 15.0, 150.0), slab_width=30.0, seed=7),
+              args.cfg1_relax, args.cfg1_steps)]
+    for name, spec, relax, steps in cases:
+        system = synth.build_system(spec)
+        pos = spec.pos
+        if relax:
+            # strong friction and 2 fs steps take the random packing's
+            # overlaps out without heating the system
+            rel = ocm.Context(system, ocm.LangevinIntegrator(spec.temperature, 5.0, 0.002, 3),
+                              device=local_device())
+            rel.setPositions(pos)
+            rel.setVelocitiesToTemperature(spec.temperature, 3)
+            rel.step(relax)
+            pos = rel.getPositions()
+            del rel
+        ctx = ocm.Context(system, ocm.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, 5),
+                          device=local_device())
+        ctx.setPositions(pos)
+        ctx.setVelocitiesToTemperature(spec.temperature, 5)
+        ctx.step(200)  # graph capture and the first list builds
+        t0 = time.perf_counter()
+        ctx.step(steps)
+        t = time.perf_counter() - t0
+        st = ctx.stats()
+        out[name] = {"beads": int(spec.n), "steps": int(steps), "bead_steps_per_s": spec.n * steps / t,
+                     "ns_per_day": steps / t * spec.dt * 86400 * 1e-3, "us_per_step": t / steps * 1e6,
+                     "list_builds": int(st["list_builds"]), "tiles": int(st["tiles"]),
+                     "untimed_relaxation_steps": int(relax)}
+    return out
+
+
 def run_cpu_baseline(specs, sample_systems=48, md_steps=20):
     from concurrent.futures import ThreadPoolExecutor
 
@@ -413,7 +468,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--md-steps", type=int, default=100)
@@ -423,8 +478,11 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--serve-requests", type=int, default=96)
-    ap.add_argument("--traffic-bytes", type=float, default=0.0,
-                    help="DRAM bytes per k_batch launch from an ncu capture, reported as roofline.traffic")
+    ap.add_argument("--traffic-bytes", type=float, default=K_BATCH_DRAM_BYTES,
+                    help="DRAM bytes per k_batch launch (ncu), reported as roofline.traffic")
+    ap.add_argument("--cfg0-steps", type=int, default=10000)
+    ap.add_argument("--cfg1-steps", type=int, default=2000)
+    ap.add_argument("--cfg1-relax", type=int, default=3000)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-step-scale", type=int, default=50)
     ap.add_argument("--serve-chunk", type=int, default=100)

@@ -1048,14 +1048,17 @@ void PlainContext::ensure_capacity() {
         OCM_CK(cudaMemcpyAsync(&masks, mask_count_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
         OCM_CK(cudaMemcpyAsync(&flags, flags_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
         OCM_CK(cudaStreamSynchronize(stream_));
-        bool grown = false;
+        // A buffer that is reallocated loses the list just built into it, so
+        // any growth (also the pre-emptive one below 80% headroom) is
+        // followed by another build before the list is used.
+        bool realloced = false;
         if (total > tile_cap_ || (int64_t)total * 5 / 4 + 64 > tile_cap_) {
             const int64_t want = std::min<int64_t>(nc * (nc + 1) / 2, (int64_t)total * 2 + 1024);
             if (want > tile_cap_) {
                 tile_cap_ = want;
                 tile_j_.alloc(tile_cap_);
                 tile_mask_.alloc(tile_cap_);
-                grown = total > 0;
+                realloced = true;
                 clear_graphs();
             }
         }
@@ -1064,17 +1067,17 @@ void PlainContext::ensure_capacity() {
             if (want > mask_cap_) {
                 mask_cap_ = want;
                 masks_.alloc(mask_cap_ * 128);
+                realloced = true;
                 clear_graphs();
             }
         }
-        if (!(flags & (ListFlags::kTileOverflow | ListFlags::kMaskOverflow)) && total <= tile_cap_ &&
-            masks <= mask_cap_) {
+        if (!realloced && !(flags & (ListFlags::kTileOverflow | ListFlags::kMaskOverflow)) &&
+            total <= tile_cap_ && masks <= mask_cap_) {
             tiles_last = total;
             masked_last = masks;
             list_builds++;
             return;
         }
-        (void)grown;
     }
     throw Error(4, "[error] tile list capacity could not be established");
 }

@@ -248,7 +248,10 @@ def hps_slab(n_chains: int, chain_len: int, box, slab_width: float, seed: int,
                     cand = pos[i - 1] + 0.38 * dvec
                     if cand[2] < zlo or cand[2] > zhi:
                         continue
-                    if not clash(cand, skip=(i - 1, i - 2)):
+                    # only the bonded predecessor may be closer than min_dist (the
+                    # bond-angle range keeps i-2 at >= 0.58 nm; a free direction
+                    # must not fold back onto it)
+                    if not clash(cand, skip=(i - 1,)):
                         placed = True
                         break
                 if not placed:

@@ -222,6 +222,70 @@ static void gaussian3(uint32_t seed, uint32_t stream, uint32_t bead, uint64_t st
 
 using namespace oracle;
 
+// Every unordered pair (i < j) closer than `cell` (minimum image when
+// periodic) exactly once, found through a grid of cells at least `cell`
+// wide.  Returns false (nothing visited) when a periodic box is narrower
+// than three cells, where the all-pairs loop applies.
+template <class Fn>
+static bool cell_pairs(int64_t n, const V3* x, bool periodic, const double L[3], double cell, Fn&& fn) {
+    double lo[3], ext[3];
+    int nc[3];
+    for (int c = 0; c < 3; ++c) {
+        if (periodic) {
+            lo[c] = 0;
+            ext[c] = L[c];
+        } else {
+            double mn = 1e300, mx = -1e300;
+            for (int64_t i = 0; i < n; ++i) {
+                const double v = c == 0 ? x[i].x : (c == 1 ? x[i].y : x[i].z);
+                mn = std::min(mn, v);
+                mx = std::max(mx, v);
+            }
+            lo[c] = mn;
+            ext[c] = mx - mn + 1e-9;
+        }
+        nc[c] = std::max(1, (int)std::floor(ext[c] / cell));
+        if (periodic && nc[c] < 3) return false;
+        nc[c] = std::min(nc[c], 1024);
+    }
+    const int64_t ncell = (int64_t)nc[0] * nc[1] * nc[2];
+    std::vector<int64_t> head(ncell, -1), next(n, -1);
+    std::vector<int> cidx(3 * n);
+    for (int64_t i = 0; i < n; ++i) {
+        const double v[3] = {x[i].x, x[i].y, x[i].z};
+        int64_t lin = 0;
+        for (int c = 0; c < 3; ++c) {
+            double w = v[c] - lo[c];
+            if (periodic) w -= L[c] * std::floor(w / L[c]);
+            int k = (int)std::floor(w / ext[c] * nc[c]);
+            k = std::min(nc[c] - 1, std::max(0, k));
+            cidx[3 * i + c] = k;
+            lin = lin * nc[c] + k;
+        }
+        next[i] = head[lin];
+        head[lin] = i;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        const int* ci = &cidx[3 * i];
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dz = -1; dz <= 1; ++dz) {
+                    int k[3] = {ci[0] + dx, ci[1] + dy, ci[2] + dz};
+                    bool ok = true;
+                    int64_t lin = 0;
+                    for (int c = 0; c < 3; ++c) {
+                        if (periodic) k[c] = (k[c] + nc[c]) % nc[c];
+                        else if (k[c] < 0 || k[c] >= nc[c]) ok = false;
+                        lin = lin * nc[c] + k[c];
+                    }
+                    if (!ok) continue;
+                    for (int64_t j = head[lin]; j >= 0; j = next[j])
+                        if (j > i) fn(i, j);
+                }
+    }
+    return true;
+}
+
 extern "C" {
 
 // Flat description of one system in the units the generators receive.
@@ -274,6 +338,8 @@ typedef struct OracleSystem {
     const double* lja_sigma;
     int lja_ign_bond, lja_ign_contact;
     int fp32_cutoff;  // decide r < rc on the engine's FP32 r^2
+    // pair enumeration: 0 all pairs, 1 cell grid, -1 cell grid above 4096 beads
+    int pair_cells;
 } OracleSystem;
 
 // Energy slots: EXV, DH, LJR, LJA, HB, GO, FLA, FLD.
@@ -547,9 +613,9 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
     float rc2f[4];
     for (int t = 0; t < 4; ++t) rc2f[t] = (float)(T[t].rc * T[t].rc);
     const bool any_pair = s->exv_on || s->dh_on || s->ljr_on || s->lja_on;
-    if (any_pair) {
-        for (int64_t i = 0; i < n; ++i) {
-            for (int64_t j = i + 1; j < n; ++j) {
+    // One unordered pair (i < j): every pair term, exclusions and the
+    // FP32 cutoff emulation; both enumerations below call it.
+    auto pair = [&](int64_t i, int64_t j) {
                 const V3 d = min_image(sub(x[j], x[i]), s->periodic);
                 const double r2 = dot(d, d);
                 const double r = std::sqrt(r2);
@@ -621,7 +687,15 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
                     add(i, scale(d, -sc));
                     add(j, scale(d, sc));
                 }
-            }
+    };
+    if (any_pair) {
+        double rcmax = 0;
+        for (int t = 0; t < 4; ++t)
+            if (T[t].on) rcmax = std::max(rcmax, T[t].rc);
+        const bool want_cells = s->pair_cells > 0 || (s->pair_cells < 0 && n > 4096);
+        if (!want_cells || !cell_pairs(n, x.data(), s->periodic, L, rcmax * 1.0001, pair)) {
+            for (int64_t i = 0; i < n; ++i)
+                for (int64_t j = i + 1; j < n; ++j) pair(i, j);
         }
     }
     if (forces)

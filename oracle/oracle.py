@@ -34,7 +34,7 @@ class OracleSystem(C.Structure):
         ("ljr_ign_bond", C.c_int), ("ljr_ign_contact", C.c_int),
         ("lja_on", C.c_int), ("lja_ratio", C.c_double), ("lja_eps", _D), ("lja_sigma", _D),
         ("lja_ign_bond", C.c_int), ("lja_ign_contact", C.c_int),
-        ("fp32_cutoff", C.c_int),
+        ("fp32_cutoff", C.c_int), ("pair_cells", C.c_int),
     ]
 
 
@@ -96,7 +96,7 @@ class _Keep:
         return arr.ctypes.data_as(_I32)
 
 
-def make_system(spec, fp32_cutoff: bool = True, pos=None):
+def make_system(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
     """Translate a synth.CGSpec into the oracle's flat description."""
     k = _Keep()
     s = OracleSystem()
@@ -134,6 +134,7 @@ def make_system(spec, fp32_cutoff: bool = True, pos=None):
         s.lja_on, s.lja_ratio, s.lja_eps, s.lja_sigma = 1, t.ratio, k.d(t.p0), k.d(t.p1)
         s.lja_ign_bond, s.lja_ign_contact = t.ign_bond, t.ign_contact
     s.fp32_cutoff = int(fp32_cutoff)
+    s.pair_cells = int(cells)
     return s, k
 
 
@@ -141,9 +142,11 @@ SLOTS = ("ExcludedVolume", "DebyeHuckel", "LennardJonesRepulsive", "LennardJones
          "HarmonicBond", "GoContact", "FlexibleLocalAngle", "FlexibleLocalDihedral")
 
 
-def evaluate(spec, fp32_cutoff: bool = True, pos=None):
-    """FP64 forces (n, 3) and per-term energies {name: kJ/mol}."""
-    s, keep = make_system(spec, fp32_cutoff, pos)
+def evaluate(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
+    """FP64 forces (n, 3) and per-term energies {name: kJ/mol}.  Pairs are
+    enumerated over all pairs (cells=0) or a cell grid (cells=1; -1 picks
+    the grid above 4096 beads)."""
+    s, keep = make_system(spec, fp32_cutoff, pos, cells)
     f = np.zeros((spec.n, 3))
     e = np.zeros(8)
     lib().oracle_evaluate(C.byref(s), f.ctypes.data_as(_D), e.ctypes.data_as(_D))

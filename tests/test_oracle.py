@@ -235,3 +235,20 @@ def test_langevin_friction_free_is_leapfrog():
 def test_oracle_noise_is_standard_normal():
     g = np.array([oracle.gaussian3(9, 0, b, 3) for b in range(20000)]).ravel()
     assert abs(g.mean()) < 0.02 and abs(g.std() - 1) < 0.02
+
+
+@pytest.mark.parametrize("case", ["slab", "protein"])
+def test_cell_grid_matches_all_pairs(case):
+    """The oracle's cell-grid pair enumeration (used for large systems)
+    visits exactly the pairs of the all-pairs loop."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    if case == "slab":
+        spec = synth.hps_slab(12, 100, (12.0, 12.0, 40.0), slab_width=14.0, seed=21)
+    else:
+        spec = synth.go_protein(700, 22)
+    f0, e0 = oracle.evaluate(spec, cells=0)
+    f1, e1 = oracle.evaluate(spec, cells=1)
+    assert np.max(np.abs(f1 - f0)) <= 1e-9 * np.abs(f0).max()
+    for k in e0:
+        assert abs(e1[k] - e0[k]) <= 1e-9 * max(1.0, abs(e0[k])), k

@@ -187,3 +187,30 @@ def test_long_run_stays_finite_and_rebuilds(gpu):
     assert np.all(np.isfinite(x))
     st = ctx.stats()
     assert st["steps_done"] == 500 and st["list_builds"] >= 500 // max(1, st["rebuild_interval"])
+
+
+def test_first_evaluation_after_list_growth(gpu):
+    """An 8,000-bead slab outgrows the initial tile and mask capacity on the
+    first evaluation: the forces of that evaluation, of a repeated one and
+    of one after dynamics all match the oracle (a regrown buffer must be
+    rebuilt before use)."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    spec = synth.hps_slab(40, 200, (15.0, 15.0, 150.0), slab_width=30.0, seed=31)
+    system, ctx = _ctx(gpu, spec)
+    f1, _ = ctx.getState(energy=False)
+    f2, _ = ctx.getState(energy=False)
+    assert np.array_equal(f1, f2)
+    f_ref, _ = oracle.evaluate(spec, cells=1)
+    assert rel_force_err(f1, f_ref) <= FORCE_TOL
+    ctx.step(300)
+    # the kernels compute pairs from FP32 box-frame coordinates: hand both
+    # sides the same FP32-exact configuration
+    L = np.array(spec.box)
+    x = ctx.getPositions()
+    x = (x - L * np.floor(x / L)).astype(np.float32).astype(np.float64)
+    x = np.where(x >= L, x - L, x)
+    ctx.setPositions(x)
+    f3, _ = ctx.getState(energy=False)
+    f_ref3, _ = oracle.evaluate(spec, pos=x, cells=1)
+    assert rel_force_err(f3, f_ref3) <= FORCE_TOL
