@@ -96,6 +96,7 @@ class PlainContext {
     bool positions_set_ = false;
     LangevinConsts lc_{};
     int cell_dims_[3] = {1, 1, 1};
+    int num_sms_ = 1;
     int64_t n_cells_ = 0;
     int64_t tile_cap_ = 0, mask_cap_ = 0;
     float3 box_{0, 0, 0}, inv_box_{0, 0, 0};

@@ -30,6 +30,7 @@ namespace {
 
 constexpr int kForceThreads = 128;
 constexpr int kWarpsPerForceBlock = kForceThreads / 32;
+constexpr int kTilesPerChunk = 4;
 constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ float4 shfl4(float4 v, int src) {
@@ -336,90 +337,119 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
     int blk = blockIdx.x;
     if (blk < a.blocks_tiles) {
         // ---------------- cluster-pair tiles ----------------
-        const int I = blk * kWarpsPerForceBlock + (threadIdx.x >> 5);
-        if (I >= a.nc) return;
-        if (a.tile_start[a.nc] > a.tile_cap) return;  // overflowed list (flagged for a retry)
-        const int ki = I * 32 + lane;
-        const float4 xi = a.xs[ki];
-        const float4 p0i = a.p0s[ki];
-        const float4 p1i = (TERMS & kTermLJA) ? a.p1s[ki] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const uint32_t labi = a.labs[ki];
+        // Warps take chunks of kTilesPerChunk consecutive tiles of the
+        // flattened (row-major) tile list in a grid-stride loop, so every
+        // SM holds many warps whatever the row lengths; the i-side force of
+        // a row is flushed when the chunk crosses into the next row.
+        // Fixed-point accumulation keeps the result independent of the split.
+        const int total = a.tile_start[a.nc];
+        if (total > a.tile_cap) return;  // overflowed list (flagged for a retry)
+        const int gw = blk * kWarpsPerForceBlock + (threadIdx.x >> 5);
+        const int stride = a.blocks_tiles * kWarpsPerForceBlock * kTilesPerChunk;
         const bool labels = a.pc.uses_labels != 0;
-        float3 fi = make_float3(0.f, 0.f, 0.f);
         double eacc[4] = {0.0, 0.0, 0.0, 0.0};
-        const int t0 = a.tile_start[I], t1 = a.tile_start[I + 1];
-        for (int t = t0; t < t1; ++t) {
-            const int J = a.tile_j[t];
-            const int m = a.tile_mask[t];
-            const int kj = J * 32 + lane;
-            float4 xj = a.xs[kj];
-            float4 p0j = a.p0s[kj];
-            float4 p1j = (TERMS & kTermLJA) ? a.p1s[kj] : make_float4(0.f, 0.f, 0.f, 0.f);
-            uint32_t labj = a.labs[kj];
-            float3 fj = make_float3(0.f, 0.f, 0.f);
-            uint32_t mw[4] = {0u, 0u, 0u, 0u};
-            if (m >= 0) {
-#pragma unroll
-                for (int term = 0; term < 4; ++term)
-                    if (TERMS & (1 << term)) mw[term] = a.masks[(size_t)m * 128 + term * 32 + lane];
+        for (int c0 = gw * kTilesPerChunk; c0 < total; c0 += stride) {
+            const int c1 = min(total, c0 + kTilesPerChunk);
+            // row of tile c0: the last I with tile_start[I] <= c0
+            int lo = 0, hi = a.nc - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (a.tile_start[mid] <= c0) lo = mid;
+                else hi = mid - 1;
             }
-            const bool diag = (J == I);
-            PairEnergy e;
-            e.zero();
-            for (int r = 0; r < 32; ++r) {
-                const bool do_pair = !diag || (r > 0 && (r < 16 || (r == 16 && lane < 16)));
-                if (do_pair) {
-                    const float3 d = separation<PERIODIC>(xi, xj, a.box, a.inv_box);
-                    const float r2 = norm2(d);
-                    if (r2 < a.pc.list_rc2) {
-                        uint32_t ex = a.excl_all;
-#pragma unroll
-                        for (int term = 0; term < 4; ++term)
-                            if (TERMS & (1 << term)) ex |= ((mw[term] >> r) & 1u) << term;
-                        if (labels) {
-#pragma unroll
+            int I = lo;
+            int row_end = a.tile_start[I + 1];
+            int ki = I * 32 + lane;
+            float4 xi = a.xs[ki];
+            float4 p0i = a.p0s[ki];
+            float4 p1i = (TERMS & kTermLJA) ? a.p1s[ki] : make_float4(0.f, 0.f, 0.f, 0.f);
+            uint32_t labi = a.labs[ki];
+            float3 fi = make_float3(0.f, 0.f, 0.f);
+            for (int t = c0; t < c1; ++t) {
+                while (t >= row_end) {
+                    const int oi = a.perm[ki];
+                    if (oi >= 0) add_force(a.F, a.n, oi, fi);
+                    fi = make_float3(0.f, 0.f, 0.f);
+                    ++I;
+                    row_end = a.tile_start[I + 1];
+                    ki = I * 32 + lane;
+                    xi = a.xs[ki];
+                    p0i = a.p0s[ki];
+                    if (TERMS & kTermLJA) p1i = a.p1s[ki];
+                    labi = a.labs[ki];
+                }
+                const int J = a.tile_j[t];
+                const int m = a.tile_mask[t];
+                const int kj = J * 32 + lane;
+                float4 xj = a.xs[kj];
+                float4 p0j = a.p0s[kj];
+                float4 p1j = (TERMS & kTermLJA) ? a.p1s[kj] : make_float4(0.f, 0.f, 0.f, 0.f);
+                uint32_t labj = a.labs[kj];
+                float3 fj = make_float3(0.f, 0.f, 0.f);
+                uint32_t mw[4] = {0u, 0u, 0u, 0u};
+                if (m >= 0) {
+    #pragma unroll
+                    for (int term = 0; term < 4; ++term)
+                        if (TERMS & (1 << term)) mw[term] = a.masks[(size_t)m * 128 + term * 32 + lane];
+                }
+                const bool diag = (J == I);
+                PairEnergy e;
+                e.zero();
+                for (int r = 0; r < 32; ++r) {
+                    const bool do_pair = !diag || (r > 0 && (r < 16 || (r == 16 && lane < 16)));
+                    if (do_pair) {
+                        const float3 d = separation<PERIODIC>(xi, xj, a.box, a.inv_box);
+                        const float r2 = norm2(d);
+                        if (r2 < a.pc.list_rc2) {
+                            uint32_t ex = a.excl_all;
+    #pragma unroll
                             for (int term = 0; term < 4; ++term)
-                                if ((TERMS & (1 << term)) && (a.pc.uses_labels & (1 << term)) &&
-                                    !labels_allow(labi, labj, term, a.pc.allow[term]))
-                                    ex |= 1u << term;
+                                if (TERMS & (1 << term)) ex |= ((mw[term] >> r) & 1u) << term;
+                            if (labels) {
+    #pragma unroll
+                                for (int term = 0; term < 4; ++term)
+                                    if ((TERMS & (1 << term)) && (a.pc.uses_labels & (1 << term)) &&
+                                        !labels_allow(labi, labj, term, a.pc.allow[term]))
+                                        ex |= 1u << term;
+                            }
+                            const float s = pair_scalar<TERMS, ENERGY>(r2, p0i, p0j, p1i, p1j, ex, a.pc, e);
+                            fi.x -= s * d.x;
+                            fi.y -= s * d.y;
+                            fi.z -= s * d.z;
+                            fj.x += s * d.x;
+                            fj.y += s * d.y;
+                            fj.z += s * d.z;
                         }
-                        const float s = pair_scalar<TERMS, ENERGY>(r2, p0i, p0j, p1i, p1j, ex, a.pc, e);
-                        fi.x -= s * d.x;
-                        fi.y -= s * d.y;
-                        fi.z -= s * d.z;
-                        fj.x += s * d.x;
-                        fj.y += s * d.y;
-                        fj.z += s * d.z;
                     }
+                    const int src = (lane + 1) & 31;
+                    xj = shfl4(xj, src);
+                    if (TERMS & kTermEXV) p0j.x = __shfl_sync(kFull, p0j.x, src);
+                    if (TERMS & kTermDH) p0j.y = __shfl_sync(kFull, p0j.y, src);
+                    if (TERMS & kTermLJR) {
+                        p0j.z = __shfl_sync(kFull, p0j.z, src);
+                        p0j.w = __shfl_sync(kFull, p0j.w, src);
+                    }
+                    if (TERMS & kTermLJA) {
+                        p1j.x = __shfl_sync(kFull, p1j.x, src);
+                        p1j.y = __shfl_sync(kFull, p1j.y, src);
+                    }
+                    if (labels) labj = __shfl_sync(kFull, labj, src);
+                    fj.x = __shfl_sync(kFull, fj.x, src);
+                    fj.y = __shfl_sync(kFull, fj.y, src);
+                    fj.z = __shfl_sync(kFull, fj.z, src);
                 }
-                const int src = (lane + 1) & 31;
-                xj = shfl4(xj, src);
-                if (TERMS & kTermEXV) p0j.x = __shfl_sync(kFull, p0j.x, src);
-                if (TERMS & kTermDH) p0j.y = __shfl_sync(kFull, p0j.y, src);
-                if (TERMS & kTermLJR) {
-                    p0j.z = __shfl_sync(kFull, p0j.z, src);
-                    p0j.w = __shfl_sync(kFull, p0j.w, src);
+                const int oj = a.perm[kj];
+                if (oj >= 0) add_force(a.F, a.n, oj, fj);
+                if (ENERGY) {
+                    eacc[0] += e.exv;
+                    eacc[1] += e.dh;
+                    eacc[2] += e.ljr;
+                    eacc[3] += e.lja;
                 }
-                if (TERMS & kTermLJA) {
-                    p1j.x = __shfl_sync(kFull, p1j.x, src);
-                    p1j.y = __shfl_sync(kFull, p1j.y, src);
-                }
-                if (labels) labj = __shfl_sync(kFull, labj, src);
-                fj.x = __shfl_sync(kFull, fj.x, src);
-                fj.y = __shfl_sync(kFull, fj.y, src);
-                fj.z = __shfl_sync(kFull, fj.z, src);
             }
-            const int oj = a.perm[kj];
-            if (oj >= 0) add_force(a.F, a.n, oj, fj);
-            if (ENERGY) {
-                eacc[0] += e.exv;
-                eacc[1] += e.dh;
-                eacc[2] += e.ljr;
-                eacc[3] += e.lja;
-            }
+            const int oi = a.perm[ki];
+            if (oi >= 0) add_force(a.F, a.n, oi, fi);
         }
-        const int oi = a.perm[ki];
-        if (oi >= 0) add_force(a.F, a.n, oi, fi);
         if (ENERGY) {
 #pragma unroll
             for (int term = 0; term < 4; ++term) {
@@ -695,6 +725,7 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
         throw Error(2, "[error] no CUDA device is available");
     if (dev < 0 || dev >= count) throw Error(1, "[error] invalid device index");
     OCM_CK(cudaSetDevice(dev));
+    OCM_CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
     if (!(dt > 0)) throw Error(1, "[error] step size must be positive");
     if (!(friction >= 0)) throw Error(1, "[error] friction must be >= 0");
     if (!(temperature >= 0)) throw Error(1, "[error] temperature must be >= 0");
@@ -973,7 +1004,10 @@ void PlainContext::launch_forces(cudaStream_t s, bool energy, uint32_t slots_ena
     a.nc = (int)nc;
     a.tile_cap = (int)tile_cap_;
     a.n = (int)n;
-    a.blocks_tiles = div_up(nc, kWarpsPerForceBlock);
+    // enough warps for every chunk of the largest list the buffers hold,
+    // capped at 32 resident blocks per SM (the loop strides over the rest)
+    a.blocks_tiles = (int)std::max<int64_t>(
+        1, std::min<int64_t>(div_up(tile_cap_, kTilesPerChunk * kWarpsPerForceBlock), 32 * (int64_t)num_sms_));
     a.n_bonds = (int)cs.bonds.size();
     a.n_angles = (int)cs.angles.size();
     a.n_dih = (int)cs.dihedrals.size();
