@@ -222,9 +222,7 @@ def run_ours(args, rank, world):
         wall = time.perf_counter() - t0
         clk.stop_marker()
     dist_barrier(world)
-    dev_time = float(np.sum(times))
-    dev_time = dist_max(dev_time, world)
-    value = beads * K * args.steps * world / dev_time
+    value, dev_time = aggregate(beads, K, args.steps, float(np.sum(times)), world)
     ms_per_step = dev_time / args.steps * 1e3
 
     # ---- end to end through the public API with host buffers ----
@@ -427,13 +425,22 @@ def dist_barrier(world):
 
 
 def dist_max(v, world):
+    """Max of a host value over ranks (NCCL on the GPUs, gloo on the host)."""
     if world <= 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate(beads, md_steps, steps, dev_time_local, world):
+    """Whole-job bead-steps/s: every rank advances its own replica set by the
+    same work; the job's time is the slowest rank's (weak scaling)."""
+    t = dist_max(dev_time_local, world)
+    return beads * md_steps * steps * world / t, t
 
 
 def run_reference(args, rank, world):
