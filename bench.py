@@ -200,11 +200,16 @@ def run_ours(args, rank, world):
 
     batch = ocm.Batch(max_systems=len(specs), max_total_beads=beads + 1024,
                       max_beads_per_system=SIZE_HI, device=local_device())
-    if args.threads:
-        batch.set_threads(args.threads)
     slots = [batch.admit(sysobj, s.pos, temperature=s.temperature, friction=s.friction,
                          step_size=s.dt, seed=1000 + k, n_steps=10 ** 12)
              for k, (sysobj, s) in enumerate(zip(systems, specs))]
+    # the autotuner's trial launches are real steps of the same systems and
+    # serve as part of the warm-up; --threads fixes the shape instead
+    tuned = None
+    if args.threads:
+        batch.set_threads(args.threads)
+    else:
+        tuned = batch.autotune(steps_per_trial=K)
     for _ in range(args.warmup):
         batch.run(K, sync=True)
 
@@ -251,6 +256,8 @@ def run_ours(args, rank, world):
                                f"[{SIZE_LO},{SIZE_HI}], T~U[280,360] K, dt=10 fs",
                    "replicas": len(specs), "beads": beads, "md_steps_per_launch": K,
                    "parallelism": f"replicas x{world} (independent ensembles)",
+                   "launch_shape": {"threads_per_cta": batch.threads(), "autotuned": tuned is not None,
+                                    "trials_ms": [t["ms"] for t in tuned["trials"]] if tuned else None},
                    "l2": "flushed (256 MiB write) between timed launches"},
         "e2e": e2e, "gpu_launches": args.steps, "roofline": roof, "cpu_baseline": cpu,
         "plain_path": plain,

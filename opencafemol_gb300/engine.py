@@ -212,6 +212,31 @@ class Batch:
     def set_list_smem(self, kib: int) -> None:
         check(lib.ocm_batch_set_list_smem(self._h, int(kib)))
 
+    DEFAULT_TUNE_CANDIDATES = ((512, 96), (1024, 96), (512, -1), (1024, -1), (256, 96))
+
+    def autotune(self, steps_per_trial: int = 50, candidates=DEFAULT_TUNE_CANDIDATES) -> dict:
+        """Pick the launch shape (threads per CTA, list shared memory in KiB)
+        for the systems resident now.
+
+        Every candidate runs two real launches of ``steps_per_trial`` steps
+        (the first absorbs the set-up of that shape); the second is timed
+        with CUDA events and the fastest shape is kept.  Trajectories do not
+        depend on the shape, so the trials are ordinary simulation progress:
+        the resident systems advance by 2 * steps_per_trial steps per
+        candidate (systems with fewer steps left finish early)."""
+        trials = []
+        for th, kib in candidates:
+            self.set_threads(th)
+            self.set_list_smem(kib)
+            self.run(steps_per_trial, sync=True)
+            self.run(steps_per_trial, sync=True)
+            trials.append((self.last_run_ms(), th, kib))
+        ms, th, kib = min(trials)
+        self.set_threads(th)
+        self.set_list_smem(kib)
+        return {"threads": th, "list_smem_kib": kib, "ms_per_launch": ms,
+                "trials": [{"threads": t, "list_smem_kib": k, "ms": m} for m, t, k in trials]}
+
     def threads(self) -> int:
         t = C.c_int32()
         check(lib.ocm_batch_get_threads(self._h, C.byref(t)))

@@ -148,3 +148,24 @@ def test_oversize_system_rejected(gpu):
     with pytest.raises(gpu.OCMError) as ei:
         b.admit(synth.build_system(s), s.pos, n_steps=1)
     assert ei.value.code == 3
+
+
+def test_autotune_keeps_results(gpu):
+    """The autotuner times real launches under each launch shape and keeps
+    the fastest; the trajectory equals an untuned run of the same steps."""
+    from opencafemol_gb300 import synth
+    specs = _systems([60, 333, 777], seed0=950)
+    runs = []
+    for tune in (True, False):
+        b = gpu.Batch(max_systems=3, max_total_beads=1300, max_beads_per_system=800)
+        slots = [b.admit(synth.build_system(s), s.pos, seed=5 + k, n_steps=10 ** 6) for k, s in enumerate(specs)]
+        cands = ((512, 96), (1024, -1), (256, 48))
+        if tune:
+            res = b.autotune(steps_per_trial=20, candidates=cands)
+            assert (res["threads"], res["list_smem_kib"]) in cands and len(res["trials"]) == 3
+            assert b.threads() == res["threads"]
+        else:
+            b.run(2 * 20 * len(cands), sync=True)
+        runs.append([b.positions(k) for k in slots])
+    for xa, xb in zip(*runs):
+        assert np.array_equal(xa, xb)
