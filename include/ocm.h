@@ -118,6 +118,19 @@ int ocm_add_harmonic_bond(ocm_system* sys, int64_t n, const int64_t* indices,
 int ocm_add_go_contact(ocm_system* sys, int64_t n, const int64_t* indices,
                        const double* ks, const double* r0s, int use_periodic,
                        int* group_out);
+/* GaussianBondForceFieldGenerator(indices, ks, v0s, sigmas, use_periodic)
+ * (GaussianBondForceFieldGenerator.hpp:22-48, .cpp:3-23): the AICG2+
+ * k exp(-(r - v0)^2 / (2 sigma^2)); ks in kJ/mol, v0s and sigmas in nm. */
+int ocm_add_gaussian_bond(ocm_system* sys, int64_t n, const int64_t* indices, const double* ks,
+                          const double* v0s, const double* sigmas, int use_periodic,
+                          int* group_out);
+/* GaussianDihedralForceFieldGenerator(indices, ks, theta0s, sigmas, use_periodic)
+ * (GaussianDihedralForceFieldGenerator.hpp:22-50, .cpp:3-27): the AICG2+
+ * k exp(-dphi^2 / (2 sigma^2)), dphi = phi - theta0 wrapped to [-pi, pi);
+ * theta0s and sigmas in radians. */
+int ocm_add_gaussian_dihedral(ocm_system* sys, int64_t n, const int64_t* indices,
+                              const double* ks, const double* theta0s, const double* sigmas,
+                              int use_periodic, int* group_out);
 /* FlexibleLocalAngleForceFieldGenerator(indices, ks, spline_table, aa_name,
  * use_periodic) with the default theta range
  * (FlexibleLocalAngleForceFieldGenerator.hpp:21-47, .cpp:3-68). */

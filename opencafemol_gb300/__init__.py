@@ -1,14 +1,16 @@
 """GB300-native force-and-integrate engine for OpenCafeMol's coarse-grained
 protein force field (harmonic bonds, Go 10-12 contacts, flexible-local
-angles and dihedrals, excluded volume, Debye-Hueckel, HPS Lennard-Jones)
-with a Langevin integrator, behind the C ABI in include/ocm.h.
+angles and dihedrals, AICG2+ Gaussian bonds and dihedrals, excluded volume,
+Debye-Hueckel, HPS Lennard-Jones) with a Langevin integrator, behind the C
+ABI in include/ocm.h.
 """
 from ._lib import LIB_PATH, OCMError, device_count, lib
 from .engine import ALL_GROUPS, Batch, Context
 from .forcefield import (AMINO_ACIDS, DebyeHuckelForceFieldGenerator,
                          ExcludedVolumeForceFieldGenerator,
                          FlexibleLocalAngleForceFieldGenerator,
-                         FlexibleLocalDihedralForceFieldGenerator, GoContactForceFieldGenerator,
+                         FlexibleLocalDihedralForceFieldGenerator, GaussianBondForceFieldGenerator,
+                         GaussianDihedralForceFieldGenerator, GoContactForceFieldGenerator,
                          HarmonicBondForceFieldGenerator, LangevinIntegrator,
                          LangevinIntegratorGenerator, LennardJonesAttractiveForceFieldGenerator,
                          LennardJonesRepulsiveForceFieldGenerator, System, SystemGenerator,
@@ -19,6 +21,7 @@ __all__ = [
     "LIB_PATH", "OCMError", "device_count", "lib", "ALL_GROUPS", "Batch", "Context",
     "AMINO_ACIDS", "DebyeHuckelForceFieldGenerator", "ExcludedVolumeForceFieldGenerator",
     "FlexibleLocalAngleForceFieldGenerator", "FlexibleLocalDihedralForceFieldGenerator",
+    "GaussianBondForceFieldGenerator", "GaussianDihedralForceFieldGenerator",
     "GoContactForceFieldGenerator", "HarmonicBondForceFieldGenerator", "LangevinIntegrator",
     "LangevinIntegratorGenerator", "LennardJonesAttractiveForceFieldGenerator",
     "LennardJonesRepulsiveForceFieldGenerator", "System", "SystemGenerator", "Topology",

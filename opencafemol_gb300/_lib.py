@@ -65,6 +65,8 @@ SIGNATURES = {
     "ocm_system_describe": (C.c_int, [_P, C.c_char_p, C.c_int64, _I64P]),
     "ocm_add_harmonic_bond": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP, C.c_int, _I32P]),
     "ocm_add_go_contact": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP, C.c_int, _I32P]),
+    "ocm_add_gaussian_bond": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP, _DP, C.c_int, _I32P]),
+    "ocm_add_gaussian_dihedral": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP, _DP, C.c_int, _I32P]),
     "ocm_add_flexible_local_angle": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP, _CP, C.c_int, _I32P]),
     "ocm_add_flexible_local_dihedral": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP, _CP, C.c_int, _I32P]),
     "ocm_add_excluded_volume": (C.c_int, [_P, C.c_double, C.c_double, _DP, C.c_int64, _I64P, C.c_int,

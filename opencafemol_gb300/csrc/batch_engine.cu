@@ -443,6 +443,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         const uint2* aij = reinterpret_cast<const uint2*>(bsrc + R.ra_ij);
         const float* ak = reinterpret_cast<const float*>(bsrc + R.ra_k);
         const uint4* drec = reinterpret_cast<const uint4*>(bsrc + R.rd);
+        const float2* gdp = reinterpret_cast<const float2*>(bsrc + R.rgd);
         const FlaTable* fla = reinterpret_cast<const FlaTable*>(bsrc + R.rfla);
         const FldTable* fld = reinterpret_cast<const FldTable*>(bsrc + R.rfld);
         uint16_t* slist = reinterpret_cast<uint16_t*>(smem + off);
@@ -611,22 +612,31 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                 const int n_ad = n_dih + n_angles, n_all = n_ad + n_bonds;
                 const bool fld_on = (slots_en & (1u << kSlotFLD)) != 0;
                 const bool fla_on = (slots_en & (1u << kSlotFLA)) != 0;
+                const bool gd_on = (slots_en & (1u << kSlotGD)) != 0;
                 for (int t = tid; t < n_all; t += THREADS) {
                     if (t < n_dih) {
-                        if (!fld_on) continue;
                         const uint4 qd = drec[t];
-                        const int qi = qd.x & 0xFFFF, qj = qd.x >> 16, qk = qd.y & 0xFFFF, ql = qd.y >> 16;
+                        const bool gauss = (qd.x >> 31) != 0;
+                        if (!(gauss ? gd_on : fld_on)) continue;
+                        const int qi = qd.x & 0xFFFF, qj = (qd.x >> 16) & 0x7FFF, qk = qd.y & 0xFFFF,
+                                  ql = qd.y >> 16;
                         const float3 F = ffsep(sx, sxl, ns, qj, qi);
                         const float3 G = ffsep(sx, sxl, ns, qk, qj);
                         const float3 H = ffsep(sx, sxl, ns, qk, ql);
                         float3 f1, f2, f3, f4;
                         float en;
-                        fld_forces(F, G, H, __uint_as_float(qd.w), fld[qd.z], f1, f2, f3, f4, en);
+                        if (gauss) {
+                            const float2 gp = gdp[qd.z];
+                            gauss_dihedral_forces(F, G, H, __uint_as_float(qd.w), gp.x, gp.y, f1, f2, f3, f4,
+                                                  en);
+                        } else {
+                            fld_forces(F, G, H, __uint_as_float(qd.w), fld[qd.z], f1, f2, f3, f4, en);
+                        }
                         sadd(sF, ns, qi, f1);
                         sadd(sF, ns, qj, f2);
                         sadd(sF, ns, qk, f3);
                         sadd(sF, ns, ql, f4);
-                        if (ENERGY) eacc[kSlotFLD] += en;
+                        if (ENERGY) eacc[gauss ? kSlotGD : kSlotFLD] += en;
                     } else if (t < n_ad) {
                         if (!fla_on) continue;
                         const int b = t - n_dih;
@@ -644,17 +654,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                     } else {
                         const int b = t - n_ad;
                         const uint32_t ij = bij[b];
-                        const int kind = (ij >> 31) ? kBondGo : kBondHarmonic;
-                        const int sl = kind == kBondHarmonic ? kSlotHB : kSlotGO;
+                        const int kind = (int)(ij >> 30);
+                        const int sl = kind == kBondHarmonic ? kSlotHB : (kind == kBondGo ? kSlotGO : kSlotGB);
                         if (!(slots_en & (1u << sl))) continue;
-                        const int bi = ij & 0xFFFF, bj = (ij >> 16) & 0x7FFF;
+                        const int bi = ij & 0xFFFF, bj = (ij >> 16) & 0x3FFF;
                         const float4 bp = bpar[b];
                         float3 dh, dl;
                         ff_sep(sx[bi], lo3(sxl, ns, bi), sx[bj], lo3(sxl, ns, bj), dh, dl);
                         const float3 d = make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
                         const float delta = ff_bond_delta(dh, dl, bp.z, bp.w);
                         float en;
-                        const float sc = bond_scalar(kind, norm2(d), delta, bp.x, bp.y, en);
+                        const float sc = bond_scalar(kind, norm2(d), delta, bp.x, bp.y, bp.z, en);
                         sadd(sF, ns, bi, make_float3(-sc * d.x, -sc * d.y, -sc * d.z));
                         sadd(sF, ns, bj, make_float3(sc * d.x, sc * d.y, sc * d.z));
                         if (ENERGY) eacc[sl] += en;
@@ -813,7 +823,7 @@ int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 struct BlobLayout {
     int64_t size = 0;
     int off_p0, off_p1, off_lab, off_invm, off_tmask, off_masks, off_ex_start, off_ex;
-    int off_bonded, bonded_bytes, rb_p, rb_ij, ra_ij, ra_k, rd, rfla, rfld;
+    int off_bonded, bonded_bytes, rb_p, rb_ij, ra_ij, ra_k, rd, rgd, rfla, rfld;
     int n_tiles, n_masks;
 };
 
@@ -843,6 +853,9 @@ BlobLayout blob_layout(const CompiledSystem& c, int n_masks) {
     L.ra_ij = take(8 * na) - L.off_bonded;
     L.ra_k = take(4 * na) - L.off_bonded;
     L.rd = take(16 * nd) - L.off_bonded;
+    int64_t ngd = 0;
+    for (const auto& t : c.dihedrals) ngd += t.kind == kDihGauss ? 1 : 0;
+    L.rgd = take(8 * ngd) - L.off_bonded;
     L.rfla = take((int64_t)sizeof(FlaTable) * c.fla.size()) - L.off_bonded;
     L.rfld = take((int64_t)sizeof(FldTable) * c.fld.size()) - L.off_bonded;
     L.bonded_bytes = (int)(o - L.off_bonded);
@@ -1084,7 +1097,7 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
         for (size_t b = 0; b < c.bonds.size(); ++b) {
             const BondTerm& t = c.bonds[b];
             bp[b] = make_float4(t.p0, t.p1, t.r0sq_hi, t.r0sq_lo);
-            bij[b] = (uint32_t)t.i | ((uint32_t)t.j << 16) | (t.kind == kBondGo ? 0x80000000u : 0u);
+            bij[b] = (uint32_t)t.i | ((uint32_t)t.j << 16) | ((uint32_t)t.kind << 30);
         }
         std::vector<uint2> aij(c.angles.size());
         std::vector<float> ak(c.angles.size());
@@ -1093,13 +1106,22 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
             aij[b] = make_uint2((uint32_t)t.i | ((uint32_t)t.j << 16), (uint32_t)t.k | ((uint32_t)t.table << 16));
             ak[b] = t.kk;
         }
+        // dihedral record: FLD table index, or (bit 31 of .x set) the index
+        // of the Gaussian dihedral's (theta0, 1 / (2 sigma^2))
         std::vector<uint4> dr(c.dihedrals.size());
+        std::vector<float2> gd;
         for (size_t b = 0; b < c.dihedrals.size(); ++b) {
             const DihedralTerm& t = c.dihedrals[b];
             uint32_t kb;
             std::memcpy(&kb, &t.kk, 4);
-            dr[b] = make_uint4((uint32_t)t.i | ((uint32_t)t.j << 16), (uint32_t)t.k | ((uint32_t)t.l << 16),
-                               (uint32_t)t.table, kb);
+            const bool gauss = t.kind == kDihGauss;
+            uint32_t third = (uint32_t)t.table;
+            if (gauss) {
+                third = (uint32_t)gd.size();
+                gd.push_back(make_float2(t.theta0, t.inv2s2));
+            }
+            dr[b] = make_uint4((uint32_t)t.i | ((uint32_t)t.j << 16) | (gauss ? 0x80000000u : 0u),
+                               (uint32_t)t.k | ((uint32_t)t.l << 16), third, kb);
         }
         const int ob = L.off_bonded;
         put(ob + L.rb_p, bp.data(), 16 * bp.size());
@@ -1107,6 +1129,7 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
         put(ob + L.ra_ij, aij.data(), 8 * aij.size());
         put(ob + L.ra_k, ak.data(), 4 * ak.size());
         put(ob + L.rd, dr.data(), 16 * dr.size());
+        put(ob + L.rgd, gd.data(), 8 * gd.size());
         put(ob + L.rfla, c.fla.data(), sizeof(FlaTable) * c.fla.size());
         put(ob + L.rfld, c.fld.data(), sizeof(FldTable) * c.fld.size());
     }
@@ -1131,7 +1154,7 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     R.n_masks = L.n_masks;
     R.off_p0 = L.off_p0; R.off_p1 = L.off_p1; R.off_lab = L.off_lab; R.off_invm = L.off_invm;
     R.off_bonded = L.off_bonded; R.bonded_bytes = L.bonded_bytes;
-    R.rb_p = L.rb_p; R.rb_ij = L.rb_ij; R.ra_ij = L.ra_ij; R.ra_k = L.ra_k; R.rd = L.rd;
+    R.rb_p = L.rb_p; R.rb_ij = L.rb_ij; R.ra_ij = L.ra_ij; R.ra_k = L.ra_k; R.rd = L.rd; R.rgd = L.rgd;
     R.rfla = L.rfla; R.rfld = L.rfld;
     R.off_tmask = L.off_tmask; R.off_masks = L.off_masks;
     R.off_ex_start = L.off_ex_start; R.off_ex = L.off_ex;

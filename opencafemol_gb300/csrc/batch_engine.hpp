@@ -27,7 +27,7 @@ struct BatchSys {
     // [off_bonded, off_bonded + bonded_bytes) that the kernel stages into
     // shared memory when it fits; section offsets are relative to it.
     int off_bonded, bonded_bytes;
-    int rb_p, rb_ij, ra_ij, ra_k, rd, rfla, rfld;
+    int rb_p, rb_ij, ra_ij, ra_k, rd, rgd, rfla, rfld;
     int off_tmask, off_masks;
     int off_ex_start, off_ex;                // exclusion CSR (j | bits << 24)
     int maxn;              // neighbour-list entries per bead

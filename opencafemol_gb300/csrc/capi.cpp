@@ -261,6 +261,37 @@ int ocm_add_go_contact(ocm_system* s, int64_t n, const int64_t* idx, const doubl
         if (group_out) *group_out = grp;
     });
 }
+int ocm_add_gaussian_bond(ocm_system* s, int64_t n, const int64_t* idx, const double* ks,
+                          const double* v0s, const double* sigmas, int use_periodic, int* group_out) {
+    return guard([&] {
+        need(s, "system");
+        auto g = std::make_unique<ocm::GaussianBondForceFieldGenerator>(
+            pairs_of(idx, n), copy_vec(ks, n, "ks"), copy_vec(v0s, n, "v0s"),
+            copy_vec(sigmas, n, "sigmas"), use_periodic != 0);
+        const int grp = s->g.add_ff_generator(std::move(g));
+        if (group_out) *group_out = grp;
+    });
+}
+int ocm_add_gaussian_dihedral(ocm_system* s, int64_t n, const int64_t* idx, const double* ks,
+                              const double* theta0s, const double* sigmas, int use_periodic,
+                              int* group_out) {
+    return guard([&] {
+        need(s, "system");
+        if (n < 0) throw ocm::Error(1, "[error] negative count");
+        if (n) need(idx, "indices");
+        std::vector<std::array<int64_t, 4>> v;
+        for (int64_t k = 0; k < n; ++k) {
+            for (int c = 0; c < 4; ++c)
+                if (idx[4 * k + c] < 0) throw ocm::Error(1, "[error] negative index");
+            v.push_back({idx[4 * k], idx[4 * k + 1], idx[4 * k + 2], idx[4 * k + 3]});
+        }
+        auto g = std::make_unique<ocm::GaussianDihedralForceFieldGenerator>(
+            std::move(v), copy_vec(ks, n, "ks"), copy_vec(theta0s, n, "theta0s"),
+            copy_vec(sigmas, n, "sigmas"), use_periodic != 0);
+        const int grp = s->g.add_ff_generator(std::move(g));
+        if (group_out) *group_out = grp;
+    });
+}
 int ocm_add_flexible_local_angle(ocm_system* s, int64_t n, const int64_t* idx, const double* ks,
                                  const double* table, const char* aa, int use_periodic,
                                  int* group_out) {

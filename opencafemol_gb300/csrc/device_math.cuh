@@ -145,16 +145,26 @@ __device__ __forceinline__ float pair_scalar(float r2, float4 pi, float4 pj, flo
 // ---------------------------------------------------------------------------
 // Harmonic bond 1/2 k (r - r0)^2 (HarmonicBondForceFieldGenerator.cpp:5-10).
 // Go 10-12: k (5 (r0/r)^12 - 6 (r0/r)^10) (GoContactForceFieldGenerator.cpp:5-7).
-// `delta` = r^2 - r0^2 evaluated without cancellation by the caller: both
-// forces are proportional to it near the native length, where an FP32
-// r - r0 would lose all its digits.  Returns s with F_a = s * (x_a - x_b).
+// Gaussian bond: k exp(-(r - v0)^2 / (2 sigma^2))
+// (GaussianBondForceFieldGenerator.cpp:5-7).
+// `delta` = r^2 - r0^2 (v0^2 for the Gaussian) evaluated without
+// cancellation by the caller: all three forces are proportional to it near
+// the centre, where an FP32 r - r0 would lose its digits.  For a Gaussian
+// bond p1 = 1 / (2 sigma^2) and p2 = the high part of v0^2 (v0 enters only
+// the r + v0 denominator).  Returns s with F_a = s * (x_a - x_b).
 __device__ __forceinline__ float bond_scalar(int kind, float r2, float delta, float p0, float p1,
-                                             float& energy) {
+                                             float p2, float& energy) {
     if (kind == kBondHarmonic) {  // p0 = r0, p1 = k
         const float r = sqrtf(r2);
         const float dr = delta / (r + p0);
         energy = 0.5f * p1 * dr * dr;
         return -p1 * dr / r;
+    } else if (kind == kBondGauss) {  // p0 = k, p1 = 1 / (2 sigma^2), p2 ~ v0^2
+        const float r = sqrtf(r2);
+        const float dr = delta / (r + sqrtf(p2));
+        const float e = p0 * expf(-dr * dr * p1);
+        energy = e;
+        return 2.f * p1 * dr * e / r;
     } else {  // Go: p0 = k, p1 = r0;  t^2 - 1 = -delta / r^2
         const float inv = 1.f / r2;
         const float t2 = p1 * p1 * inv;
@@ -237,32 +247,34 @@ __device__ __forceinline__ void fla_forces(float3 u, float3 v, float kk, const F
     f3 = make_float3(c3 * vn.x, c3 * vn.y, c3 * vn.z);
 }
 
-// Flexible-local dihedral (FlexibleLocalDihedralForceFieldGenerator.cpp:28-36):
-// E = k (c - Emin + sum_n a_n cos(n phi) + b_n sin(n phi)), phi in the IUPAC
-// convention.  F = x1 - x2, G = x2 - x3, H = x4 - x3.
-__device__ __forceinline__ void fld_forces(float3 F, float3 G, float3 H, float kk,
-                                           const FldTable& t, float3& f1, float3& f2,
-                                           float3& f3, float3& f4, float& energy) {
-    const float3 A = make_float3(F.y * G.z - F.z * G.y, F.z * G.x - F.x * G.z, F.x * G.y - F.y * G.x);
-    const float3 B = make_float3(H.y * G.z - H.z * G.y, H.z * G.x - H.x * G.z, H.x * G.y - H.y * G.x);
-    const float AA = fmaxf(norm2(A), 1e-30f);
-    const float BB = fmaxf(norm2(B), 1e-30f);
-    const float GG = norm2(G);
-    const float Gl = sqrtf(GG);
-    const float inv_ab = rsqrtf(AA * BB);
-    const float c1 = (A.x * B.x + A.y * B.y + A.z * B.z) * inv_ab;
-    const float s1 = -Gl * (F.x * B.x + F.y * B.y + F.z * B.z) * inv_ab;
-    // multiple angles
-    const float c2 = c1 * c1 - s1 * s1, s2 = 2.f * s1 * c1;
-    const float c3 = c1 * c2 - s1 * s2, s3 = s1 * c2 + c1 * s2;
-    energy = kk * (t.c[0] - t.emin + t.c[1] * c1 + t.c[2] * s1 + t.c[3] * c2 + t.c[4] * s2 +
-                   t.c[5] * c3 + t.c[6] * s3);
-    const float dE = kk * (-t.c[1] * s1 + t.c[2] * c1 - 2.f * t.c[3] * s2 + 2.f * t.c[4] * c2 -
-                           3.f * t.c[5] * s3 + 3.f * t.c[6] * c3);
-    // Blondel-Karplus gradients.
-    const float ga = Gl / AA, gb = Gl / BB;
-    const float fg = (F.x * G.x + F.y * G.y + F.z * G.z) / (AA * Gl);
-    const float hg = (H.x * G.x + H.y * G.y + H.z * G.z) / (BB * Gl);
+// Torsion geometry of (x1, x2, x3, x4) from F = x1 - x2, G = x2 - x3,
+// H = x4 - x3: cos and sin of the IUPAC dihedral angle (OpenMM's torsion
+// convention) without an arc tangent, and the Blondel-Karplus derivatives
+// of the angle with respect to the four positions.
+struct Torsion {
+    float3 A, B;
+    float AA, BB, Gl, c, s;
+};
+__device__ __forceinline__ Torsion torsion_geometry(float3 F, float3 G, float3 H) {
+    Torsion t;
+    t.A = make_float3(F.y * G.z - F.z * G.y, F.z * G.x - F.x * G.z, F.x * G.y - F.y * G.x);
+    t.B = make_float3(H.y * G.z - H.z * G.y, H.z * G.x - H.x * G.z, H.x * G.y - H.y * G.x);
+    t.AA = fmaxf(norm2(t.A), 1e-30f);
+    t.BB = fmaxf(norm2(t.B), 1e-30f);
+    t.Gl = sqrtf(norm2(G));
+    const float inv_ab = rsqrtf(t.AA * t.BB);
+    t.c = (t.A.x * t.B.x + t.A.y * t.B.y + t.A.z * t.B.z) * inv_ab;
+    t.s = -t.Gl * (F.x * t.B.x + F.y * t.B.y + F.z * t.B.z) * inv_ab;
+    return t;
+}
+// Forces f_a = -dE/dphi * dphi/dx_a.
+__device__ __forceinline__ void torsion_forces(const Torsion& t, float3 F, float3 G, float3 H,
+                                               float dE, float3& f1, float3& f2, float3& f3,
+                                               float3& f4) {
+    const float3 A = t.A, B = t.B;
+    const float ga = t.Gl / t.AA, gb = t.Gl / t.BB;
+    const float fg = (F.x * G.x + F.y * G.y + F.z * G.z) / (t.AA * t.Gl);
+    const float hg = (H.x * G.x + H.y * G.y + H.z * G.z) / (t.BB * t.Gl);
     // dphi/dx1 = -ga A ; dphi/dx4 = gb B
     const float3 d1 = make_float3(-ga * A.x, -ga * A.y, -ga * A.z);
     const float3 d4 = make_float3(gb * B.x, gb * B.y, gb * B.z);
@@ -275,6 +287,40 @@ __device__ __forceinline__ void fld_forces(float3 F, float3 G, float3 H, float k
     f2 = make_float3(-dE * d2.x, -dE * d2.y, -dE * d2.z);
     f3 = make_float3(-dE * d3.x, -dE * d3.y, -dE * d3.z);
     f4 = make_float3(-dE * d4.x, -dE * d4.y, -dE * d4.z);
+}
+
+// Flexible-local dihedral (FlexibleLocalDihedralForceFieldGenerator.cpp:7-59):
+// E = k (c - Emin + sum_n a_n cos(n phi) + b_n sin(n phi)), n = 1..3, with
+// the multiple angles from cos/sin recurrences.
+__device__ __forceinline__ void fld_forces(float3 F, float3 G, float3 H, float kk,
+                                           const FldTable& t, float3& f1, float3& f2,
+                                           float3& f3, float3& f4, float& energy) {
+    const Torsion g = torsion_geometry(F, G, H);
+    const float c1 = g.c, s1 = g.s;
+    const float c2 = c1 * c1 - s1 * s1, s2 = 2.f * s1 * c1;
+    const float c3 = c1 * c2 - s1 * s2, s3 = s1 * c2 + c1 * s2;
+    energy = kk * (t.c[0] - t.emin + t.c[1] * c1 + t.c[2] * s1 + t.c[3] * c2 + t.c[4] * s2 +
+                   t.c[5] * c3 + t.c[6] * s3);
+    const float dE = kk * (-t.c[1] * s1 + t.c[2] * c1 - 2.f * t.c[3] * s2 + 2.f * t.c[4] * c2 -
+                           3.f * t.c[5] * s3 + 3.f * t.c[6] * c3);
+    torsion_forces(g, F, G, H, dE, f1, f2, f3, f4);
+}
+
+// Gaussian dihedral (GaussianDihedralForceFieldGenerator.cpp:5-12):
+// E = k exp(-dp^2 / (2 sigma^2)), dp = d - floor((d + pi) / (2 pi)) 2 pi,
+// d = phi - theta0; inv2s2 = 1 / (2 sigma^2).
+__device__ __forceinline__ void gauss_dihedral_forces(float3 F, float3 G, float3 H, float kk,
+                                                      float theta0, float inv2s2, float3& f1,
+                                                      float3& f2, float3& f3, float3& f4,
+                                                      float& energy) {
+    const Torsion g = torsion_geometry(F, G, H);
+    const float phi = atan2f(g.s, g.c);
+    const float two_pi = 6.2831853071795865f;
+    float d = phi - theta0;
+    d -= floorf((d + 3.1415926535897932f) * (1.f / two_pi)) * two_pi;
+    const float e = kk * expf(-d * d * inv2s2);
+    energy = e;
+    torsion_forces(g, F, G, H, -2.f * inv2s2 * d * e, f1, f2, f3, f4);
 }
 
 // ---------------------------------------------------------------------------

@@ -26,11 +26,17 @@ enum EnergySlot {
     kSlotGO = 5,
     kSlotFLA = 6,
     kSlotFLD = 7,
-    kNumSlots = 8
+    kSlotGB = 8,   // Gaussian bond (AICG2+)
+    kSlotGD = 9,   // Gaussian dihedral (AICG2+)
+    kNumSlots = 10
 };
 
 constexpr int kBondHarmonic = 0;
 constexpr int kBondGo = 1;
+constexpr int kBondGauss = 2;
+
+constexpr int kDihFLD = 0;
+constexpr int kDihGauss = 1;
 
 // Philox4x32-10 constants (Salmon et al. 2011).
 constexpr uint32_t kPhiloxM0 = 0xD2511F53u;
@@ -67,13 +73,13 @@ struct FldTable {
     float emin;
 };
 
-// Explicit bond-like term (harmonic bond or Go contact).
+// Explicit bond-like term (harmonic bond, Go contact or Gaussian bond).
 struct BondTerm {
     int32_t i, j;
-    int32_t kind;      // kBondHarmonic / kBondGo
+    int32_t kind;      // kBondHarmonic / kBondGo / kBondGauss
     int32_t periodic;  // minimum image when nonzero
-    float p0, p1;      // (r0, k) harmonic; (k, r0) Go
-    float r0sq_hi, r0sq_lo;  // r0^2 as an unevaluated float sum
+    float p0, p1;      // (r0, k) harmonic; (k, r0) Go; (k, 1 / (2 sigma^2)) Gaussian
+    float r0sq_hi, r0sq_lo;  // r0^2 (v0^2 for the Gaussian) as an unevaluated float sum
 };
 struct AngleTerm {
     int32_t i, j, k, table;
@@ -82,9 +88,10 @@ struct AngleTerm {
 };
 struct DihedralTerm {
     int32_t i, j, k, l;
-    int32_t table, periodic;
+    int32_t table, periodic;  // table: FLD Fourier table (kDihFLD)
     float kk;
-    int32_t pad_;
+    int32_t kind;             // kDihFLD / kDihGauss
+    float theta0, inv2s2;     // Gaussian: centre (rad) and 1 / (2 sigma^2)
 };
 
 // Langevin constants of one system (OpenMM LangevinIntegrator).

@@ -198,6 +198,52 @@ GeneratedForce GoContactForceFieldGenerator::generate() const {
     return f;
 }
 
+GaussianBondForceFieldGenerator::GaussianBondForceFieldGenerator(
+    std::vector<std::pair<int64_t, int64_t>> idx, std::vector<double> ks, std::vector<double> v0s,
+    std::vector<double> sigmas, bool use_periodic)
+    : idx_(std::move(idx)), ks_(std::move(ks)), v0s_(std::move(v0s)), sigmas_(std::move(sigmas)),
+      periodic_(use_periodic) {
+    if (!(idx_.size() == v0s_.size() && v0s_.size() == ks_.size() && ks_.size() == sigmas_.size()))
+        throw Error(1, "[error] GaussianBondForceFieldGenerator: parameter number of indices_vec (" +
+                           sz(idx_.size()) + "), k (" + sz(ks_.size()) + "), v0 (" + sz(v0s_.size()) +
+                           ") and sigmas (" + sz(sigmas_.size()) +
+                           ") is not matched.The number of these parameters must be same.");
+}
+GeneratedForce GaussianBondForceFieldGenerator::generate() const {
+    GeneratedForce f;
+    f.kind = ForceKind::GaussianBond;
+    f.name = name();
+    f.periodic = periodic_;
+    for (std::size_t i = 0; i < idx_.size(); ++i) {
+        f.idx.push_back({idx_[i].first, idx_[i].second, -1, -1});
+        f.par.push_back({ks_[i], v0s_[i], sigmas_[i]});
+    }
+    return f;
+}
+
+GaussianDihedralForceFieldGenerator::GaussianDihedralForceFieldGenerator(
+    std::vector<std::array<int64_t, 4>> idx, std::vector<double> ks, std::vector<double> theta0s,
+    std::vector<double> sigmas, bool use_periodic)
+    : idx_(std::move(idx)), ks_(std::move(ks)), theta0s_(std::move(theta0s)),
+      sigmas_(std::move(sigmas)), periodic_(use_periodic) {
+    if (!(idx_.size() == ks_.size() && idx_.size() == theta0s_.size() && idx_.size() == sigmas_.size()))
+        throw Error(1, "[error] GaussianDihedralForceFieldGenerator : parameter number of indices_vec (" +
+                           sz(idx_.size()) + "), k (" + sz(ks_.size()) + "), theta0 (" +
+                           sz(theta0s_.size()) + ") and simga (" + sz(sigmas_.size()) +
+                           " is not matched.The number of these parameters must be same.");
+}
+GeneratedForce GaussianDihedralForceFieldGenerator::generate() const {
+    GeneratedForce f;
+    f.kind = ForceKind::GaussianDihedral;
+    f.name = name();
+    f.periodic = periodic_;
+    for (std::size_t i = 0; i < idx_.size(); ++i) {
+        f.idx.push_back(idx_[i]);
+        f.par.push_back({ks_[i], theta0s_[i], sigmas_[i]});
+    }
+    return f;
+}
+
 FlexibleLocalAngleForceFieldGenerator::FlexibleLocalAngleForceFieldGenerator(
     std::vector<std::array<int64_t, 3>> idx, std::vector<double> ks,
     const std::array<double, 10>& spline_table, const std::string& aa_name, bool use_periodic,
@@ -595,6 +641,8 @@ CompiledSystem compile_system(const SystemDesc& d) {
             case ForceKind::GoContact: slot = kSlotGO; break;
             case ForceKind::FlexibleLocalAngle: slot = kSlotFLA; break;
             case ForceKind::FlexibleLocalDihedral: slot = kSlotFLD; break;
+            case ForceKind::GaussianBond: slot = kSlotGB; break;
+            case ForceKind::GaussianDihedral: slot = kSlotGD; break;
         }
         if (term >= 0) {
             const int bit = 1 << term;
@@ -699,6 +747,38 @@ CompiledSystem compile_system(const SystemDesc& d) {
                 if (b.i < 0 || b.j < 0) throw Error(1, "[error] negative particle index");
                 c.bonds.push_back(b);
             }
+        } else if (f.kind == ForceKind::GaussianBond) {
+            for (std::size_t t = 0; t < f.idx.size(); ++t) {
+                BondTerm b{};
+                b.i = (int32_t)f.idx[t][0];
+                b.j = (int32_t)f.idx[t][1];
+                b.kind = kBondGauss;
+                b.periodic = f.periodic ? 1 : 0;
+                b.p0 = (float)f.par[t][0];                                  // k
+                b.p1 = (float)(1.0 / (2.0 * f.par[t][2] * f.par[t][2]));  // 1 / (2 sigma^2)
+                const double v0sq = f.par[t][1] * f.par[t][1];
+                b.r0sq_hi = (float)v0sq;
+                b.r0sq_lo = (float)(v0sq - (double)b.r0sq_hi);
+                if (b.i < 0 || b.j < 0) throw Error(1, "[error] negative particle index");
+                c.bonds.push_back(b);
+            }
+        } else if (f.kind == ForceKind::GaussianDihedral) {
+            for (std::size_t a = 0; a < f.idx.size(); ++a) {
+                DihedralTerm dt{};
+                dt.i = (int32_t)f.idx[a][0];
+                dt.j = (int32_t)f.idx[a][1];
+                dt.k = (int32_t)f.idx[a][2];
+                dt.l = (int32_t)f.idx[a][3];
+                if (dt.i < 0 || dt.j < 0 || dt.k < 0 || dt.l < 0)
+                    throw Error(1, "[error] negative particle index");
+                dt.kind = kDihGauss;
+                dt.table = -1;
+                dt.periodic = f.periodic ? 1 : 0;
+                dt.kk = (float)f.par[a][0];
+                dt.theta0 = (float)f.par[a][1];
+                dt.inv2s2 = (float)(1.0 / (2.0 * f.par[a][2] * f.par[a][2]));
+                c.dihedrals.push_back(dt);
+            }
         } else if (f.kind == ForceKind::FlexibleLocalAngle) {
             FlaTable t{};
             const double h = (f.theta_max - f.theta_min) / 9.0;
@@ -738,6 +818,7 @@ CompiledSystem compile_system(const SystemDesc& d) {
                 dt.l = (int32_t)f.idx[a][3];
                 if (dt.i < 0 || dt.j < 0 || dt.k < 0 || dt.l < 0)
                     throw Error(1, "[error] negative particle index");
+                dt.kind = kDihFLD;
                 dt.table = tid;
                 dt.periodic = f.periodic ? 1 : 0;
                 dt.kk = (float)f.par[a][0];

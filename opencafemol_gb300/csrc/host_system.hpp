@@ -86,7 +86,7 @@ GroupPairs extract_interaction_group(const std::vector<bool>& has_value,
 // ---------------------------------------------------------------------------
 enum class ForceKind { HarmonicBond, GoContact, FlexibleLocalAngle, FlexibleLocalDihedral,
                        ExcludedVolume, DebyeHuckel, LennardJonesRepulsive,
-                       LennardJonesAttractive };
+                       LennardJonesAttractive, GaussianBond, GaussianDihedral };
 
 struct GeneratedForce {
     ForceKind kind;
@@ -95,7 +95,7 @@ struct GeneratedForce {
     bool periodic = false;
     // explicit terms
     std::vector<std::array<int64_t, 4>> idx;
-    std::vector<std::array<double, 2>> par;
+    std::vector<std::array<double, 3>> par;
     // FlexibleLocalAngle
     std::array<double, 10> spline_y{};
     double theta_min = 0, theta_max = 0, min_energy = 0;
@@ -139,6 +139,36 @@ class GoContactForceFieldGenerator final : public ForceFieldGeneratorBase {
   private:
     std::vector<std::pair<int64_t, int64_t>> idx_;
     std::vector<double> ks_, r0s_;
+    bool periodic_;
+};
+
+// GaussianBondForceFieldGenerator (GaussianBondForceFieldGenerator.hpp:22-48,
+// .cpp:3-23): k exp(-(r - v0)^2 / (2 sigma^2)).
+class GaussianBondForceFieldGenerator final : public ForceFieldGeneratorBase {
+  public:
+    GaussianBondForceFieldGenerator(std::vector<std::pair<int64_t, int64_t>> idx,
+                                    std::vector<double> ks, std::vector<double> v0s,
+                                    std::vector<double> sigmas, bool use_periodic);
+    GeneratedForce generate() const override;
+    std::string name() const override { return "GaussianBond"; }
+  private:
+    std::vector<std::pair<int64_t, int64_t>> idx_;
+    std::vector<double> ks_, v0s_, sigmas_;
+    bool periodic_;
+};
+
+// GaussianDihedralForceFieldGenerator (GaussianDihedralForceFieldGenerator.hpp,
+// .cpp:3-27): k exp(-dphi^2 / (2 sigma^2)) with dphi wrapped to [-pi, pi).
+class GaussianDihedralForceFieldGenerator final : public ForceFieldGeneratorBase {
+  public:
+    GaussianDihedralForceFieldGenerator(std::vector<std::array<int64_t, 4>> idx,
+                                        std::vector<double> ks, std::vector<double> theta0s,
+                                        std::vector<double> sigmas, bool use_periodic);
+    GeneratedForce generate() const override;
+    std::string name() const override { return "GaussianDihedral"; }
+  private:
+    std::vector<std::array<int64_t, 4>> idx_;
+    std::vector<double> ks_, theta0s_, sigmas_;
     bool periodic_;
 };
 

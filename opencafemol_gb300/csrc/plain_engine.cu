@@ -462,12 +462,12 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
     }
     blk -= a.blocks_tiles;
     if (blk < a.blocks_bonds) {
-        // ---------------- harmonic bonds and Go contacts ----------------
+        // ------------ harmonic bonds, Go contacts, Gaussian bonds ------------
         const int t = blk * kForceThreads + threadIdx.x;
-        float eh = 0.f, eg = 0.f;
+        float eh = 0.f, eg = 0.f, eb = 0.f;
         if (t < a.n_bonds) {
             const BondTerm b = a.bonds[t];
-            const int slot = b.kind == kBondHarmonic ? kSlotHB : kSlotGO;
+            const int slot = b.kind == kBondHarmonic ? kSlotHB : (b.kind == kBondGo ? kSlotGO : kSlotGB);
             if (a.slots_enabled & (1u << slot)) {
                 double dx = a.x[b.j] - a.x[b.i], dy = a.y[b.j] - a.y[b.i], dz = a.z[b.j] - a.z[b.i];
                 if (b.periodic) {
@@ -479,18 +479,20 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                 const float delta = (float)(r2d - ((double)b.r0sq_hi + (double)b.r0sq_lo));
                 const float3 d = make_float3((float)dx, (float)dy, (float)dz);
                 float en;
-                const float s = bond_scalar(b.kind, norm2(d), delta, b.p0, b.p1, en);
+                const float s = bond_scalar(b.kind, norm2(d), delta, b.p0, b.p1, b.r0sq_hi, en);
                 add_force(a.F, a.n, b.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
                 add_force(a.F, a.n, b.j, make_float3(s * d.x, s * d.y, s * d.z));
                 if (b.kind == kBondHarmonic) eh = en;
-                else eg = en;
+                else if (b.kind == kBondGo) eg = en;
+                else eb = en;
             }
         }
         if (ENERGY) {
-            const double vh = warp_sum((double)eh), vg = warp_sum((double)eg);
+            const double vh = warp_sum((double)eh), vg = warp_sum((double)eg), vb = warp_sum((double)eb);
             if (lane == 0) {
                 if (vh != 0.0) atomicAdd(&a.energy[kSlotHB], vh);
                 if (vg != 0.0) atomicAdd(&a.energy[kSlotGO], vg);
+                if (vb != 0.0) atomicAdd(&a.energy[kSlotGB], vb);
             }
         }
         return;
@@ -518,22 +520,35 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
     blk -= a.blocks_angles;
     {
         const int t = blk * kForceThreads + threadIdx.x;
-        float en = 0.f;
-        if (t < a.n_dih && (a.slots_enabled & (1u << kSlotFLD))) {
+        float efld = 0.f, egd = 0.f;
+        if (t < a.n_dih) {
             const DihedralTerm q = a.dih[t];
-            const float3 F = bonded_sep(a, q.j, q.i, q.periodic);  // x1 - x2
-            const float3 G = bonded_sep(a, q.k, q.j, q.periodic);  // x2 - x3
-            const float3 H = bonded_sep(a, q.k, q.l, q.periodic);  // x4 - x3
-            float3 f1, f2, f3, f4;
-            fld_forces(F, G, H, q.kk, a.fld[q.table], f1, f2, f3, f4, en);
-            add_force(a.F, a.n, q.i, f1);
-            add_force(a.F, a.n, q.j, f2);
-            add_force(a.F, a.n, q.k, f3);
-            add_force(a.F, a.n, q.l, f4);
+            const int slot = q.kind == kDihFLD ? kSlotFLD : kSlotGD;
+            if (a.slots_enabled & (1u << slot)) {
+                const float3 F = bonded_sep(a, q.j, q.i, q.periodic);  // x1 - x2
+                const float3 G = bonded_sep(a, q.k, q.j, q.periodic);  // x2 - x3
+                const float3 H = bonded_sep(a, q.k, q.l, q.periodic);  // x4 - x3
+                float3 f1, f2, f3, f4;
+                float en;
+                if (q.kind == kDihFLD) {
+                    fld_forces(F, G, H, q.kk, a.fld[q.table], f1, f2, f3, f4, en);
+                    efld = en;
+                } else {
+                    gauss_dihedral_forces(F, G, H, q.kk, q.theta0, q.inv2s2, f1, f2, f3, f4, en);
+                    egd = en;
+                }
+                add_force(a.F, a.n, q.i, f1);
+                add_force(a.F, a.n, q.j, f2);
+                add_force(a.F, a.n, q.k, f3);
+                add_force(a.F, a.n, q.l, f4);
+            }
         }
         if (ENERGY) {
-            const double v = warp_sum((double)en);
-            if (lane == 0 && v != 0.0) atomicAdd(&a.energy[kSlotFLD], v);
+            const double v = warp_sum((double)efld), vg = warp_sum((double)egd);
+            if (lane == 0) {
+                if (v != 0.0) atomicAdd(&a.energy[kSlotFLD], v);
+                if (vg != 0.0) atomicAdd(&a.energy[kSlotGD], vg);
+            }
         }
     }
 }

@@ -21,6 +21,7 @@ from ._lib import (OCMError, as_f64, as_i32, as_i64, check, dptr, i32ptr, i64ptr
 
 __all__ = [
     "Topology", "HarmonicBondForceFieldGenerator", "GoContactForceFieldGenerator",
+    "GaussianBondForceFieldGenerator", "GaussianDihedralForceFieldGenerator",
     "FlexibleLocalAngleForceFieldGenerator", "FlexibleLocalDihedralForceFieldGenerator",
     "ExcludedVolumeForceFieldGenerator", "DebyeHuckelForceFieldGenerator",
     "LennardJonesRepulsiveForceFieldGenerator", "LennardJonesAttractiveForceFieldGenerator",
@@ -160,6 +161,55 @@ class GoContactForceFieldGenerator(_Generator):
         g = C.c_int32()
         check(lib.ocm_add_go_contact(h, len(self.indices), i64ptr(self.indices), dptr(self.ks),
                                      dptr(self.r0s), int(self.use_periodic), C.byref(g)))
+        return g.value
+
+
+class GaussianBondForceFieldGenerator(_Generator):
+    """AICG2+ k exp(-(r - v0)^2 / (2 sigma^2)); ks in kJ/mol, v0s and sigmas in nm."""
+
+    def __init__(self, indices_vec, ks, v0s, sigmas, use_periodic: bool):
+        self.indices = _pairs_arg(indices_vec, 2)
+        self.ks, self.v0s, self.sigmas = as_f64(ks), as_f64(v0s), as_f64(sigmas)
+        self.use_periodic = bool(use_periodic)
+        if not (len(self.indices) == len(self.ks) == len(self.v0s) == len(self.sigmas)):
+            raise OCMError(1, "[error] GaussianBondForceFieldGenerator: parameter number of "
+                              f"indices_vec ({len(self.indices)}), k ({len(self.ks)}), v0 ({len(self.v0s)}) "
+                              f"and sigmas ({len(self.sigmas)}) is not matched."
+                              "The number of these parameters must be same.")
+
+    def name(self) -> str:
+        return "GaussianBond"
+
+    def add_to(self, h) -> int:
+        g = C.c_int32()
+        check(lib.ocm_add_gaussian_bond(h, len(self.indices), i64ptr(self.indices), dptr(self.ks),
+                                        dptr(self.v0s), dptr(self.sigmas), int(self.use_periodic),
+                                        C.byref(g)))
+        return g.value
+
+
+class GaussianDihedralForceFieldGenerator(_Generator):
+    """AICG2+ k exp(-dphi^2 / (2 sigma^2)), dphi = phi - theta0 wrapped to
+    [-pi, pi); theta0s and sigmas in radians."""
+
+    def __init__(self, indices_vec, ks, theta0s, sigmas, use_periodic: bool):
+        self.indices = _pairs_arg(indices_vec, 4)
+        self.ks, self.theta0s, self.sigmas = as_f64(ks), as_f64(theta0s), as_f64(sigmas)
+        self.use_periodic = bool(use_periodic)
+        if not (len(self.indices) == len(self.ks) == len(self.theta0s) == len(self.sigmas)):
+            raise OCMError(1, "[error] GaussianDihedralForceFieldGenerator : parameter number of "
+                              f"indices_vec ({len(self.indices)}), k ({len(self.ks)}), theta0 "
+                              f"({len(self.theta0s)}) and simga ({len(self.sigmas)} is not matched."
+                              "The number of these parameters must be same.")
+
+    def name(self) -> str:
+        return "GaussianDihedral"
+
+    def add_to(self, h) -> int:
+        g = C.c_int32()
+        check(lib.ocm_add_gaussian_dihedral(h, len(self.indices), i64ptr(self.indices), dptr(self.ks),
+                                            dptr(self.theta0s), dptr(self.sigmas), int(self.use_periodic),
+                                            C.byref(g)))
         return g.value
 
 

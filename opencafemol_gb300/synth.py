@@ -23,7 +23,8 @@ import numpy as np
 
 from .forcefield import (AMINO_ACIDS, DebyeHuckelForceFieldGenerator,
                          ExcludedVolumeForceFieldGenerator, FlexibleLocalAngleForceFieldGenerator,
-                         FlexibleLocalDihedralForceFieldGenerator, GoContactForceFieldGenerator,
+                         FlexibleLocalDihedralForceFieldGenerator, GaussianBondForceFieldGenerator,
+                         GaussianDihedralForceFieldGenerator, GoContactForceFieldGenerator,
                          HarmonicBondForceFieldGenerator, LennardJonesAttractiveForceFieldGenerator,
                          LennardJonesRepulsiveForceFieldGenerator, System, SystemGenerator,
                          Topology, fla_spline_table, fld_fourier_table, fld_table_keys)
@@ -70,6 +71,16 @@ class CGSpec:
     fld_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
     fld_aa1: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     fld_aa2: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    # AICG2+ Gaussian bonds (k kJ/mol, v0 and sigma nm) and dihedrals
+    # (k kJ/mol, theta0 and sigma rad)
+    gb_idx: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int64))
+    gb_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    gb_v0: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    gb_sigma: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    gd_idx: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.int64))
+    gd_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    gd_theta0: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    gd_sigma: np.ndarray = field(default_factory=lambda: np.zeros(0))
     exv: PairTerm | None = None
     dh: PairTerm | None = None
     ljr: PairTerm | None = None
@@ -170,6 +181,39 @@ def go_protein(n: int, seed: int, temperature: float = 300.0, cutoff: float = 2.
     s.dh = PairTerm(ratio=cutoff / debye_length(temperature, ionic_strength), p0=q,
                     ionic_strength=ionic_strength, temperature=temperature, ign_bond=3)
     return s
+
+
+def dihedral_angles(pos: np.ndarray, idx: np.ndarray) -> np.ndarray:
+    """IUPAC dihedral angles (OpenMM's torsion convention) of quadruplets."""
+    b1 = pos[idx[:, 1]] - pos[idx[:, 0]]
+    b2 = pos[idx[:, 2]] - pos[idx[:, 1]]
+    b3 = pos[idx[:, 3]] - pos[idx[:, 2]]
+    n1, n2 = np.cross(b1, b2), np.cross(b2, b3)
+    y = np.linalg.norm(b2, axis=1) * np.sum(b1 * n2, axis=1)
+    return np.arctan2(y, np.sum(n1 * n2, axis=1))
+
+
+def add_aicg_gaussians(spec: CGSpec, seed: int, gb_sigma: float = 0.015,
+                       gd_sigma: float = 0.15) -> CGSpec:
+    """Attach AICG2+-shaped Gaussian terms to a chain (as in the AICG2+
+    sample inputs): bonds between beads i and i+2 centred on their current
+    distance and dihedrals over i..i+3 centred on their current angle, with
+    negative k (attractive wells) drawn from a seeded generator."""
+    rng = np.random.default_rng(seed)
+    n = spec.n
+    if n >= 3:
+        i = np.arange(n - 2)
+        spec.gb_idx = np.stack([i, i + 2], 1).astype(np.int64)
+        spec.gb_v0 = np.linalg.norm(spec.pos[i + 2] - spec.pos[i], axis=1)
+        spec.gb_k = -rng.uniform(0.5, 1.5, n - 2) * KJ_PER_KCAL
+        spec.gb_sigma = np.full(n - 2, gb_sigma)
+    if n >= 4:
+        i = np.arange(n - 3)
+        spec.gd_idx = np.stack([i, i + 1, i + 2, i + 3], 1).astype(np.int64)
+        spec.gd_theta0 = dihedral_angles(spec.pos, spec.gd_idx)
+        spec.gd_k = -rng.uniform(0.2, 0.6, n - 3) * KJ_PER_KCAL
+        spec.gd_sigma = np.full(n - 3, gd_sigma)
+    return spec
 
 
 def hps_slab(n_chains: int, chain_len: int, box, slab_width: float, seed: int,
@@ -326,8 +370,9 @@ def _ignore(topo: Topology, bond: int, contact: int) -> np.ndarray:
 
 
 def build_generator(spec: CGSpec) -> SystemGenerator:
-    """Assemble the spec in the order the TOML reader would (local forces,
-    then global pair forces), through the reference-named generators."""
+    """Assemble the spec through the reference-named generators, local
+    forces first (harmonic, Go, Gaussian bond, FLA, Gaussian dihedral, FLD:
+    the order of the AICG2+ sample inputs) and then the pair forces."""
     per = spec.periodic
     topo = Topology(spec.n)
     if len(spec.bonds):
@@ -341,11 +386,17 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
         sg.add_ff_generator(HarmonicBondForceFieldGenerator(spec.bonds, spec.bond_v0, spec.bond_k, per))
     if len(spec.contacts):
         sg.add_ff_generator(GoContactForceFieldGenerator(spec.contacts, spec.go_k, spec.go_r0, per))
+    if len(spec.gb_idx):
+        sg.add_ff_generator(GaussianBondForceFieldGenerator(spec.gb_idx, spec.gb_k, spec.gb_v0,
+                                                            spec.gb_sigma, per))
     if len(spec.fla_idx):
         for a, aa in enumerate(AMINO_ACIDS):
             sel = spec.fla_aa == a
             sg.add_ff_generator(FlexibleLocalAngleForceFieldGenerator(
                 spec.fla_idx[sel], spec.fla_k[sel], fla_spline_table(aa), aa, per))
+    if len(spec.gd_idx):
+        sg.add_ff_generator(GaussianDihedralForceFieldGenerator(spec.gd_idx, spec.gd_k, spec.gd_theta0,
+                                                                spec.gd_sigma, per))
     if len(spec.fld_idx):
         a1 = [AMINO_ACIDS[v] for v in spec.fld_aa1]
         a2 = [AMINO_ACIDS[v] for v in spec.fld_aa2]
@@ -379,7 +430,8 @@ def build_system(spec: CGSpec) -> System:
 # ---------------------------------------------------------------------------
 _PAIR_KEYS = ("exv", "dh", "ljr", "lja")
 _ARRAY_KEYS = ("pos", "masses", "bonds", "bond_v0", "bond_k", "contacts", "go_k", "go_r0", "fla_idx",
-               "fla_k", "fla_aa", "fld_idx", "fld_k", "fld_aa1", "fld_aa2")
+               "fla_k", "fla_aa", "fld_idx", "fld_k", "fld_aa1", "fld_aa2", "gb_idx", "gb_k", "gb_v0",
+               "gb_sigma", "gd_idx", "gd_k", "gd_theta0", "gd_sigma")
 
 
 def spec_to_arrays(spec: CGSpec) -> dict:
@@ -407,7 +459,8 @@ def spec_from_arrays(d) -> CGSpec:
     if spec.periodic:
         spec.box = tuple(float(v) for v in d["box"])
     for k in _ARRAY_KEYS[2:]:
-        setattr(spec, k, np.array(d[k]))
+        if k in d:
+            setattr(spec, k, np.array(d[k]))
     for key in _PAIR_KEYS:
         if f"{key}_scalars" not in d:
             continue
@@ -438,6 +491,11 @@ def subset_spec(spec: CGSpec, n_keep: int) -> CGSpec:
     s.fla_idx, s.fla_k, s.fla_aa = spec.fla_idx[m], spec.fla_k[m], spec.fla_aa[m]
     m = keep(spec.fld_idx)
     s.fld_idx, s.fld_k, s.fld_aa1, s.fld_aa2 = spec.fld_idx[m], spec.fld_k[m], spec.fld_aa1[m], spec.fld_aa2[m]
+    m = keep(spec.gb_idx)
+    s.gb_idx, s.gb_k, s.gb_v0, s.gb_sigma = spec.gb_idx[m], spec.gb_k[m], spec.gb_v0[m], spec.gb_sigma[m]
+    m = keep(spec.gd_idx)
+    s.gd_idx, s.gd_k, s.gd_theta0, s.gd_sigma = (spec.gd_idx[m], spec.gd_k[m], spec.gd_theta0[m],
+                                                 spec.gd_sigma[m])
     for key in _PAIR_KEYS:
         t = getattr(s, key)
         if t is not None:

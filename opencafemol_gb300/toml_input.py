@@ -26,9 +26,13 @@ conversions:
   ``coef`` pair, with the reader's GLY/PRO rules (including a GLY-PRO coef
   counted by both the GLY-PRO and the R2-PRO class).
 
-Terms outside the covered set (Gaussian bonds and dihedrals, 3SPN2, WCA,
-walls, group-based ignores, molecule-based ignores) raise ``ValueError``,
-or, with ``strict=False``, are left out and listed in ``skipped``.
+* AICG2+ Gaussian bonds (k kcal/mol -> kJ/mol, v0 and sigma Angstrom -> nm)
+  and Gaussian dihedrals (k kcal/mol -> kJ/mol, v0 and sigma in radians)
+  (ReadTOMLForceFieldGenerator.cpp:92-150, 494-540).
+
+Terms outside the covered set (cosine dihedrals, 3SPN2, WCA, walls,
+group-based ignores, molecule-based ignores) raise ``ValueError``, or, with
+``strict=False``, are left out and listed in ``skipped``.
 """
 from __future__ import annotations
 
@@ -173,6 +177,8 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
     contacts, go_k, go_r0 = [], [], []
     fla_idx, fla_k, fla_aa = [], [], []
     fld_idx, fld_k, fld_aa1, fld_aa2 = [], [], [], []
+    gb_idx, gb_k, gb_v0, gb_sigma = [], [], [], []
+    gd_idx, gd_k, gd_theta0, gd_sigma = [], [], [], []
     ff = data["forcefields"][0]
     for loc in ff.get("local", []):
         inter, pot = loc["interaction"], loc["potential"]
@@ -195,6 +201,26 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                 go_r0.append(float(p["v0"]) * NM_PER_ANGSTROM)
             if loc.get("topology") != "contact":
                 unsupported(f"{what}: only topology = \"contact\" is covered")
+        elif inter == "BondLength" and pot == "Gaussian":
+            for p in loc["parameters"]:
+                ij = _indices(p)
+                _check_range(ij, n, "read_toml_gaussian_bond_ff_generator")
+                gb_idx.append(ij)
+                gb_k.append(float(p["k"]) * KJ_PER_KCAL)
+                gb_v0.append(float(p["v0"]) * NM_PER_ANGSTROM)
+                gb_sigma.append(float(p["sigma"] if "sigma" in p else p["σ"]) * NM_PER_ANGSTROM)
+            if loc.get("topology", "none") != "none":
+                unsupported(f"{what}: only topology = \"none\" is covered")
+        elif inter == "DihedralAngle" and pot == "Gaussian":
+            for p in loc["parameters"]:
+                ijkl = _indices(p)
+                _check_range(ijkl, n, "read_toml_gaussian_dihedral_ff_generator")
+                gd_idx.append(ijkl)
+                gd_k.append(float(p["k"]) * KJ_PER_KCAL)
+                gd_theta0.append(float(p["v0"]))  # radian
+                gd_sigma.append(float(p["sigma"] if "sigma" in p else p["σ"]))  # radian
+            if loc.get("topology", "none") != "none":
+                unsupported(f"{what}: only topology = \"none\" is covered")
         elif inter == "BondAngle" and pot == "FlexibleLocalAngle":
             for p in loc["parameters"]:
                 ijk = _indices(p)
@@ -219,6 +245,12 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
     if contacts:
         spec.contacts = np.array(contacts, np.int64)
         spec.go_k, spec.go_r0 = np.array(go_k), np.array(go_r0)
+    if gb_idx:
+        spec.gb_idx, spec.gb_k = np.array(gb_idx, np.int64), np.array(gb_k)
+        spec.gb_v0, spec.gb_sigma = np.array(gb_v0), np.array(gb_sigma)
+    if gd_idx:
+        spec.gd_idx, spec.gd_k = np.array(gd_idx, np.int64), np.array(gd_k)
+        spec.gd_theta0, spec.gd_sigma = np.array(gd_theta0), np.array(gd_sigma)
     if fla_idx:
         spec.fla_idx, spec.fla_k = np.array(fla_idx, np.int64), np.array(fla_k)
         spec.fla_aa = np.array(fla_aa, np.int32)

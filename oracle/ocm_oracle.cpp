@@ -340,6 +340,20 @@ typedef struct OracleSystem {
     int fp32_cutoff;  // decide r < rc on the engine's FP32 r^2
     // pair enumeration: 0 all pairs, 1 cell grid, -1 cell grid above 4096 beads
     int pair_cells;
+    // AICG2+ Gaussian bonds k exp(-(r - v0)^2 / (2 sigma^2)) and dihedrals
+    // k exp(-dphi^2 / (2 sigma^2)) (theta0, sigma in radians)
+    int64_t n_gb;
+    const int64_t* gb_idx;
+    const double* gb_k;
+    const double* gb_v0;
+    const double* gb_sigma;
+    int gb_periodic;
+    int64_t n_gd;
+    const int64_t* gd_idx;
+    const double* gd_k;
+    const double* gd_theta0;
+    const double* gd_sigma;
+    int gd_periodic;
 } OracleSystem;
 
 // Energy slots: EXV, DH, LJR, LJA, HB, GO, FLA, FLD.
@@ -404,7 +418,7 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
     const int64_t n = s->n;
     std::vector<V3> x(n), f(n, V3{0, 0, 0});
     for (int64_t i = 0; i < n; ++i) x[i] = {s->pos[3 * i], s->pos[3 * i + 1], s->pos[3 * i + 2]};
-    double E[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double E[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const double L[3] = {s->box[0], s->box[1], s->box[2]};
     auto min_image = [&](V3 d, bool per) {
         if (!per) return d;
@@ -440,6 +454,20 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
         E[5] += s->go_k[b] * (5 * t12 - 6 * t10);
         const double dEdr = s->go_k[b] * (-60 * t12 + 60 * t10) / r;
         const double sc = -dEdr / r;
+        add(i, scale(d, -sc));
+        add(j, scale(d, sc));
+    }
+    // -------- Gaussian bonds (GaussianBondForceFieldGenerator.cpp:5-7) --------
+    for (int64_t b = 0; b < s->n_gb; ++b) {
+        const int64_t i = s->gb_idx[2 * b], j = s->gb_idx[2 * b + 1];
+        const V3 d = min_image(sub(x[j], x[i]), s->gb_periodic);
+        const double r = std::sqrt(dot(d, d));
+        const double dr = r - s->gb_v0[b];
+        const double sg = s->gb_sigma[b];
+        const double e = s->gb_k[b] * std::exp(-dr * dr / (2 * sg * sg));
+        E[8] += e;
+        const double dEdr = -e * dr / (sg * sg);
+        const double sc = -dEdr / r;  // F_i = sc (x_i - x_j)
         add(i, scale(d, -sc));
         add(j, scale(d, sc));
     }
@@ -527,6 +555,34 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
                 add(i4, scale(d4, -dE));
             }
         }
+    }
+    // -------- Gaussian dihedrals (GaussianDihedralForceFieldGenerator.cpp:5-12) --------
+    for (int64_t q = 0; q < s->n_gd; ++q) {
+        const int64_t i1 = s->gd_idx[4 * q], i2 = s->gd_idx[4 * q + 1];
+        const int64_t i3 = s->gd_idx[4 * q + 2], i4 = s->gd_idx[4 * q + 3];
+        const V3 F = min_image(sub(x[i1], x[i2]), s->gd_periodic);
+        const V3 G = min_image(sub(x[i2], x[i3]), s->gd_periodic);
+        const V3 H = min_image(sub(x[i4], x[i3]), s->gd_periodic);
+        const V3 A = cross(F, G), B = cross(H, G);
+        const double AA = dot(A, A), BB = dot(B, B), Gl = std::sqrt(dot(G, G));
+        const V3 b1 = scale(F, -1), b2 = scale(G, -1), b3 = H;
+        const double phi = std::atan2(Gl * dot(b1, cross(b2, b3)), dot(cross(b1, b2), cross(b2, b3)));
+        const double pi = 3.1415926535897932385;
+        double dt = phi - s->gd_theta0[q];
+        dt -= std::floor((dt + pi) / (2 * pi)) * (2 * pi);
+        const double sg = s->gd_sigma[q];
+        const double e = s->gd_k[q] * std::exp(-dt * dt / (2 * sg * sg));
+        E[9] += e;
+        const double dE = -e * dt / (sg * sg);
+        const double ga = Gl / AA, gb = Gl / BB;
+        const double fg = dot(F, G) / (AA * Gl), hg = dot(H, G) / (BB * Gl);
+        const V3 d1 = scale(A, -ga), d4 = scale(B, gb);
+        const V3 d2 = {(ga + fg) * A.x - hg * B.x, (ga + fg) * A.y - hg * B.y, (ga + fg) * A.z - hg * B.z};
+        const V3 d3 = {-fg * A.x + (hg - gb) * B.x, -fg * A.y + (hg - gb) * B.y, -fg * A.z + (hg - gb) * B.z};
+        add(i1, scale(d1, -dE));
+        add(i2, scale(d2, -dE));
+        add(i3, scale(d3, -dE));
+        add(i4, scale(d4, -dE));
     }
     // -------- pair terms --------
     std::vector<std::pair<int64_t, int64_t>> bond_edges, contact_edges;
@@ -705,7 +761,7 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
             forces[3 * i + 2] = f[i].z;
         }
     if (energies)
-        for (int k = 0; k < 8; ++k) energies[k] = E[k];
+        for (int k = 0; k < 10; ++k) energies[k] = E[k];
     return 0;
 }
 

@@ -35,6 +35,10 @@ class OracleSystem(C.Structure):
         ("lja_on", C.c_int), ("lja_ratio", C.c_double), ("lja_eps", _D), ("lja_sigma", _D),
         ("lja_ign_bond", C.c_int), ("lja_ign_contact", C.c_int),
         ("fp32_cutoff", C.c_int), ("pair_cells", C.c_int),
+        ("n_gb", C.c_int64), ("gb_idx", _I64), ("gb_k", _D), ("gb_v0", _D), ("gb_sigma", _D),
+        ("gb_periodic", C.c_int),
+        ("n_gd", C.c_int64), ("gd_idx", _I64), ("gd_k", _D), ("gd_theta0", _D), ("gd_sigma", _D),
+        ("gd_periodic", C.c_int),
     ]
 
 
@@ -135,11 +139,23 @@ def make_system(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
         s.lja_ign_bond, s.lja_ign_contact = t.ign_bond, t.ign_contact
     s.fp32_cutoff = int(fp32_cutoff)
     s.pair_cells = int(cells)
+    gb = getattr(spec, "gb_idx", np.zeros((0, 2), np.int64))
+    s.n_gb = len(gb)
+    if s.n_gb:
+        s.gb_idx, s.gb_k, s.gb_v0, s.gb_sigma = k.i64(gb), k.d(spec.gb_k), k.d(spec.gb_v0), k.d(spec.gb_sigma)
+    s.gb_periodic = int(spec.periodic)
+    gd = getattr(spec, "gd_idx", np.zeros((0, 4), np.int64))
+    s.n_gd = len(gd)
+    if s.n_gd:
+        s.gd_idx, s.gd_k = k.i64(gd), k.d(spec.gd_k)
+        s.gd_theta0, s.gd_sigma = k.d(spec.gd_theta0), k.d(spec.gd_sigma)
+    s.gd_periodic = int(spec.periodic)
     return s, k
 
 
 SLOTS = ("ExcludedVolume", "DebyeHuckel", "LennardJonesRepulsive", "LennardJonesAttractive",
-         "HarmonicBond", "GoContact", "FlexibleLocalAngle", "FlexibleLocalDihedral")
+         "HarmonicBond", "GoContact", "FlexibleLocalAngle", "FlexibleLocalDihedral", "GaussianBond",
+         "GaussianDihedral")
 
 
 def evaluate(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
@@ -148,7 +164,7 @@ def evaluate(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
     the grid above 4096 beads)."""
     s, keep = make_system(spec, fp32_cutoff, pos, cells)
     f = np.zeros((spec.n, 3))
-    e = np.zeros(8)
+    e = np.zeros(len(SLOTS))
     lib().oracle_evaluate(C.byref(s), f.ctypes.data_as(_D), e.ctypes.data_as(_D))
     del keep
     return f, dict(zip(SLOTS, e))

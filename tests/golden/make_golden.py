@@ -5,10 +5,10 @@ The reference ships no expected outputs (its tests only check that inputs
 parse), so the expected values here are the FP64 oracle's, evaluated on
 systems read from the reference's sample TOML files:
 
-* ``sh3_aicg2.npz``: sample/toml_input/sh3_AICG2+.toml, all 56 beads, with
-  HarmonicBond, GoContact, FlexibleLocalAngle, FlexibleLocalDihedral and
-  ExcludedVolume (the file's Gaussian bond and dihedral terms are outside
-  the covered set and are left out);
+* ``sh3_aicg2.npz``: sample/toml_input/sh3_AICG2+.toml, all 56 beads and
+  every term of the file: HarmonicBond, GoContact, GaussianBond,
+  FlexibleLocalAngle, GaussianDihedral, FlexibleLocalDihedral and
+  ExcludedVolume;
 * ``fus_hps_2chains.npz``: the first two 163-bead chains of
   sample/toml_input/FUS_100_HPS.toml in the file's periodic box, with
   HarmonicBond, LennardJonesRepulsive, LennardJonesAttractive and

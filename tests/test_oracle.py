@@ -252,3 +252,44 @@ def test_cell_grid_matches_all_pairs(case):
     assert np.max(np.abs(f1 - f0)) <= 1e-9 * np.abs(f0).max()
     for k in e0:
         assert abs(e1[k] - e0[k]) <= 1e-9 * max(1.0, abs(e0[k])), k
+
+
+def test_gaussian_terms_at_their_centres():
+    """At the structure the AICG2+ Gaussian terms are centred on, every bond
+    and dihedral sits at the bottom of its well: E = sum k, zero force."""
+    spec = synth.add_aicg_gaussians(synth.go_protein(30, 41), seed=42)
+    only = synth.CGSpec(n=spec.n, pos=spec.pos, masses=spec.masses)
+    for k in ("gb_idx", "gb_k", "gb_v0", "gb_sigma", "gd_idx", "gd_k", "gd_theta0", "gd_sigma"):
+        setattr(only, k, getattr(spec, k))
+    f, e = oracle.evaluate(only, fp32_cutoff=False)
+    assert e["GaussianBond"] == pytest.approx(spec.gb_k.sum(), rel=1e-12)
+    assert e["GaussianDihedral"] == pytest.approx(spec.gd_k.sum(), rel=1e-12)
+    assert np.abs(f).max() < 1e-9
+
+
+def test_gaussian_dihedral_is_periodic():
+    """dphi is wrapped to [-pi, pi): a centre shifted by 2 pi is the same term."""
+    spec = synth.add_aicg_gaussians(synth.go_protein(12, 43), seed=44)
+    spec.gb_idx = spec.gb_idx[:0]
+    x = spec.pos + np.random.default_rng(1).normal(scale=0.05, size=spec.pos.shape)
+    f0, e0 = oracle.evaluate(spec, fp32_cutoff=False, pos=x)
+    shifted = copy.deepcopy(spec)
+    shifted.gd_theta0 = spec.gd_theta0 + 2 * math.pi
+    f1, e1 = oracle.evaluate(shifted, fp32_cutoff=False, pos=x)
+    assert e1["GaussianDihedral"] == pytest.approx(e0["GaussianDihedral"], rel=1e-12)
+    assert np.allclose(f1, f0, rtol=1e-10, atol=1e-10)
+
+
+def test_gaussian_forces_are_minus_gradient():
+    spec = synth.add_aicg_gaussians(synth.go_protein(40, 45), seed=46)
+    pos = spec.pos + np.random.default_rng(2).normal(scale=0.01, size=spec.pos.shape)
+    f, _ = oracle.evaluate(spec, fp32_cutoff=False, pos=pos)
+    rng = np.random.default_rng(3)
+    h = 1e-6
+    for i in rng.choice(spec.n, 8, replace=False):
+        for c in range(3):
+            xp, xm = pos.copy(), pos.copy()
+            xp[i, c] += h
+            xm[i, c] -= h
+            fd = -(_total_energy(spec, xp) - _total_energy(spec, xm)) / (2 * h)
+            assert fd == pytest.approx(f[i, c], rel=2e-5, abs=2e-4 * (1 + abs(f[i, c])))

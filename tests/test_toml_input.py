@@ -137,15 +137,42 @@ def test_periodic_box():
 def test_unsupported_terms():
     text = BASE + """
 [[forcefields.local]]
+interaction = "DihedralAngle"
+potential = "Cosine"
+topology = "none"
+parameters = [{indices = [0, 1, 2, 3], v0 = -1.0, k = -4.0, n = 7}]
+"""
+    with pytest.raises(ValueError, match="Cosine"):
+        _read(text)
+    t = _read(text, strict=False)
+    assert t.skipped == ["local force DihedralAngle/Cosine is not covered"]
+
+
+def test_gaussian_terms():
+    """AICG2+ Gaussian bond (v0, sigma in Angstrom) and dihedral (v0, sigma
+    in radians; the sigma key may be spelled "σ")."""
+    text = BASE + """
+[[forcefields.local]]
 interaction = "BondLength"
 potential = "Gaussian"
 topology = "none"
-parameters = [{indices = [0, 2], v0 = 6.9, k = -1.3, "σ" = 0.15}]
+parameters = [{indices = [0, 2], v0 = 6.9701, k = -1.3709, "σ" = 0.15}]
+[[forcefields.local]]
+interaction = "DihedralAngle"
+potential = "Gaussian"
+topology = "none"
+parameters = [{indices = [0, 1, 2, 3], v0 = -2.2089, k = -0.435, sigma = 0.15}]
 """
-    with pytest.raises(ValueError, match="Gaussian"):
-        _read(text)
-    t = _read(text, strict=False)
-    assert t.skipped == ["local force BondLength/Gaussian is not covered"]
+    from opencafemol_gb300 import synth
+    s = _read(text).spec
+    assert s.gb_idx.tolist() == [[0, 2]]
+    assert s.gb_k[0] == pytest.approx(-1.3709 * 4.184) and s.gb_v0[0] == pytest.approx(0.69701)
+    assert s.gb_sigma[0] == pytest.approx(0.015)
+    assert s.gd_idx.tolist() == [[0, 1, 2, 3]]
+    assert s.gd_k[0] == pytest.approx(-0.435 * 4.184) and s.gd_theta0[0] == -2.2089
+    assert s.gd_sigma[0] == 0.15
+    names = synth.build_system(s).group_names()
+    assert "GaussianBond" in names and "GaussianDihedral" in names
 
 
 def test_index_out_of_range():
