@@ -89,7 +89,8 @@ __device__ __forceinline__ float pair_scalar(float r2, float4 pi, float4 pj, flo
             e.exv += pc.exv_eps * (u6 - w3 * w3);
         }
     }
-    if ((TERMS & kTermDH) && !(excl & kTermDH) && r2 < pc.dh_rc2) {
+    // q_i q_j = 0 adds exactly nothing, so skipping it changes no bit
+    if ((TERMS & kTermDH) && !(excl & kTermDH) && r2 < pc.dh_rc2 && pi.y != 0.f && pj.y != 0.f) {
         const float r = r2 * rinv;
         const float ex = exp2f(-r * pc.dh_inv_lambda_log2e);
         const float qq = pi.y * pj.y * pc.dh_k;
