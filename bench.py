@@ -234,8 +234,8 @@ def run_ours(args, rank, world):
     e2e = run_e2e(ocm, synth, specs, systems, args, world)
 
     # ---- plain single-system path on a sample of the same mix ----
-    plain = run_plain(ocm, specs, systems, args)
-    plain_cfgs = run_plain_configs(ocm, args) if args.cfg1_steps > 0 else None
+    plain = run_plain(ocm, specs, systems, args) if args.plain_sample > 0 else None
+    plain_cfgs = run_plain_configs(ocm, args) if (args.cfg0_steps > 0 or args.cfg1_steps > 0) else None
 
     # ---- served stream (continuous batching), p50/p99 completion latency ----
     serve = run_serving(ocm, args) if args.serve_requests > 0 and rank == 0 else None
@@ -364,9 +364,12 @@ def run_plain_configs(ocm, args):
     friction, 2 fs steps).  Wall-clock timing around synchronous steps."""
     from opencafemol_gb300 import synth
     out = {}
-    cases = [("go_protein_60", synth.go_protein(60, 11), 0, args.cfg0_steps),
-             ("hps_slab_20000", synth.hps_slab(100, 200, (15.0, 15.0, 150.0), slab_width=30.0, seed=7),
-              args.cfg1_relax, args.cfg1_steps)]
+    cases = []
+    if args.cfg0_steps > 0:
+        cases.append(("go_protein_60", synth.go_protein(60, 11), 0, args.cfg0_steps))
+    if args.cfg1_steps > 0:
+        cases.append(("hps_slab_20000", synth.hps_slab(100, 200, (15.0, 15.0, 150.0), slab_width=30.0, seed=7),
+                      args.cfg1_relax, args.cfg1_steps))
     for name, spec, relax, steps in cases:
         system = synth.build_system(spec)
         pos = spec.pos
