@@ -395,6 +395,7 @@ def run_plain_configs(ocm, args):
         out[name] = {"beads": int(spec.n), "steps": int(steps), "bead_steps_per_s": spec.n * steps / t,
                      "ns_per_day": steps / t * spec.dt * 86400 * 1e-3, "us_per_step": t / steps * 1e6,
                      "list_builds": int(st["list_builds"]), "tiles": int(st["tiles"]),
+                     "charged_pairs": int(st["charged_pairs"]), "tile_cutoff_nm": round(st["tile_cutoff"], 4),
                      "untimed_relaxation_steps": int(relax)}
     return out
 

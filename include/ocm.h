@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define OCM_ABI_VERSION 1
+#define OCM_ABI_VERSION 2
 
 enum ocm_status {
     OCM_OK = 0,
@@ -228,14 +228,20 @@ typedef struct ocm_context_stats {
     int32_t reordered;        /* 1 if beads are Morton-sorted into clusters */
     double  skin;             /* nm */
     double  max_cutoff;       /* nm */
+    double  tile_cutoff;      /* nm: largest cutoff the cluster-pair tiles serve */
+    int64_t charged_pairs;    /* entries of the charged-pair list (0 without one) */
+    int32_t charged_split;    /* 1 if Debye-Hueckel runs on its own charged-pair list */
+    int32_t reserved_;
 } ocm_context_stats;
 int ocm_context_get_stats(ocm_context* ctx, ocm_context_stats* out);
 /* Rebuild interval / skin overrides (0 keeps the current value). */
 int ocm_context_set_list_options(ocm_context* ctx, int32_t rebuild_interval, double skin);
 /* Debug/verification: every pair (i<j, original indices) that the tile list
  * makes the nonbonded kernel test AND that passes the FP32 cutoff test of
- * the largest pair cutoff, written to out_pairs.  Used to prove the list
- * is bit-exact against brute force. */
+ * the largest cutoff the tiles serve (stats.tile_cutoff), followed, when
+ * Debye-Hueckel runs on its own charged-pair list (stats.charged_split),
+ * by the listed charged pairs that pass its FP32 cutoff test; written to
+ * out_pairs.  Used to prove the lists are bit-exact against brute force. */
 int ocm_context_list_pairs(ocm_context* ctx, int64_t* out_pairs, int64_t capacity,
                            int64_t* n_out);
 /* Debug/verification: the bead order of the cluster layout (sorted slot ->

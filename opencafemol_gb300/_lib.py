@@ -33,7 +33,9 @@ class OCMError(RuntimeError):
 class ContextStats(C.Structure):
     _fields_ = [("steps_done", C.c_int64), ("list_builds", C.c_int64), ("tiles", C.c_int64),
                 ("masked_tiles", C.c_int64), ("rebuild_interval", C.c_int32),
-                ("reordered", C.c_int32), ("skin", C.c_double), ("max_cutoff", C.c_double)]
+                ("reordered", C.c_int32), ("skin", C.c_double), ("max_cutoff", C.c_double),
+                ("tile_cutoff", C.c_double), ("charged_pairs", C.c_int64), ("charged_split", C.c_int32),
+                ("reserved_", C.c_int32)]
 
 
 _P = C.c_void_p

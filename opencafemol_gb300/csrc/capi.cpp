@@ -439,7 +439,9 @@ int ocm_context_get_stats(ocm_context* ctx, ocm_context_stats* out) {
              out->list_builds = c.list_builds; out->tiles = c.tiles_last;
              out->masked_tiles = c.masked_last; out->rebuild_interval = c.rebuild_interval;
              out->reordered = c.reorder ? 1 : 0; out->skin = c.skin;
-             out->max_cutoff = c.cs.max_cutoff);
+             out->max_cutoff = c.cs.max_cutoff; out->tile_cutoff = c.tile_cutoff();
+             out->charged_pairs = c.charged_pairs(); out->charged_split = c.charged_split() ? 1 : 0;
+             out->reserved_ = 0);
 }
 int ocm_context_set_list_options(ocm_context* ctx, int32_t interval, double skin) {
     CTX_CALL(ctx->c->set_list_options(interval, skin));

@@ -48,7 +48,7 @@ struct DevBuf {
 };
 
 struct ListFlags {
-    enum : int { kTileOverflow = 1, kMaskOverflow = 2, kSkinViolation = 4 };
+    enum : int { kTileOverflow = 1, kMaskOverflow = 2, kSkinViolation = 4, kChargedOverflow = 8 };
 };
 
 // Device-resident single system, the part of an OpenMM Context + Langevin
@@ -70,6 +70,9 @@ class PlainContext {
     void set_list_options(int32_t interval, double skin);
     void list_pairs(int64_t* out, int64_t cap, int64_t* n_out);
     void cluster_order(int64_t* out, int64_t cap, int64_t* n_out);
+    bool charged_split() const { return charged_split_; }
+    double tile_cutoff() const { return tile_cutoff_; }
+    int64_t charged_pairs() const { return charged_last_; }
 
     int device = 0;
     int64_t n = 0, np = 0, nc = 0;
@@ -87,6 +90,7 @@ class PlainContext {
     void ensure_capacity();
     cudaGraphExec_t graph_for(int chunk);
     void clear_graphs();
+    void setup_charged_cells();
     void eval(uint32_t groups, bool energy, double* forces, double* slot_energy);
     uint32_t slots_for_groups(uint32_t groups) const;
     void check_positions_set() const;
@@ -100,6 +104,15 @@ class PlainContext {
     int64_t n_cells_ = 0;
     int64_t tile_cap_ = 0, mask_cap_ = 0;
     float3 box_{0, 0, 0}, inv_box_{0, 0, 0};
+    // Charged-pair list: when the Debye-Hueckel cutoff is the largest, the
+    // tiles serve the other pair terms only and every charged bead gets a
+    // row of its charged partners within the Debye-Hueckel cutoff (+ skin),
+    // built from a cell grid over the charged beads.
+    bool charged_split_ = false;
+    double tile_cutoff_ = 0;  // largest cutoff the tiles serve
+    int charged_cells_[3] = {1, 1, 1};
+    int64_t n_charged_ = 0, n_charged_cells_ = 0, charged_last_ = 0;
+    int64_t chg_row_cap_ = 0;  // entries per charged bead's row
 
     // per particle (original order)
     DevBuf<double> x_, y_, z_;
@@ -122,6 +135,10 @@ class PlainContext {
     // exclusions
     DevBuf<int32_t> ex_start_, ex_j_;
     DevBuf<uint8_t> ex_bits_;
+    // charged-pair list
+    DevBuf<int32_t> chg_idx_, chg_key_, chg_count_, chg_start_, chg_fill_, chg_bucket_;
+    DevBuf<int32_t> chg_rows_, chg_len_, chg_stats_;  // rows, row lengths, {longest, entries}
+    DevBuf<int32_t> ex_csr_;  // per-bead start of its exclusion row (n + 1)
     // bonded
     DevBuf<BondTerm> bonds_;
     DevBuf<AngleTerm> angles_;

@@ -288,11 +288,128 @@ __global__ void k_excl(int nnz, int nc, int tile_cap, const int32_t* __restrict_
 }
 
 // ---------------------------------------------------------------------------
+// Charged-pair list (Debye-Hueckel beyond the other terms' cutoffs): a cell
+// grid over the charged beads, cells at least (cutoff + skin) wide, and per
+// charged bead t a row of every charged partner j != i within range that the
+// Debye-Hueckel exclusions keep (both directions of each pair are listed, so
+// the force kernel writes only bead i's force and needs no atomics per pair).
+// A row's order depends on atomic timing in the cell scatter; the forces do
+// not, because each pair's force is rounded to fixed point before it is
+// summed.
+// ---------------------------------------------------------------------------
+__global__ void k_chg_keys(int m, const int32_t* __restrict__ idx, const float4* __restrict__ xq,
+                           int nx, int ny, int nz, float3 box, int32_t* __restrict__ key,
+                           int32_t* __restrict__ count) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    const float4 p = xq[idx[t]];
+    const int cx = min(nx - 1, max(0, (int)(p.x * ((float)nx / box.x))));
+    const int cy = min(ny - 1, max(0, (int)(p.y * ((float)ny / box.y))));
+    const int cz = min(nz - 1, max(0, (int)(p.z * ((float)nz / box.z))));
+    const int k = (cz * ny + cy) * nx + cx;
+    key[t] = k;
+    atomicAdd(&count[k], 1);
+}
+
+__global__ void k_chg_scatter(int m, const int32_t* __restrict__ key, const int32_t* __restrict__ start,
+                              int32_t* __restrict__ fill, int32_t* __restrict__ bucket) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    const int k = key[t];
+    bucket[start[k] + atomicAdd(&fill[k], 1)] = t;
+}
+
+// One warp per charged bead: the 27 neighbour cells in a fixed order, 32
+// candidates at a time, kept partners compacted by ballot.  row_stats[0] is
+// the longest row, row_stats[1] the number of row entries.
+__global__ void k_chg_rows(int m, const int32_t* __restrict__ idx, const int32_t* __restrict__ key,
+                           const float4* __restrict__ xq, int nx, int ny, int nz, float3 box,
+                           float3 inv_box, float cut2, const int32_t* __restrict__ start,
+                           const int32_t* __restrict__ bucket, const int32_t* __restrict__ ex_csr,
+                           const int32_t* __restrict__ ex_j, const uint8_t* __restrict__ ex_bits,
+                           int32_t* __restrict__ rows, int32_t* __restrict__ row_len, int row_cap,
+                           int32_t* __restrict__ row_stats, int32_t* flags) {
+    const int lane = threadIdx.x & 31;
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (t >= m) return;  // warp-uniform
+    const int i = idx[t];
+    const float4 xi = xq[i];
+    const int k = key[t];
+    const int cx = k % nx, cy = (k / nx) % ny, cz = k / (nx * ny);
+    const int e0 = ex_csr[i], e1 = ex_csr[i + 1];
+    int32_t* row = rows + (size_t)t * row_cap;
+    int len = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int c = (((cz + dz + nz) % nz) * ny + (cy + dy + ny) % ny) * nx + (cx + dx + nx) % nx;
+                const int q1 = start[c + 1];
+                for (int q0 = start[c]; q0 < q1; q0 += 32) {
+                    const int q = q0 + lane;
+                    bool keep = false;
+                    int j = 0;
+                    if (q < q1) {
+                        j = idx[bucket[q]];
+                        if (j != i) {
+                            const float r2 = norm2(separation<true>(xi, xq[j], box, inv_box));
+                            keep = r2 < cut2;
+                            if (keep && e0 < e1) {
+                                int lo = e0, hi = e1;  // this row's exclusions, sorted by j
+                                while (lo < hi) {
+                                    const int mid = (lo + hi) >> 1;
+                                    if (ex_j[mid] < j) lo = mid + 1;
+                                    else hi = mid;
+                                }
+                                if (lo < e1 && ex_j[lo] == j && (ex_bits[lo] & kTermDH)) keep = false;
+                            }
+                        }
+                    }
+                    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                    if (keep) {
+                        const int at = len + __popc(bal & ((1u << lane) - 1u));
+                        if (at < row_cap) row[at] = j;
+                    }
+                    len += __popc(bal);
+                }
+            }
+    if (lane == 0) {
+        row_len[t] = len;
+        atomicMax(&row_stats[0], len);
+        atomicAdd(&row_stats[1], len);
+        if (len > row_cap) atomicOr(flags, ListFlags::kChargedOverflow);
+    }
+}
+
+// Verification: the charged pairs (i < j) of the rows whose FP32 r^2 is
+// below the Debye-Hueckel cutoff squared.
+__global__ void k_chg_list_pairs(int m, const int32_t* __restrict__ idx, const int32_t* __restrict__ rows,
+                                 const int32_t* __restrict__ row_len, int row_cap,
+                                 const float4* __restrict__ xq, float3 box, float3 inv_box, float rc2,
+                                 long long* out, long long out_cap, unsigned long long* count) {
+    const int t = blockIdx.x;
+    if (t >= m) return;
+    const int i = idx[t];
+    const int len = min(row_len[t], row_cap);
+    for (int p = threadIdx.x; p < len; p += blockDim.x) {
+        const int j = rows[(size_t)t * row_cap + p];
+        if (j < i) continue;
+        const float r2 = norm2(separation<true>(xq[i], xq[j], box, inv_box));
+        if (r2 < rc2) {
+            const unsigned long long at = atomicAdd(count, 1ull);
+            if ((long long)at < out_cap) {
+                out[2 * at] = i;
+                out[2 * at + 1] = j;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Fused force kernel
 // ---------------------------------------------------------------------------
 struct ForceArgs {
     int tile_cap;
-    int nc, blocks_tiles, blocks_bonds, blocks_angles, blocks_dih;
+    int nc, blocks_tiles, blocks_bonds, blocks_angles, blocks_dih, blocks_chg;
     int n;
     const float4 *xs, *p0s, *p1s;
     const uint32_t* labs;
@@ -311,6 +428,10 @@ struct ForceArgs {
     uint32_t slots_enabled;
     uint32_t excl_all;
     double* energy;
+    // charged-pair rows (blocks_chg > 0)
+    const float4 *xq, *p0;
+    const int32_t *chg_idx, *chg_rows, *chg_len;
+    int n_chg, chg_row_cap;
 };
 
 __device__ __forceinline__ void add_force(unsigned long long* F, int n, int i, float3 f) {
@@ -518,7 +639,7 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
         return;
     }
     blk -= a.blocks_angles;
-    {
+    if (blk < a.blocks_dih) {
         const int t = blk * kForceThreads + threadIdx.x;
         float efld = 0.f, egd = 0.f;
         if (t < a.n_dih) {
@@ -549,6 +670,56 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                 if (v != 0.0) atomicAdd(&a.energy[kSlotFLD], v);
                 if (vg != 0.0) atomicAdd(&a.energy[kSlotGD], vg);
             }
+        }
+        return;
+    }
+    blk -= a.blocks_dih;
+    {
+        // ---------------- charged pairs (Debye-Hueckel) ----------------
+        // One warp per charged bead over its row; each pair's force on bead
+        // i is rounded to fixed point and summed as integers, then added
+        // once per bead.
+        const int warp = threadIdx.x >> 5;
+        float edh = 0.f;
+        if (a.slots_enabled & (1u << kSlotDH)) {
+            const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int t = blk * kWarpsPerForceBlock + warp; t < a.n_chg; t += a.blocks_chg * kWarpsPerForceBlock) {
+                const int i = a.chg_idx[t];
+                const float4 xi = a.xq[i];
+                const float4 pi = a.p0[i];
+                const int len = min(a.chg_len[t], a.chg_row_cap);
+                const int32_t* row = a.chg_rows + (size_t)t * a.chg_row_cap;
+                long long fx = 0, fy = 0, fz = 0;
+                for (int p = lane; p < len; p += 32) {
+                    const int j = row[p];
+                    const float3 d = separation<PERIODIC>(xi, a.xq[j], a.box, a.inv_box);
+                    const float r2 = norm2(d);
+                    if (r2 < a.pc.dh_rc2) {
+                        PairEnergy e;
+                        e.zero();
+                        const float sc = pair_scalar<kTermDH, ENERGY>(r2, pi, a.p0[j], zero4, zero4, 0u, a.pc, e);
+                        fx += (long long)to_fixed(-sc * d.x);
+                        fy += (long long)to_fixed(-sc * d.y);
+                        fz += (long long)to_fixed(-sc * d.z);
+                        if (ENERGY && i < j) edh += e.dh;
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    fx += __shfl_xor_sync(0xffffffffu, fx, o);
+                    fy += __shfl_xor_sync(0xffffffffu, fy, o);
+                    fz += __shfl_xor_sync(0xffffffffu, fz, o);
+                }
+                if (lane == 0) {
+                    if (fx) atomicAdd(&a.F[i], (unsigned long long)fx);
+                    if (fy) atomicAdd(&a.F[a.n + i], (unsigned long long)fy);
+                    if (fz) atomicAdd(&a.F[2 * a.n + i], (unsigned long long)fz);
+                }
+            }
+        }
+        if (ENERGY) {
+            const double v = warp_sum((double)edh);
+            if (lane == 0 && v != 0.0) atomicAdd(&a.energy[kSlotDH], v);
         }
     }
 }
@@ -836,6 +1007,40 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
         ex_start_.upload(ei, s);  // row index of each entry
         ex_j_.upload(cs.ex_j, s);
         ex_bits_.upload(cs.ex_bits, s);
+        ex_csr_.upload(cs.ex_start, s);
+    }
+    // Charged-pair list: worth it when the Debye-Hueckel cutoff clearly
+    // exceeds the other pair cutoffs (most of the tiles' volume would serve
+    // the few charged pairs only) and no interaction groups restrict it.
+    tile_cutoff_ = cs.max_cutoff;
+    {
+        const PairConsts& pc = cs.pc;
+        double other = 0.0;
+        if (pc.terms & kTermEXV) other = std::max(other, std::sqrt((double)pc.exv_rc2));
+        if (pc.terms & kTermLJR) other = std::max(other, std::sqrt((double)pc.ljr_rc2));
+        if (pc.terms & kTermLJA) other = std::max(other, std::sqrt((double)pc.lja_rc2));
+        const double dh = (pc.terms & kTermDH) ? std::sqrt((double)pc.dh_rc2) : 0.0;
+        std::vector<int32_t> idx;
+        for (int64_t i = 0; i < n; ++i)
+            if (cs.p0[4 * i + 1] != 0.f) idx.push_back((int32_t)i);
+        if (reorder && cs.periodic && (pc.terms & kTermDH) && !(pc.uses_labels & kTermDH) && dh > other + 0.3 &&
+            !idx.empty()) {
+            n_charged_ = (int64_t)idx.size();
+            chg_idx_.upload(idx, s);
+            chg_key_.alloc(n_charged_);
+            chg_bucket_.alloc(n_charged_);
+            chg_len_.alloc(n_charged_);
+            OCM_CK(cudaMemsetAsync(chg_len_.p, 0, n_charged_ * sizeof(int32_t), s));
+            chg_stats_.alloc(2);
+            OCM_CK(cudaMemsetAsync(chg_stats_.p, 0, 2 * sizeof(int32_t), s));
+            charged_split_ = true;
+            tile_cutoff_ = other;
+            setup_charged_cells();
+            if (charged_split_) {
+                chg_row_cap_ = 128;
+                chg_rows_.alloc(n_charged_ * chg_row_cap_);
+            }
+        }
     }
     bonds_.upload(cs.bonds, s);
     angles_.upload(cs.angles, s);
@@ -978,7 +1183,7 @@ void PlainContext::rebuild(cudaStream_t s) {
     const int wblocks = div_up(nc * 32, 128);
     if (per) k_bbox<true><<<wblocks, 128, 0, s>>>(nc_i, xs_.p, perm_.p, box_, inv_box_, bb_c_.p, bb_h_.p);
     else k_bbox<false><<<wblocks, 128, 0, s>>>(nc_i, xs_.p, perm_.p, box_, inv_box_, bb_c_.p, bb_h_.p);
-    const float cut = (float)(cs.max_cutoff + skin) * 1.0001f + 1e-4f;
+    const float cut = (float)(tile_cutoff_ + skin) * 1.0001f + 1e-4f;
     const float cut2 = cut * cut;
     if (per) {
         k_tiles<true, false><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2,
@@ -1012,6 +1217,21 @@ void PlainContext::rebuild(cudaStream_t s) {
                                                        flags_.p);
     }
     OCM_CK(cudaGetLastError());
+    if (charged_split_) {
+        const int m = (int)n_charged_;
+        OCM_CK(cudaMemsetAsync(chg_count_.p, 0, n_charged_cells_ * sizeof(int32_t), s));
+        OCM_CK(cudaMemsetAsync(chg_fill_.p, 0, n_charged_cells_ * sizeof(int32_t), s));
+        OCM_CK(cudaMemsetAsync(chg_stats_.p, 0, 2 * sizeof(int32_t), s));
+        k_chg_keys<<<div_up(m, 256), 256, 0, s>>>(m, chg_idx_.p, xq_.p, charged_cells_[0], charged_cells_[1],
+                                                  charged_cells_[2], box_, chg_key_.p, chg_count_.p);
+        k_scan<<<1, 1024, 0, s>>>((int)n_charged_cells_, chg_count_.p, chg_start_.p);
+        k_chg_scatter<<<div_up(m, 256), 256, 0, s>>>(m, chg_key_.p, chg_start_.p, chg_fill_.p, chg_bucket_.p);
+        const float ccut = (float)(std::sqrt((double)cs.pc.dh_rc2) + skin) * 1.0001f + 1e-4f;
+        k_chg_rows<<<div_up((int64_t)m * 32, 128), 128, 0, s>>>(
+            m, chg_idx_.p, chg_key_.p, xq_.p, charged_cells_[0], charged_cells_[1], charged_cells_[2], box_,
+            inv_box_, ccut * ccut, chg_start_.p, chg_bucket_.p, ex_csr_.p, ex_j_.p, ex_bits_.p, chg_rows_.p,
+            chg_len_.p, (int)chg_row_cap_, chg_stats_.p, flags_.p);
+    }
 }
 
 void PlainContext::launch_forces(cudaStream_t s, bool energy, uint32_t slots_enabled, int) {
@@ -1043,14 +1263,27 @@ void PlainContext::launch_forces(cudaStream_t s, bool energy, uint32_t slots_ena
     const int pair_slots[4] = {kSlotEXV, kSlotDH, kSlotLJR, kSlotLJA};
     for (int t = 0; t < 4; ++t)
         if (!(slots_enabled & (1u << pair_slots[t]))) excl_all |= 1u << t;
+    if (charged_split_) {
+        // the tiles leave Debye-Hueckel to the charged-pair list
+        excl_all |= kTermDH;
+        a.pc.list_rc2 = (float)(tile_cutoff_ * tile_cutoff_);
+    }
     a.excl_all = excl_all;
+    a.xq = xq_.p;
+    a.p0 = p0_.p;
+    a.chg_idx = chg_idx_.p;
+    a.chg_rows = chg_rows_.p;
+    a.chg_len = chg_len_.p;
+    a.n_chg = (int)n_charged_;
+    a.chg_row_cap = (int)chg_row_cap_;
+    a.blocks_chg = charged_split_ ? (int)std::max<int64_t>(1, div_up(n_charged_, kWarpsPerForceBlock)) : 0;
     a.energy = energy_.p;
     int blocks_tiles = a.blocks_tiles;
     if ((cs.pc.terms & ~excl_all & 15) == 0) {
         a.blocks_tiles = 0;
         blocks_tiles = 0;
     }
-    const int grid = blocks_tiles + a.blocks_bonds + a.blocks_angles + a.blocks_dih;
+    const int grid = blocks_tiles + a.blocks_bonds + a.blocks_angles + a.blocks_dih + a.blocks_chg;
     if (grid == 0) return;
     const int terms = cs.pc.terms;
     const bool per = cs.periodic;
@@ -1092,7 +1325,9 @@ void PlainContext::ensure_capacity() {
     for (int attempt = 0; attempt < 8; ++attempt) {
         OCM_CK(cudaMemsetAsync(flags_.p, 0, sizeof(int32_t), stream_));
         rebuild(stream_);
-        int32_t total = 0, masks = 0, flags = 0;
+        int32_t total = 0, masks = 0, flags = 0, chg[2] = {0, 0};
+        if (charged_split_)
+            OCM_CK(cudaMemcpyAsync(chg, chg_stats_.p, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
         OCM_CK(cudaMemcpyAsync(&total, tile_start_.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
         OCM_CK(cudaMemcpyAsync(&masks, mask_count_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
         OCM_CK(cudaMemcpyAsync(&flags, flags_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
@@ -1120,10 +1355,22 @@ void PlainContext::ensure_capacity() {
                 clear_graphs();
             }
         }
-        if (!realloced && !(flags & (ListFlags::kTileOverflow | ListFlags::kMaskOverflow)) &&
-            total <= tile_cap_ && masks <= mask_cap_) {
+        if (charged_split_ && ((int64_t)chg[0] * 5 / 4 + 16 > chg_row_cap_)) {
+            // rows with 25% headroom, a multiple of 32 entries
+            const int64_t want = ((int64_t)chg[0] * 3 / 2 + 32 + 31) / 32 * 32;
+            if (want > chg_row_cap_) {
+                chg_row_cap_ = want;
+                chg_rows_.alloc(n_charged_ * chg_row_cap_);
+                realloced = true;
+                clear_graphs();
+            }
+        }
+        if (!realloced &&
+            !(flags & (ListFlags::kTileOverflow | ListFlags::kMaskOverflow | ListFlags::kChargedOverflow)) &&
+            total <= tile_cap_ && masks <= mask_cap_ && chg[0] <= chg_row_cap_) {
             tiles_last = total;
             masked_last = masks;
+            charged_last_ = chg[1] / 2;
             list_builds++;
             return;
         }
@@ -1260,6 +1507,10 @@ void PlainContext::step(int64_t nsteps) {
                 throw Error(7, "[error] particles moved more than half the skin in one step");
             rebuild_interval = std::max(1, rebuild_interval / 2);
         }
+        if (flags & ListFlags::kChargedOverflow) {
+            chg_row_cap_ *= 2;
+            chg_rows_.alloc(n_charged_ * chg_row_cap_);
+        }
         if (flags & (ListFlags::kTileOverflow | ListFlags::kMaskOverflow)) {
             tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, tile_cap_ * 2);
             tile_j_.alloc(tile_cap_);
@@ -1277,6 +1528,27 @@ void PlainContext::set_list_options(int32_t interval, double sk) {
     if (interval < 0 || sk < 0) throw Error(1, "[error] invalid list options");
     if (interval > 0) rebuild_interval = interval;
     if (sk > 0) skin = sk;
+    setup_charged_cells();  // cells must stay at least cutoff + skin wide
+    clear_graphs();
+}
+
+void PlainContext::setup_charged_cells() {
+    if (!charged_split_) return;
+    const double cell = (std::sqrt((double)cs.pc.dh_rc2) + skin) * 1.0001 + 1e-4;
+    int dims[3];
+    for (int a = 0; a < 3; ++a) dims[a] = (int)std::min(1023.0, std::floor(cs.box[a] / cell));
+    if (dims[0] < 3 || dims[1] < 3 || dims[2] < 3) {
+        // box too narrow for a 27-cell neighbourhood: back to one tile list
+        charged_split_ = false;
+        tile_cutoff_ = cs.max_cutoff;
+        clear_graphs();
+        return;
+    }
+    for (int a = 0; a < 3; ++a) charged_cells_[a] = dims[a];
+    n_charged_cells_ = (int64_t)dims[0] * dims[1] * dims[2];
+    chg_count_.alloc(n_charged_cells_);
+    chg_start_.alloc(n_charged_cells_ + 1);
+    chg_fill_.alloc(n_charged_cells_);
     clear_graphs();
 }
 
@@ -1290,14 +1562,20 @@ void PlainContext::list_pairs(int64_t* out, int64_t cap, int64_t* n_out) {
     cnt.alloc(1);
     OCM_CK(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), stream_));
     const int wblocks = div_up(nc * 32, 128);
+    const float tile_rc2 = charged_split_ ? (float)(tile_cutoff_ * tile_cutoff_) : cs.pc.list_rc2;
     if (cs.periodic)
         k_list_pairs<true><<<wblocks, 128, 0, stream_>>>((int)nc, xs_.p, perm_.p, tile_start_.p,
-                                                        tile_j_.p, box_, inv_box_, cs.pc.list_rc2,
+                                                        tile_j_.p, box_, inv_box_, tile_rc2,
                                                         buf.p, cap, cnt.p, tile_cap_);
     else
         k_list_pairs<false><<<wblocks, 128, 0, stream_>>>((int)nc, xs_.p, perm_.p, tile_start_.p,
-                                                         tile_j_.p, box_, inv_box_, cs.pc.list_rc2,
+                                                         tile_j_.p, box_, inv_box_, tile_rc2,
                                                          buf.p, cap, cnt.p, tile_cap_);
+    if (charged_split_)
+        k_chg_list_pairs<<<(int)n_charged_, 128, 0, stream_>>>(
+            (int)n_charged_, chg_idx_.p, chg_rows_.p, chg_len_.p, (int)chg_row_cap_, xq_.p, box_, inv_box_,
+            cs.pc.dh_rc2, buf.p, cap,
+            cnt.p);
     OCM_CK(cudaGetLastError());
     unsigned long long c = 0;
     OCM_CK(cudaMemcpyAsync(&c, cnt.p, sizeof(c), cudaMemcpyDeviceToHost, stream_));

@@ -29,7 +29,12 @@ def test_every_declared_symbol_is_exported():
 
 
 def test_abi_version_and_device_count():
-    assert ocm.lib.ocm_abi_version() == 1
+    """The library reports the version the header declares (bumped whenever
+    a struct or signature of the header changes)."""
+    import re
+    header = (Path(__file__).resolve().parents[1] / "include" / "ocm.h").read_text()
+    declared = int(re.search(r"#define OCM_ABI_VERSION (\d+)", header).group(1))
+    assert ocm.lib.ocm_abi_version() == declared == 2
     assert ocm.device_count() >= 0
 
 

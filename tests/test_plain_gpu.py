@@ -64,14 +64,18 @@ def test_hps_slab_forces_energies(gpu, chains, length, box, seed):
     assert rel_force_err(f, f_ref) <= FORCE_TOL
     _check_energies(e_ref, _group_energy_map(system, ctx.getGroupEnergies()))
     assert ctx.stats()["reordered"] == int(spec.n > 2048)
+    assert ctx.stats()["charged_split"] == int(spec.n > 2048)  # DH on its own charged-pair list
 
 
-def test_group_masks(gpu):
+@pytest.mark.parametrize("kind", ["go", "hps"])
+def test_group_masks(gpu, kind):
     """getState(groups=1<<g) returns exactly that group's forces and energy
-    (Observer.cpp:339-341 queries one group at a time)."""
+    (Observer.cpp:339-341 queries one group at a time); the HPS slab case
+    runs Debye-Hueckel on the separate charged-pair list."""
     from opencafemol_gb300 import synth
     from oracle import oracle
-    spec = synth.go_protein(200, 9)
+    spec = (synth.go_protein(200, 9) if kind == "go"
+            else synth.hps_slab(30, 100, (15.0, 15.0, 60.0), slab_width=20.0, seed=8))
     system, ctx = _ctx(gpu, spec)
     _, e_ref = oracle.evaluate(spec)
     total_f = np.zeros((spec.n, 3))
@@ -84,20 +88,35 @@ def test_group_masks(gpu):
 
 
 def test_pair_set_bit_exact(gpu):
-    """The pairs the tile list makes the kernel test within the largest
-    cutoff equal a brute-force FP32 enumeration with the same r^2 formula."""
+    """The pairs the tile list makes the kernel test within the cutoff the
+    tiles serve equal a brute-force FP32 enumeration with the same r^2
+    formula; with a separate charged-pair list (Debye-Hueckel cutoff well
+    above the others) its pairs equal the charged pairs within the
+    Debye-Hueckel cutoff that its exclusions keep."""
+    from collections import Counter
+
     from opencafemol_gb300 import synth
-    spec = synth.hps_slab(30, 100, (15.0, 15.0, 60.0), slab_width=20.0, seed=6)
+    chain_len = 100
+    spec = synth.hps_slab(30, chain_len, (15.0, 15.0, 60.0), slab_width=20.0, seed=6)
     system, ctx = _ctx(gpu, spec)
-    pairs = ctx.list_pairs()
-    got = set(map(tuple, pairs.tolist()))
-    assert len(got) == len(pairs), "a pair was evaluated twice"
-    rc = ctx.stats()["max_cutoff"]
-    ref = brute_force_pairs(spec.pos, spec.box, rc)
+    pairs = ctx.list_pairs()  # builds the lists
+    st = ctx.stats()
+    assert st["charged_split"] == 1  # DH 3.5 nm against a 2.0 nm HPS cutoff
+    assert st["tile_cutoff"] < st["max_cutoff"]
+    got = Counter(map(tuple, pairs.tolist()))
+    ref = Counter(brute_force_pairs(spec.pos, spec.box, st["tile_cutoff"]))
+    q = spec.dh.p0
+    charged = ~np.isnan(q) & (np.nan_to_num(q) != 0)
+    dh_excluded = lambda i, j: i // chain_len == j // chain_len and abs(i - j) <= 3  # ign_bond=3
+    chg = {(i, j) for i, j in brute_force_pairs(spec.pos, spec.box, st["max_cutoff"], mask=charged)
+           if not dh_excluded(i, j)}
+    assert len(chg) > 1000 and st["charged_pairs"] >= len(chg)
+    ref.update(chg)
+    assert max(got.values()) <= 2, "a pair was evaluated more than once per list"
     assert got == ref
 
 
-def brute_force_pairs(pos, box, rc):
+def brute_force_pairs(pos, box, rc, mask=None):
     L = np.asarray(box, np.float64)
     x = np.asarray(pos, np.float64)
     w = x - L * np.floor(x * (1.0 / L))
@@ -107,13 +126,18 @@ def brute_force_pairs(pos, box, rc):
     out = set()
     n = len(xf)
     for i in range(n - 1):
+        if mask is not None and not mask[i]:
+            continue
         d = xf[i + 1:] - xf[i]
         d = (d - Lf * np.rint(d * iLf)).astype(np.float32)  # separate rounding, equals the fma result
         # emulate fmaf(dz,dz,fmaf(dy,dy,dx*dx)) exactly in float64 then round once per fma
         dx2 = (d[:, 0] * d[:, 0]).astype(np.float32)
         s1 = (d[:, 1].astype(np.float64) * d[:, 1] + dx2).astype(np.float32)
         r2 = (d[:, 2].astype(np.float64) * d[:, 2] + s1).astype(np.float32)
-        for j in np.nonzero(r2 < rc2)[0]:
+        hit = r2 < rc2
+        if mask is not None:
+            hit &= mask[i + 1:]
+        for j in np.nonzero(hit)[0]:
             out.add((i, i + 1 + int(j)))
     return out
 
