@@ -91,6 +91,7 @@ class PlainContext {
     cudaGraphExec_t graph_for(int chunk);
     void clear_graphs();
     void setup_charged_cells();
+    void setup_columns(double width);
     void eval(uint32_t groups, bool energy, double* forces, double* slot_energy);
     uint32_t slots_for_groups(uint32_t groups) const;
     void check_positions_set() const;
@@ -129,9 +130,9 @@ class PlainContext {
     DevBuf<int32_t> tile_count_, tile_start_, tile_j_, tile_mask_;
     DevBuf<uint32_t> masks_;
     DevBuf<int32_t> mask_count_;
-    // cell sort
-    DevBuf<uint32_t> cell_rank_;
-    DevBuf<int32_t> cell_key_, cell_count_, cell_start_, cell_fill_, bucket_;
+    // cluster order: columns in x-y, each sorted along z in thin slices
+    double col_wmin_ = 1.0;
+    DevBuf<int32_t> cell_key_, cell_count_, cell_start_, cell_fill_, bucket_, col_slots_, col_start_;
     // exclusions
     DevBuf<int32_t> ex_start_, ex_j_;
     DevBuf<uint8_t> ex_bits_;

@@ -50,17 +50,26 @@ __device__ __forceinline__ double warp_sum(double v) {
 // Rebuild kernels
 // ---------------------------------------------------------------------------
 __global__ void k_cell_keys(int n, const float4* __restrict__ xq, int nx, int ny, int nz,
-                            float3 box, const uint32_t* __restrict__ cell_rank,
-                            int32_t* __restrict__ key, int32_t* __restrict__ count) {
+                            float3 box, int32_t* __restrict__ key, int32_t* __restrict__ count) {
+    // cell = (column, z slice); cells of one column are consecutive
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 p = xq[i];
     const int cx = min(nx - 1, max(0, (int)(p.x * ((float)nx / box.x))));
     const int cy = min(ny - 1, max(0, (int)(p.y * ((float)ny / box.y))));
     const int cz = min(nz - 1, max(0, (int)(p.z * ((float)nz / box.z))));
-    const int k = (int)cell_rank[(cz * ny + cy) * nx + cx];
+    const int k = (cy * nx + cx) * nz + cz;
     key[i] = k;
     atomicAdd(&count[k], 1);
+}
+
+// Slots of each column: its bead count rounded up to whole clusters.
+__global__ void k_col_slots(int ncols, int nz, const int32_t* __restrict__ cell_start,
+                            int32_t* __restrict__ col_slots) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    const int beads = cell_start[(c + 1) * nz] - cell_start[c * nz];
+    col_slots[c] = (beads + 31) & ~31;
 }
 
 // Exclusive scan of m ints into out[0..m] by one block of 1024 threads.
@@ -100,19 +109,24 @@ __global__ void k_bucket_scatter(int n, const int32_t* __restrict__ key,
 
 // Order each cell's members by particle index: the result is the unique
 // stable order (Morton rank, index), independent of atomic timing.
-__global__ void k_bucket_sort(int n_cells, const int32_t* __restrict__ start,
-                              const int32_t* __restrict__ bucket, int32_t* __restrict__ perm) {
+// Cluster order: columns one after another (each padded to whole clusters),
+// inside a column the z slices bottom-up, inside a slice ascending index.
+__global__ void k_bucket_sort(int n_cells, int nz, const int32_t* __restrict__ start,
+                              const int32_t* __restrict__ col_start, const int32_t* __restrict__ bucket,
+                              int32_t* __restrict__ perm) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_cells) return;
-    const int b = start[c], e = start[c + 1];
-    for (int i = b; i < e; ++i) {
-        const int v = bucket[i];
+    const int col = c / nz;
+    const int b = start[c], m = start[c + 1] - b;
+    int32_t* out = perm + col_start[col] + (b - start[col * nz]);
+    for (int i = 0; i < m; ++i) {
+        const int v = bucket[b + i];
         int j = i - 1;
-        while (j >= b && perm[j] > v) {
-            perm[j + 1] = perm[j];
+        while (j >= 0 && out[j] > v) {
+            out[j + 1] = out[j];
             --j;
         }
-        perm[j + 1] = v;
+        out[j + 1] = v;
     }
 }
 
@@ -156,6 +170,7 @@ __global__ void k_bbox(int nc, const float4* __restrict__ xs, const int32_t* __r
     float3 d = make_float3(0.f, 0.f, 0.f);
     if (valid) d = separation<PERIODIC>(base, xs[I * 32 + lane], box, inv_box);
     float lx = d.x, ly = d.y, lz = d.z, hx = d.x, hy = d.y, hz = d.z;
+    const bool any = __ballot_sync(kFull, valid) != 0u;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         lx = fminf(lx, __shfl_xor_sync(kFull, lx, o));
@@ -168,7 +183,8 @@ __global__ void k_bbox(int nc, const float4* __restrict__ xs, const int32_t* __r
     if (lane == 0) {
         bc[I] = make_float4(base.x + 0.5f * (lx + hx), base.y + 0.5f * (ly + hy),
                             base.z + 0.5f * (lz + hz), 0.f);
-        bh[I] = make_float4(0.5f * (hx - lx), 0.5f * (hy - ly), 0.5f * (hz - lz), 0.f);
+        // w < 0 marks a cluster of padding slots only
+        bh[I] = make_float4(0.5f * (hx - lx), 0.5f * (hy - ly), 0.5f * (hz - lz), any ? 0.f : -1.f);
     }
 }
 
@@ -209,10 +225,13 @@ __global__ void k_tiles(int nc, const float4* __restrict__ bc, const float4* __r
     }
     const float4 ci = bc[I], hi = bh[I];
     int pos = FILL ? start[I] : 0;
-    for (int J0 = I; J0 < nc; J0 += 32) {
+    for (int J0 = I; J0 < nc && hi.w >= 0.f; J0 += 32) {
         const int J = J0 + lane;
         bool ok = false;
-        if (J < nc) ok = boxes_close<PERIODIC>(ci, hi, bc[J], bh[J], box, inv_box, cut, cut2);
+        if (J < nc) {
+            const float4 hj = bh[J];
+            ok = hj.w >= 0.f && boxes_close<PERIODIC>(ci, hi, bc[J], hj, box, inv_box, cut, cut2);
+        }
         const unsigned b = __ballot_sync(kFull, ok);
         if (FILL && ok) {
             const int at = pos + __popc(b & ((1u << lane) - 1u));
@@ -887,15 +906,6 @@ void launch_forces_t(const ForceArgs& a, int grid, cudaStream_t s, bool periodic
     }
 }
 
-uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
-    auto spread = [](uint32_t v) {
-        uint32_t r = 0;
-        for (int b = 0; b < 10; ++b) r |= ((v >> b) & 1u) << (3 * b);
-        return r;
-    };
-    return spread(x) | (spread(y) << 1) | (spread(z) << 2);
-}
-
 inline int div_up(int64_t a, int b) { return (int)((a + b - 1) / b); }
 
 }  // namespace
@@ -919,8 +929,6 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
     n = cs.n;
     if (n <= 0) throw Error(1, "[error] system has no particles");
     if (n > (1 << 27)) throw Error(6, "[error] system too large");
-    np = ((n + 31) / 32) * 32;
-    nc = np / 32;
     OCM_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     OCM_CK(cudaMallocHost(&h_flags_, 16 * sizeof(int32_t)));
 
@@ -940,6 +948,16 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
                            cs.box[1] > 0 ? (float)(1.0 / cs.box[1]) : 0.f,
                            cs.box[2] > 0 ? (float)(1.0 / cs.box[2]) : 0.f);
     reorder = cs.periodic && n > 2048;
+    np = ((n + 31) / 32) * 32;
+    if (reorder) {
+        // Columns at least this wide number at most n / 32, so the padding of
+        // each column to whole clusters at most doubles the slots.
+        col_wmin_ = std::max(1.0, std::sqrt(cs.box[0] * cs.box[1] * 32.0 / (double)n));
+        const int64_t max_cols = (int64_t)std::max(1.0, std::floor(cs.box[0] / col_wmin_)) *
+                                 (int64_t)std::max(1.0, std::floor(cs.box[1] / col_wmin_));
+        np += 32 * max_cols;
+    }
+    nc = np / 32;
 
     cudaStream_t s = stream_;
     x_.alloc(n); y_.alloc(n); z_.alloc(n);
@@ -978,26 +996,9 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
     mask_count_.alloc(1);
 
     if (reorder) {
-        // Cells of ~1 nm tiling the box; visiting order = Morton rank.
-        for (int a = 0; a < 3; ++a)
-            cell_dims_[a] = (int)std::max(1.0, std::min(1023.0, std::floor(cs.box[a] / 1.0)));
-        n_cells_ = (int64_t)cell_dims_[0] * cell_dims_[1] * cell_dims_[2];
-        std::vector<std::pair<uint32_t, uint32_t>> codes(n_cells_);
-        for (int cz = 0; cz < cell_dims_[2]; ++cz)
-            for (int cy = 0; cy < cell_dims_[1]; ++cy)
-                for (int cx = 0; cx < cell_dims_[0]; ++cx) {
-                    const uint32_t c = (uint32_t)((cz * cell_dims_[1] + cy) * cell_dims_[0] + cx);
-                    codes[c] = {morton3(cx, cy, cz), c};
-                }
-        std::sort(codes.begin(), codes.end());
-        std::vector<uint32_t> rank(n_cells_);
-        for (int64_t k = 0; k < n_cells_; ++k) rank[codes[k].second] = (uint32_t)k;
-        cell_rank_.upload(rank, s);
         cell_key_.alloc(n);
-        cell_count_.alloc(n_cells_);
-        cell_start_.alloc(n_cells_ + 1);
-        cell_fill_.alloc(n_cells_);
         bucket_.alloc(n);
+        setup_columns(std::max(col_wmin_, 2.5));  // until positions give the density
     }
     // exclusions (CSR -> flat (i, j, bits))
     {
@@ -1087,6 +1088,27 @@ void PlainContext::set_positions(const double* xyz) {
         if (!std::isfinite(a[i]) || !std::isfinite(b[i]) || !std::isfinite(c[i]))
             throw Error(7, "[error] non-finite position for particle " + std::to_string(i));
     }
+    if (reorder) {
+        // Bead density over the occupied 1 nm cells sets the column width:
+        // clusters of 32 beads then come out about as tall as wide.
+        int g[3];
+        for (int k = 0; k < 3; ++k) g[k] = (int)std::max(1.0, std::min(1024.0, std::floor(cs.box[k])));
+        std::vector<int64_t> cells(n);
+        const double* v[3] = {a.data(), b.data(), c.data()};
+        for (int64_t i = 0; i < n; ++i) {
+            int64_t key = 0;
+            for (int k = 0; k < 3; ++k) {
+                const double w = v[k][i] - cs.box[k] * std::floor(v[k][i] / cs.box[k]);
+                key = key * 1024 + std::min<int64_t>(g[k] - 1, std::max<int64_t>(0, (int64_t)(w * g[k] / cs.box[k])));
+            }
+            cells[i] = key;
+        }
+        std::sort(cells.begin(), cells.end());
+        const int64_t occupied = std::unique(cells.begin(), cells.end()) - cells.begin();
+        const double cell_vol = cs.box[0] * cs.box[1] * cs.box[2] / ((double)g[0] * g[1] * g[2]);
+        const double density = (double)n / ((double)occupied * cell_vol);
+        setup_columns(1.2 * std::cbrt(32.0 / density));
+    }
     x_.upload(a, stream_);
     y_.upload(b, stream_);
     z_.upload(c, stream_);
@@ -1165,16 +1187,19 @@ double PlainContext::kinetic_energy() {
 void PlainContext::rebuild(cudaStream_t s) {
     const int np_i = (int)np, n_i = (int)n, nc_i = (int)nc;
     if (reorder) {
+        const int ncols = cell_dims_[0] * cell_dims_[1];
         OCM_CK(cudaMemsetAsync(cell_count_.p, 0, n_cells_ * sizeof(int32_t), s));
         OCM_CK(cudaMemsetAsync(cell_fill_.p, 0, n_cells_ * sizeof(int32_t), s));
+        OCM_CK(cudaMemsetAsync(perm_.p, 0xff, np * sizeof(int32_t), s));
         k_cell_keys<<<div_up(n, 256), 256, 0, s>>>(n_i, xq_.p, cell_dims_[0], cell_dims_[1],
-                                                   cell_dims_[2], box_, cell_rank_.p, cell_key_.p,
-                                                   cell_count_.p);
+                                                   cell_dims_[2], box_, cell_key_.p, cell_count_.p);
         k_scan<<<1, 1024, 0, s>>>((int)n_cells_, cell_count_.p, cell_start_.p);
+        k_col_slots<<<div_up(ncols, 256), 256, 0, s>>>(ncols, cell_dims_[2], cell_start_.p, col_slots_.p);
+        k_scan<<<1, 1024, 0, s>>>(ncols, col_slots_.p, col_start_.p);
         k_bucket_scatter<<<div_up(n, 256), 256, 0, s>>>(n_i, cell_key_.p, cell_start_.p,
                                                         cell_fill_.p, bucket_.p);
-        k_bucket_sort<<<div_up(n_cells_, 128), 128, 0, s>>>((int)n_cells_, cell_start_.p,
-                                                           bucket_.p, perm_.p);
+        k_bucket_sort<<<div_up(n_cells_, 128), 128, 0, s>>>((int)n_cells_, cell_dims_[2], cell_start_.p,
+                                                           col_start_.p, bucket_.p, perm_.p);
     }
     k_gather_sorted<<<div_up(np, 256), 256, 0, s>>>(np_i, perm_.p, xq_.p, p0_.p, p1_.p, lab_.p,
                                                     slot_.p, xs_.p, p0s_.p, p1s_.p, labs_.p,
@@ -1529,6 +1554,26 @@ void PlainContext::set_list_options(int32_t interval, double sk) {
     if (interval > 0) rebuild_interval = interval;
     if (sk > 0) skin = sk;
     setup_charged_cells();  // cells must stay at least cutoff + skin wide
+    clear_graphs();
+}
+
+void PlainContext::setup_columns(double width) {
+    // Columns of about `width` in x and y, z slices of 0.25 nm (fewer when
+    // the cells would outnumber the beads four to one).
+    width = std::max(width, col_wmin_);
+    int dims[3];
+    for (int a = 0; a < 2; ++a) dims[a] = (int)std::max(1.0, std::min(1023.0, std::floor(cs.box[a] / width)));
+    const int64_t ncols = (int64_t)dims[0] * dims[1];
+    const int64_t zmax = std::max<int64_t>(1, std::max<int64_t>(4 * n, 65536) / ncols);
+    dims[2] = (int)std::max<int64_t>(1, std::min<int64_t>(zmax, (int64_t)std::floor(cs.box[2] / 0.25)));
+    if (dims[0] == cell_dims_[0] && dims[1] == cell_dims_[1] && dims[2] == cell_dims_[2] && n_cells_ > 0) return;
+    for (int a = 0; a < 3; ++a) cell_dims_[a] = dims[a];
+    n_cells_ = ncols * dims[2];
+    cell_count_.alloc(n_cells_);
+    cell_start_.alloc(n_cells_ + 1);
+    cell_fill_.alloc(n_cells_);
+    col_slots_.alloc(ncols);
+    col_start_.alloc(ncols + 1);
     clear_graphs();
 }
 

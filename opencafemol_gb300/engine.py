@@ -99,11 +99,19 @@ class Context:
                 raise
 
     def cluster_order(self) -> np.ndarray:
+        """Bead index of every cluster slot (-1 for padding slots)."""
         n = C.c_int64()
         cap = self.n + 64
-        out = np.zeros(cap, np.int64)
-        check(lib.ocm_context_cluster_order(self._h, i64ptr(out), cap, C.byref(n)))
-        return out[: n.value].copy()
+        while True:
+            out = np.zeros(cap, np.int64)
+            try:
+                check(lib.ocm_context_cluster_order(self._h, i64ptr(out), cap, C.byref(n)))
+                return out[: n.value].copy()
+            except OCMError:
+                if n.value > cap:
+                    cap = n.value
+                    continue
+                raise
 
 
 class Batch:

@@ -142,7 +142,10 @@ def brute_force_pairs(pos, box, rc, mask=None):
     return out
 
 
-def test_morton_order_deterministic(gpu):
+def test_cluster_order_deterministic(gpu):
+    """Clusters are 32 consecutive beads of one x-y column sorted along z;
+    the order is reproducible, covers every bead once, and each cluster's
+    padding slots (a column's last cluster) come after its beads."""
     from opencafemol_gb300 import synth
     spec = synth.hps_slab(30, 100, (15.0, 15.0, 60.0), slab_width=20.0, seed=6)
     _, c1 = _ctx(gpu, spec)
@@ -151,6 +154,15 @@ def test_morton_order_deterministic(gpu):
     assert np.array_equal(o1, o2)
     real = o1[o1 >= 0]
     assert np.array_equal(np.sort(real), np.arange(spec.n))
+    cl = o1.reshape(-1, 32)
+    for row in cl:
+        valid = row >= 0
+        assert not np.any(valid[1:] & ~valid[:-1])
+    # compact clusters: every full cluster spans far less than the box
+    x = spec.pos - np.asarray(spec.box) * np.floor(spec.pos / np.asarray(spec.box))
+    full = cl[(cl >= 0).all(axis=1)]
+    ext = np.array([np.ptp(x[r], axis=0) for r in full])
+    assert np.median(ext[:, 2]) < 4.0
 
 
 def test_langevin_one_step(gpu):
