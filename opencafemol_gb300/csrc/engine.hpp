@@ -128,16 +128,19 @@ class PlainContext {
     DevBuf<uint32_t> labs_;
     DevBuf<float4> bb_c_, bb_h_;
     DevBuf<int32_t> tile_count_, tile_start_, tile_j_, tile_mask_;
+    DevBuf<int32_t> raw_start_, raw_i_, raw_j_;  // candidate tiles before pruning
+    DevBuf<uint8_t> keep_;
     DevBuf<uint32_t> masks_;
     DevBuf<int32_t> mask_count_;
     // cluster order: columns in x-y, each sorted along z in thin slices
     double col_wmin_ = 1.0;
-    DevBuf<int32_t> cell_key_, cell_count_, cell_start_, cell_fill_, bucket_, col_slots_, col_start_;
+    DevBuf<int32_t> cell_key_, cell_count_, cell_start_, cell_fill_, bucket_, col_start_;
     // exclusions
     DevBuf<int32_t> ex_start_, ex_j_;
     DevBuf<uint8_t> ex_bits_;
     // charged-pair list
-    DevBuf<int32_t> chg_idx_, chg_key_, chg_count_, chg_start_, chg_fill_, chg_bucket_;
+    DevBuf<int32_t> chg_idx_, chg_key_, chg_count_, chg_start_, chg_fill_;
+    DevBuf<float4> chg_sorted_;  // charged beads by cell: x, y, z, index bits
     DevBuf<int32_t> chg_rows_, chg_len_, chg_stats_;  // rows, row lengths, {longest, entries}
     DevBuf<int32_t> ex_csr_;  // per-bead start of its exclusion row (n + 1)
     // bonded

@@ -63,15 +63,6 @@ __global__ void k_cell_keys(int n, const float4* __restrict__ xq, int nx, int ny
     atomicAdd(&count[k], 1);
 }
 
-// Slots of each column: its bead count rounded up to whole clusters.
-__global__ void k_col_slots(int ncols, int nz, const int32_t* __restrict__ cell_start,
-                            int32_t* __restrict__ col_slots) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncols) return;
-    const int beads = cell_start[(c + 1) * nz] - cell_start[c * nz];
-    col_slots[c] = (beads + 31) & ~31;
-}
-
 // Exclusive scan of m ints into out[0..m] by one block of 1024 threads.
 __global__ void __launch_bounds__(1024) k_scan(int m, const int32_t* __restrict__ in,
                                                int32_t* __restrict__ out) {
@@ -98,6 +89,33 @@ __global__ void __launch_bounds__(1024) k_scan(int m, const int32_t* __restrict_
     if (t == 1023) out[m] = part[1023];
 }
 
+// Start slot of every column (exclusive scan of its bead count rounded up to
+// whole clusters), one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_col_scan(int ncols, int nz, const int32_t* __restrict__ cell_start,
+                                                   int32_t* __restrict__ col_start) {
+    __shared__ int32_t part[1024];
+    const int t = threadIdx.x;
+    const int per = (ncols + 1023) / 1024;
+    const int b = t * per, e = min(ncols, b + per);
+    auto slots = [&](int c) { return (cell_start[(c + 1) * nz] - cell_start[c * nz] + 31) & ~31; };
+    int32_t s = 0;
+    for (int c = b; c < e; ++c) s += slots(c);
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int32_t v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int32_t run = part[t] - s;
+    for (int c = b; c < e; ++c) {
+        col_start[c] = run;
+        run += slots(c);
+    }
+    if (t == 1023) col_start[ncols] = part[1023];
+}
+
 __global__ void k_bucket_scatter(int n, const int32_t* __restrict__ key,
                                  const int32_t* __restrict__ start, int32_t* __restrict__ fill,
                                  int32_t* __restrict__ bucket) {
@@ -107,27 +125,20 @@ __global__ void k_bucket_scatter(int n, const int32_t* __restrict__ key,
     bucket[start[k] + atomicAdd(&fill[k], 1)] = i;
 }
 
-// Order each cell's members by particle index: the result is the unique
-// stable order (Morton rank, index), independent of atomic timing.
 // Cluster order: columns one after another (each padded to whole clusters),
 // inside a column the z slices bottom-up, inside a slice ascending index.
-__global__ void k_bucket_sort(int n_cells, int nz, const int32_t* __restrict__ start,
-                              const int32_t* __restrict__ col_start, const int32_t* __restrict__ bucket,
-                              int32_t* __restrict__ perm) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_cells) return;
-    const int col = c / nz;
-    const int b = start[c], m = start[c + 1] - b;
-    int32_t* out = perm + col_start[col] + (b - start[col * nz]);
-    for (int i = 0; i < m; ++i) {
-        const int v = bucket[b + i];
-        int j = i - 1;
-        while (j >= 0 && out[j] > v) {
-            out[j + 1] = out[j];
-            --j;
-        }
-        out[j + 1] = v;
-    }
+// One thread per bead ranks it among its cell's members by index, so the
+// order does not depend on the atomic timing of the scatter.
+__global__ void k_bucket_rank(int n, int nz, const int32_t* __restrict__ key,
+                              const int32_t* __restrict__ start, const int32_t* __restrict__ col_start,
+                              const int32_t* __restrict__ bucket, int32_t* __restrict__ perm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = key[i], col = c / nz;
+    const int b = start[c], e = start[c + 1];
+    int rank = 0;
+    for (int q = b; q < e; ++q) rank += bucket[q] < i;
+    perm[col_start[col] + (b - start[col * nz]) + rank] = i;
 }
 
 __global__ void k_gather_sorted(int np, const int32_t* __restrict__ perm,
@@ -214,7 +225,7 @@ template <bool PERIODIC, bool FILL>
 __global__ void k_tiles(int nc, const float4* __restrict__ bc, const float4* __restrict__ bh,
                         float3 box, float3 inv_box, float cut, float cut2,
                         int32_t* __restrict__ count, const int32_t* __restrict__ start,
-                        int32_t* __restrict__ tile_j, int32_t* __restrict__ tile_mask, int cap,
+                        int32_t* __restrict__ tile_i, int32_t* __restrict__ tile_j, int cap,
                         int32_t* __restrict__ flags) {
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -235,12 +246,63 @@ __global__ void k_tiles(int nc, const float4* __restrict__ bc, const float4* __r
         const unsigned b = __ballot_sync(kFull, ok);
         if (FILL && ok) {
             const int at = pos + __popc(b & ((1u << lane) - 1u));
+            tile_i[at] = I;
             tile_j[at] = J;
-            tile_mask[at] = -1;
         }
         pos += __popc(b);
     }
     if (!FILL && lane == 0) count[I] = pos;
+}
+
+// Pruning of the candidate tiles (bounding boxes within range): one warp
+// per candidate tile, lanes on the row cluster's beads, the column cluster's
+// beads broadcast one at a time; a tile is kept if any pair is within range
+// (the diagonal tile always).  kept_count[I] counts the kept tiles of row I.
+template <bool PERIODIC>
+__global__ void k_prune(int nc, const float4* __restrict__ xs, const int32_t* __restrict__ raw_start,
+                        const int32_t* __restrict__ raw_i, const int32_t* __restrict__ raw_j, int cap,
+                        float3 box, float3 inv_box, float cut2, uint8_t* __restrict__ keep_flag,
+                        int32_t* __restrict__ kept_count) {
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int total = raw_start[nc];
+    if (t >= total || total > cap) return;  // warp-uniform
+    const int I = raw_i[t], J = raw_j[t];
+    bool keep = I == J;
+    if (!keep) {
+        const float4 xi = xs[I * 32 + lane];
+        for (int k = 0; k < 32 && !keep; ++k) {
+            const float r2 = norm2(separation<PERIODIC>(xi, xs[J * 32 + k], box, inv_box));
+            keep = __ballot_sync(kFull, r2 < cut2) != 0u;
+        }
+    }
+    if (lane == 0) {
+        keep_flag[t] = keep ? 1 : 0;
+        if (keep) atomicAdd(&kept_count[I], 1);
+    }
+}
+
+// Kept tiles of every row, in their order, into the final list (exclusion
+// masks cleared): one warp per row, compacted by ballot.
+__global__ void k_compact_tiles(int nc, const int32_t* __restrict__ raw_start, const int32_t* __restrict__ raw_j,
+                                const uint8_t* __restrict__ keep_flag, int cap, const int32_t* __restrict__ start,
+                                int32_t* __restrict__ tile_j, int32_t* __restrict__ tile_mask) {
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (I >= nc || raw_start[nc] > cap) return;
+    const int r0 = raw_start[I], r1 = raw_start[I + 1];
+    int at = start[I];
+    for (int q0 = r0; q0 < r1; q0 += 32) {
+        const int q = q0 + lane;
+        const bool keep = q < r1 && keep_flag[q];
+        const unsigned b = __ballot_sync(kFull, keep);
+        if (keep) {
+            const int k = at + __popc(b & ((1u << lane) - 1u));
+            tile_j[k] = raw_j[q];
+            tile_mask[k] = -1;
+        }
+        at += __popc(b);
+    }
 }
 
 __device__ __forceinline__ int find_tile(const int32_t* __restrict__ start,
@@ -330,21 +392,26 @@ __global__ void k_chg_keys(int m, const int32_t* __restrict__ idx, const float4*
     atomicAdd(&count[k], 1);
 }
 
-__global__ void k_chg_scatter(int m, const int32_t* __restrict__ key, const int32_t* __restrict__ start,
-                              int32_t* __restrict__ fill, int32_t* __restrict__ bucket) {
+// Charged beads grouped by cell: position and bead index (in w) together,
+// so the row build reads one contiguous record per candidate.
+__global__ void k_chg_scatter(int m, const int32_t* __restrict__ idx, const int32_t* __restrict__ key,
+                              const float4* __restrict__ xq, const int32_t* __restrict__ start,
+                              int32_t* __restrict__ fill, float4* __restrict__ sorted) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= m) return;
-    const int k = key[t];
-    bucket[start[k] + atomicAdd(&fill[k], 1)] = t;
+    const int k = key[t], i = idx[t];
+    const float4 p = xq[i];
+    sorted[start[k] + atomicAdd(&fill[k], 1)] = make_float4(p.x, p.y, p.z, __int_as_float(i));
 }
 
-// One warp per charged bead: the 27 neighbour cells in a fixed order, 32
-// candidates at a time, kept partners compacted by ballot.  row_stats[0] is
-// the longest row, row_stats[1] the number of row entries.
+// One warp per charged bead: the 27 neighbour cells (the three cells of a
+// row along x as one range where they do not wrap), 32 candidates at a time,
+// kept partners compacted by ballot.  row_stats[0] is the longest row,
+// row_stats[1] the number of row entries.
 __global__ void k_chg_rows(int m, const int32_t* __restrict__ idx, const int32_t* __restrict__ key,
                            const float4* __restrict__ xq, int nx, int ny, int nz, float3 box,
                            float3 inv_box, float cut2, const int32_t* __restrict__ start,
-                           const int32_t* __restrict__ bucket, const int32_t* __restrict__ ex_csr,
+                           const float4* __restrict__ sorted, const int32_t* __restrict__ ex_csr,
                            const int32_t* __restrict__ ex_j, const uint8_t* __restrict__ ex_bits,
                            int32_t* __restrict__ rows, int32_t* __restrict__ row_len, int row_cap,
                            int32_t* __restrict__ row_stats, int32_t* flags) {
@@ -359,18 +426,21 @@ __global__ void k_chg_rows(int m, const int32_t* __restrict__ idx, const int32_t
     int32_t* row = rows + (size_t)t * row_cap;
     int len = 0;
     for (int dz = -1; dz <= 1; ++dz)
-        for (int dy = -1; dy <= 1; ++dy)
-            for (int dx = -1; dx <= 1; ++dx) {
-                const int c = (((cz + dz + nz) % nz) * ny + (cy + dy + ny) % ny) * nx + (cx + dx + nx) % nx;
-                const int q1 = start[c + 1];
-                for (int q0 = start[c]; q0 < q1; q0 += 32) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int r = (((cz + dz + nz) % nz) * ny + (cy + dy + ny) % ny) * nx;
+            const bool inner = cx > 0 && cx < nx - 1;
+            for (int seg = 0; seg < (inner ? 1 : 3); ++seg) {
+                const int q_begin = inner ? start[r + cx - 1] : start[r + (cx + seg - 1 + nx) % nx];
+                const int q_end = inner ? start[r + cx + 2] : start[r + (cx + seg - 1 + nx) % nx + 1];
+                for (int q0 = q_begin; q0 < q_end; q0 += 32) {
                     const int q = q0 + lane;
                     bool keep = false;
                     int j = 0;
-                    if (q < q1) {
-                        j = idx[bucket[q]];
+                    if (q < q_end) {
+                        const float4 c = sorted[q];
+                        j = __float_as_int(c.w);
                         if (j != i) {
-                            const float r2 = norm2(separation<true>(xi, xq[j], box, inv_box));
+                            const float r2 = norm2(separation<true>(xi, c, box, inv_box));
                             keep = r2 < cut2;
                             if (keep && e0 < e1) {
                                 int lo = e0, hi = e1;  // this row's exclusions, sorted by j
@@ -391,6 +461,7 @@ __global__ void k_chg_rows(int m, const int32_t* __restrict__ idx, const int32_t
                     len += __popc(bal);
                 }
             }
+        }
     if (lane == 0) {
         row_len[t] = len;
         atomicMax(&row_stats[0], len);
@@ -988,9 +1059,9 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
     }
     xs_.alloc(np); p0s_.alloc(np); p1s_.alloc(np); labs_.alloc(np);
     bb_c_.alloc(nc); bb_h_.alloc(nc);
-    tile_count_.alloc(nc); tile_start_.alloc(nc + 1);
+    tile_count_.alloc(nc); tile_start_.alloc(nc + 1); raw_start_.alloc(nc + 1);
     tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, std::max<int64_t>(4096, nc * 48));
-    tile_j_.alloc(tile_cap_); tile_mask_.alloc(tile_cap_);
+    tile_j_.alloc(tile_cap_); tile_mask_.alloc(tile_cap_); raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_);
     mask_cap_ = std::max<int64_t>(256, std::min<int64_t>(tile_cap_, nc * 8));
     masks_.alloc(mask_cap_ * 128);
     mask_count_.alloc(1);
@@ -1029,7 +1100,7 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
             n_charged_ = (int64_t)idx.size();
             chg_idx_.upload(idx, s);
             chg_key_.alloc(n_charged_);
-            chg_bucket_.alloc(n_charged_);
+            chg_sorted_.alloc(n_charged_);
             chg_len_.alloc(n_charged_);
             OCM_CK(cudaMemsetAsync(chg_len_.p, 0, n_charged_ * sizeof(int32_t), s));
             chg_stats_.alloc(2);
@@ -1194,12 +1265,11 @@ void PlainContext::rebuild(cudaStream_t s) {
         k_cell_keys<<<div_up(n, 256), 256, 0, s>>>(n_i, xq_.p, cell_dims_[0], cell_dims_[1],
                                                    cell_dims_[2], box_, cell_key_.p, cell_count_.p);
         k_scan<<<1, 1024, 0, s>>>((int)n_cells_, cell_count_.p, cell_start_.p);
-        k_col_slots<<<div_up(ncols, 256), 256, 0, s>>>(ncols, cell_dims_[2], cell_start_.p, col_slots_.p);
-        k_scan<<<1, 1024, 0, s>>>(ncols, col_slots_.p, col_start_.p);
+        k_col_scan<<<1, 1024, 0, s>>>(ncols, cell_dims_[2], cell_start_.p, col_start_.p);
         k_bucket_scatter<<<div_up(n, 256), 256, 0, s>>>(n_i, cell_key_.p, cell_start_.p,
                                                         cell_fill_.p, bucket_.p);
-        k_bucket_sort<<<div_up(n_cells_, 128), 128, 0, s>>>((int)n_cells_, cell_dims_[2], cell_start_.p,
-                                                           col_start_.p, bucket_.p, perm_.p);
+        k_bucket_rank<<<div_up(n, 256), 256, 0, s>>>(n_i, cell_dims_[2], cell_key_.p, cell_start_.p,
+                                                     col_start_.p, bucket_.p, perm_.p);
     }
     k_gather_sorted<<<div_up(np, 256), 256, 0, s>>>(np_i, perm_.p, xq_.p, p0_.p, p1_.p, lab_.p,
                                                     slot_.p, xs_.p, p0s_.p, p1s_.p, labs_.p,
@@ -1212,23 +1282,29 @@ void PlainContext::rebuild(cudaStream_t s) {
     const float cut2 = cut * cut;
     if (per) {
         k_tiles<true, false><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2,
-                                                     tile_count_.p, nullptr, nullptr, nullptr, 0,
-                                                     flags_.p);
+                                                     tile_count_.p, nullptr, nullptr, nullptr, 0, flags_.p);
     } else {
         k_tiles<false, false><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut,
-                                                      cut2, tile_count_.p, nullptr, nullptr, nullptr,
-                                                      0, flags_.p);
+                                                      cut2, tile_count_.p, nullptr, nullptr, nullptr, 0, flags_.p);
+    }
+    k_scan<<<1, 1024, 0, s>>>(nc_i, tile_count_.p, raw_start_.p);
+    OCM_CK(cudaMemsetAsync(tile_count_.p, 0, nc * sizeof(int32_t), s));
+    const int pblocks = div_up(tile_cap_ * 32, 128);  // one warp per candidate tile
+    if (per) {
+        k_tiles<true, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2, nullptr,
+                                                    raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_, flags_.p);
+        k_prune<true><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
+                                              box_, inv_box_, cut2, keep_.p, tile_count_.p);
+    } else {
+        k_tiles<false, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2,
+                                                     nullptr, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
+                                                     flags_.p);
+        k_prune<false><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
+                                               box_, inv_box_, cut2, keep_.p, tile_count_.p);
     }
     k_scan<<<1, 1024, 0, s>>>(nc_i, tile_count_.p, tile_start_.p);
-    if (per) {
-        k_tiles<true, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2,
-                                                    nullptr, tile_start_.p, tile_j_.p, tile_mask_.p,
-                                                    (int)tile_cap_, flags_.p);
-    } else {
-        k_tiles<false, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut,
-                                                     cut2, nullptr, tile_start_.p, tile_j_.p,
-                                                     tile_mask_.p, (int)tile_cap_, flags_.p);
-    }
+    k_compact_tiles<<<wblocks, 128, 0, s>>>(nc_i, raw_start_.p, raw_j_.p, keep_.p, (int)tile_cap_,
+                                            tile_start_.p, tile_j_.p, tile_mask_.p);
     const int nnz = (int)cs.ex_j.size();
     OCM_CK(cudaMemsetAsync(mask_count_.p, 0, sizeof(int32_t), s));
     if (nnz > 0) {
@@ -1250,11 +1326,12 @@ void PlainContext::rebuild(cudaStream_t s) {
         k_chg_keys<<<div_up(m, 256), 256, 0, s>>>(m, chg_idx_.p, xq_.p, charged_cells_[0], charged_cells_[1],
                                                   charged_cells_[2], box_, chg_key_.p, chg_count_.p);
         k_scan<<<1, 1024, 0, s>>>((int)n_charged_cells_, chg_count_.p, chg_start_.p);
-        k_chg_scatter<<<div_up(m, 256), 256, 0, s>>>(m, chg_key_.p, chg_start_.p, chg_fill_.p, chg_bucket_.p);
+        k_chg_scatter<<<div_up(m, 256), 256, 0, s>>>(m, chg_idx_.p, chg_key_.p, xq_.p, chg_start_.p, chg_fill_.p,
+                                                     chg_sorted_.p);
         const float ccut = (float)(std::sqrt((double)cs.pc.dh_rc2) + skin) * 1.0001f + 1e-4f;
         k_chg_rows<<<div_up((int64_t)m * 32, 128), 128, 0, s>>>(
             m, chg_idx_.p, chg_key_.p, xq_.p, charged_cells_[0], charged_cells_[1], charged_cells_[2], box_,
-            inv_box_, ccut * ccut, chg_start_.p, chg_bucket_.p, ex_csr_.p, ex_j_.p, ex_bits_.p, chg_rows_.p,
+            inv_box_, ccut * ccut, chg_start_.p, chg_sorted_.p, ex_csr_.p, ex_j_.p, ex_bits_.p, chg_rows_.p,
             chg_len_.p, (int)chg_row_cap_, chg_stats_.p, flags_.p);
     }
 }
@@ -1353,7 +1430,9 @@ void PlainContext::ensure_capacity() {
         int32_t total = 0, masks = 0, flags = 0, chg[2] = {0, 0};
         if (charged_split_)
             OCM_CK(cudaMemcpyAsync(chg, chg_stats_.p, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
-        OCM_CK(cudaMemcpyAsync(&total, tile_start_.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
+        int32_t kept = 0;  // tiles after pruning
+        OCM_CK(cudaMemcpyAsync(&total, raw_start_.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
+        OCM_CK(cudaMemcpyAsync(&kept, tile_start_.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
         OCM_CK(cudaMemcpyAsync(&masks, mask_count_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
         OCM_CK(cudaMemcpyAsync(&flags, flags_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
         OCM_CK(cudaStreamSynchronize(stream_));
@@ -1367,6 +1446,7 @@ void PlainContext::ensure_capacity() {
                 tile_cap_ = want;
                 tile_j_.alloc(tile_cap_);
                 tile_mask_.alloc(tile_cap_);
+                raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_);
                 realloced = true;
                 clear_graphs();
             }
@@ -1393,7 +1473,7 @@ void PlainContext::ensure_capacity() {
         if (!realloced &&
             !(flags & (ListFlags::kTileOverflow | ListFlags::kMaskOverflow | ListFlags::kChargedOverflow)) &&
             total <= tile_cap_ && masks <= mask_cap_ && chg[0] <= chg_row_cap_) {
-            tiles_last = total;
+            tiles_last = kept;
             masked_last = masks;
             charged_last_ = chg[1] / 2;
             list_builds++;
@@ -1540,6 +1620,7 @@ void PlainContext::step(int64_t nsteps) {
             tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, tile_cap_ * 2);
             tile_j_.alloc(tile_cap_);
             tile_mask_.alloc(tile_cap_);
+            raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_);
             mask_cap_ = std::min<int64_t>(tile_cap_, mask_cap_ * 2);
             masks_.alloc(mask_cap_ * 128);
         }
@@ -1572,7 +1653,6 @@ void PlainContext::setup_columns(double width) {
     cell_count_.alloc(n_cells_);
     cell_start_.alloc(n_cells_ + 1);
     cell_fill_.alloc(n_cells_);
-    col_slots_.alloc(ncols);
     col_start_.alloc(ncols + 1);
     clear_graphs();
 }
