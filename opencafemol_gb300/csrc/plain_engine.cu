@@ -613,9 +613,11 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                         const float r2 = norm2(d);
                         if (r2 < a.pc.list_rc2) {
                             uint32_t ex = a.excl_all;
+                            if (m >= 0) {  // the tile holds excluded pairs
     #pragma unroll
-                            for (int term = 0; term < 4; ++term)
-                                if (TERMS & (1 << term)) ex |= ((mw[term] >> r) & 1u) << term;
+                                for (int term = 0; term < 4; ++term)
+                                    if (TERMS & (1 << term)) ex |= ((mw[term] >> r) & 1u) << term;
+                            }
                             if (labels) {
     #pragma unroll
                                 for (int term = 0; term < 4; ++term)
@@ -1387,9 +1389,11 @@ void PlainContext::launch_forces(cudaStream_t s, bool energy, uint32_t slots_ena
     }
     const int grid = blocks_tiles + a.blocks_bonds + a.blocks_angles + a.blocks_dih + a.blocks_chg;
     if (grid == 0) return;
-    const int terms = cs.pc.terms;
+    // the tiles' pair terms (Debye-Hueckel leaves them for the charged rows)
+    const int terms = cs.pc.terms & ~(charged_split_ ? kTermDH : 0);
     const bool per = cs.periodic;
     if ((terms & ~(kTermEXV | kTermDH)) == 0) launch_forces_t<kTermEXV | kTermDH>(a, grid, s, per, energy);
+    else if ((terms & ~(kTermLJR | kTermLJA)) == 0) launch_forces_t<kTermLJR | kTermLJA>(a, grid, s, per, energy);
     else if ((terms & ~(kTermLJR | kTermLJA | kTermDH)) == 0)
         launch_forces_t<kTermLJR | kTermLJA | kTermDH>(a, grid, s, per, energy);
     else launch_forces_t<15>(a, grid, s, per, energy);

@@ -153,6 +153,26 @@ static double fld_min_energy(const double* f) {
     return m;
 }
 
+// The scans above depend only on the table, so each runs once per process
+// (thread-safe static initialisation).
+static double fla_min_energy_cached(int aa) {
+    static const std::vector<double> m = [] {
+        std::vector<double> v(20);
+        for (int a = 0; a < 20; ++a) v[a] = fla_min_energy(a);
+        return v;
+    }();
+    return m[aa];
+}
+
+static double fld_min_energy_cached(int cls) {
+    static const std::vector<double> m = [] {
+        std::vector<double> v(23);
+        for (int c = 0; c < 23; ++c) v[c] = fld_min_energy(kFld[c].c);
+        return v;
+    }();
+    return m[cls];
+}
+
 // ----------------------------------------------------------------------------
 // Debye-Hueckel parameters (DebyeHuckelForceFieldGenerator.cpp:22-46).
 // ----------------------------------------------------------------------------
@@ -480,7 +500,7 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
             const int aa = s->fla_aa[a];
             if (!have[aa]) {
                 natural_spline(kFlaY[aa], h, Mtab[aa]);
-                emin[aa] = fla_min_energy(aa);
+                emin[aa] = fla_min_energy_cached(aa);
                 have[aa] = true;
             }
             const int64_t i1 = s->fla_idx[3 * a], i2 = s->fla_idx[3 * a + 1], i3 = s->fla_idx[3 * a + 2];
@@ -534,7 +554,7 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
             for (int c = 0; c < nc; ++c) {
                 const double* t = kFld[cls[c]].c;
                 if (!have[cls[c]]) {
-                    emin[cls[c]] = fld_min_energy(t);
+                    emin[cls[c]] = fld_min_energy_cached(cls[c]);
                     have[cls[c]] = true;
                 }
                 const double kk = s->fld_k[q];
