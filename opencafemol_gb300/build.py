@@ -54,6 +54,8 @@ def _compile(cmd: list[str], what: str) -> None:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compiling {what} failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if "-v" in cmd:  # ptxas resource report requested
+        print(r.stderr, file=sys.stderr)
 
 
 def build(verbose: bool = False, ptxas_info: bool = False) -> Path:

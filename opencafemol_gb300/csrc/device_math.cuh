@@ -97,30 +97,51 @@ __device__ __forceinline__ float pair_scalar(float r2, float4 pi, float4 pj, flo
         s += qq * ex * (pc.dh_inv_lambda + rinv) * r2inv;
         if (ENERGY) e.dh += qq * (ex * rinv - pc.dh_corr);
     }
-    if ((TERMS & kTermLJR) && !(excl & kTermLJR) && r2 < pc.ljr_rc2) {
+    // shared sigma: mixing and powers once (same expressions, same bits)
+    float sh_sig2 = 0.f, sh_s6 = 0.f, sh_s12 = 0.f;
+    if (TERMS & kLJSameSigma) {
         const float sig = 0.5f * (pi.w + pj.w);
-        const float sig2 = sig * sig;
+        sh_sig2 = sig * sig;
+        const float s2 = sh_sig2 * r2inv;
+        sh_s6 = s2 * s2 * s2;
+        sh_s12 = sh_s6 * sh_s6;
+    }
+    if ((TERMS & kTermLJR) && !(excl & kTermLJR) && r2 < pc.ljr_rc2) {
+        float sig2 = sh_sig2;
+        if (!(TERMS & kLJSameSigma)) {
+            const float sig = 0.5f * (pi.w + pj.w);
+            sig2 = sig * sig;
+        }
         if (r2 <= sig2 * kTwoPow1_3) {
             const float eps = 0.5f * (pi.z + pj.z);
-            const float s2 = sig2 * r2inv;
-            const float s6 = s2 * s2 * s2;
-            const float s12 = s6 * s6;
+            float s6 = sh_s6, s12 = sh_s12;
+            if (!(TERMS & kLJSameSigma)) {
+                const float s2 = sig2 * r2inv;
+                s6 = s2 * s2 * s2;
+                s12 = s6 * s6;
+            }
             s += 24.f * eps * (2.f * s12 - s6) * r2inv;
             if (ENERGY) e.ljr += eps * (4.f * (s12 - s6) + 1.f);
         }
     }
     if ((TERMS & kTermLJA) && !(excl & kTermLJA) && r2 < pc.lja_rc2) {
-        const float sig = 0.5f * (qi.y + qj.y);
-        const float sig2 = sig * sig;
+        float sig2 = sh_sig2;
+        if (!(TERMS & kLJSameSigma)) {
+            const float sig = 0.5f * (qi.y + qj.y);
+            sig2 = sig * sig;
+        }
         const float eps = 0.5f * (qi.x + qj.x);
         float E, dEdr_over_r;  // dE/dr / r of the unswitched potential
         if (r2 < sig2 * kTwoPow1_3) {
             E = -eps;
             dEdr_over_r = 0.f;
         } else {
-            const float s2 = sig2 * r2inv;
-            const float s6 = s2 * s2 * s2;
-            const float s12 = s6 * s6;
+            float s6 = sh_s6, s12 = sh_s12;
+            if (!(TERMS & kLJSameSigma)) {
+                const float s2 = sig2 * r2inv;
+                s6 = s2 * s2 * s2;
+                s12 = s6 * s6;
+            }
             E = 4.f * eps * (s12 - s6);
             dEdr_over_r = -24.f * eps * (2.f * s12 - s6) * r2inv;
         }

@@ -47,6 +47,12 @@ struct DevBuf {
     }
 };
 
+// Periodic box in FP64 (L, 1/L per axis) as the kernels take it.
+struct BoxD {
+    double L[3], iL[3];
+    int periodic;
+};
+
 struct ListFlags {
     enum : int { kTileOverflow = 1, kMaskOverflow = 2, kSkinViolation = 4, kChargedOverflow = 8 };
 };
@@ -92,6 +98,8 @@ class PlainContext {
     void clear_graphs();
     void setup_charged_cells();
     void setup_columns(double width);
+    BoxD box_d() const;
+    float wrap_pad() const;
     void eval(uint32_t groups, bool energy, double* forces, double* slot_energy);
     uint32_t slots_for_groups(uint32_t groups) const;
     void check_positions_set() const;
@@ -119,7 +127,7 @@ class PlainContext {
     DevBuf<double> x_, y_, z_;
     DevBuf<float> vx_, vy_, vz_, invm_;
     DevBuf<unsigned long long> F_;  // 3*n, SoA
-    DevBuf<float4> xq_, ref_, p0_, p1_;
+    DevBuf<float4> xq_, xlo_, ref_, p0_, p1_;  // xlo: FP64 remainder of the FP32 position
     DevBuf<uint32_t> lab_;
     DevBuf<int32_t> slot_;
     // cluster order
@@ -127,7 +135,9 @@ class PlainContext {
     DevBuf<float4> xs_, p0s_, p1s_;
     DevBuf<uint32_t> labs_;
     DevBuf<float4> bb_c_, bb_h_;
+    DevBuf<float4> anc_, ext_;  // cluster anchors, largest anchored offset per axis
     DevBuf<int32_t> tile_count_, tile_start_, tile_j_, tile_mask_;
+    DevBuf<float4> tile_shift_;  // per tile: anchor shift, w != 0 when the minimum image is needed
     DevBuf<int32_t> raw_start_, raw_i_, raw_j_;  // candidate tiles before pruning
     DevBuf<uint8_t> keep_;
     DevBuf<uint32_t> masks_;
@@ -152,7 +162,6 @@ class PlainContext {
     // misc
     DevBuf<double> energy_;           // kNumSlots
     DevBuf<int32_t> flags_;           // ListFlags bits
-    DevBuf<uint32_t> maxdisp_;        // float bits, since last build
     DevBuf<unsigned long long> step_base_;
     DevBuf<double> ke_;
     // snapshot for retries

@@ -15,6 +15,10 @@ constexpr int kTermDH = 2;
 constexpr int kTermLJR = 4;
 constexpr int kTermLJA = 8;
 constexpr int kNumPairTerms = 4;
+// Kernel-template flag (not a term): the attractive LJ term's sigma equals
+// the repulsive one's for every particle, so sigma mixing and the s^6, s^12
+// powers are formed once per pair.  The results are bit-identical.
+constexpr int kLJSameSigma = 16;
 
 // Energy slots (one per term kind); mapped to force groups on the host.
 enum EnergySlot {

@@ -841,6 +841,11 @@ CompiledSystem compile_system(const SystemDesc& d) {
     for (const auto& b : c.bonds)
         if (b.periodic && !d.periodic_box) throw Error(1, "[error] periodic bond force without a box");
     c.pc.list_rc2 = (float)(c.max_cutoff * c.max_cutoff);
+    if ((c.pc.terms & kTermLJR) && (c.pc.terms & kTermLJA)) {
+        c.lj_same_sigma = true;
+        for (int64_t i = 0; i < n && c.lj_same_sigma; ++i)
+            c.lj_same_sigma = c.p0[4 * i + 3] == c.p1[4 * i + 1];
+    }
 
     std::sort(ex.begin(), ex.end());
     c.ex_start.assign(n + 1, 0);

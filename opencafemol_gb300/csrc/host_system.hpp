@@ -307,6 +307,7 @@ struct CompiledSystem {
     std::vector<int32_t> ex_start, ex_j;
     std::vector<uint8_t> ex_bits;
     double max_cutoff = 0;
+    bool lj_same_sigma = false;  // both LJ terms present with equal per-particle sigma
 };
 
 CompiledSystem compile_system(const SystemDesc& d);

@@ -40,6 +40,60 @@ __device__ __forceinline__ float4 shfl4(float4 v, int src) {
     return v;
 }
 
+// ---------------------------------------------------------------------------
+// Cluster-anchored coordinates.  Each cluster has an anchor, the FP32 centre
+// of its bounding box at the last list build; a bead is stored as its offset
+// from the anchor, taken in FP64 from the master position and rounded once
+// to FP32 (|offset| of a nm or two, so about 1e-7 nm of rounding instead of
+// the ~1e-5 nm of an FP32 coordinate 150 nm from the origin).  A pair's
+// separation is (o_j - o_i) + (a_J - a_I), the anchor shift formed exactly in
+// FP64 and rounded once per tile.  All steps are individually rounded so a
+// host enumeration reproduces r^2 bit for bit.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double wrap_coord(double x, double L, double invL) {
+    const double k = floor(__dmul_rn(x, invL));
+    return __dsub_rn(x, __dmul_rn(k, L));
+}
+
+// w - a in FP64, rounded once to FP32; when periodic and |w - a| > L/2,
+// first the minimum image e - L rint(e / L).
+__device__ __forceinline__ float anchor_offset(double w, float a, double L, double iL, int periodic) {
+    double e = __dsub_rn(w, (double)a);
+    if (periodic && fabs(e) > 0.5 * L) e = __dsub_rn(e, __dmul_rn(L, rint(__dmul_rn(e, iL))));
+    return __double2float_rn(e);
+}
+
+__device__ __forceinline__ float3 anchor_shift(float4 ai, float4 aj, const BoxD& b) {
+    return make_float3(anchor_offset((double)aj.x, ai.x, b.L[0], b.iL[0], b.periodic),
+                       anchor_offset((double)aj.y, ai.y, b.L[1], b.iL[1], b.periodic),
+                       anchor_offset((double)aj.z, ai.z, b.L[2], b.iL[2], b.periodic));
+}
+
+__device__ __forceinline__ float3 anchored_sep(float4 oi, float4 oj, float3 A) {
+    return make_float3(__fadd_rn(__fsub_rn(oj.x, oi.x), A.x), __fadd_rn(__fsub_rn(oj.y, oi.y), A.y),
+                       __fadd_rn(__fsub_rn(oj.z, oi.z), A.z));
+}
+
+// The FP32 minimum-image step of the canonical separation.
+__device__ __forceinline__ float3 min_image(float3 d, const float3& box, const float3& inv_box) {
+    d.x = __fmaf_rn(-box.x, rintf(__fmul_rn(d.x, inv_box.x)), d.x);
+    d.y = __fmaf_rn(-box.y, rintf(__fmul_rn(d.y, inv_box.y)), d.y);
+    d.z = __fmaf_rn(-box.z, rintf(__fmul_rn(d.z, inv_box.z)), d.z);
+    return d;
+}
+
+// x_j - x_i from float-float positions (hi = FP32 box-frame coordinate, lo =
+// its FP64 remainder): fl(fl(hj - hi) + fl(lj - li)), then the minimum image.
+template <bool PERIODIC>
+__device__ __forceinline__ float3 ff_separation(float4 hi_i, float4 lo_i, float4 hi_j, float4 lo_j,
+                                                const float3& box, const float3& inv_box) {
+    float3 d = make_float3(__fadd_rn(__fsub_rn(hi_j.x, hi_i.x), __fsub_rn(lo_j.x, lo_i.x)),
+                           __fadd_rn(__fsub_rn(hi_j.y, hi_i.y), __fsub_rn(lo_j.y, lo_i.y)),
+                           __fadd_rn(__fsub_rn(hi_j.z, hi_i.z), __fsub_rn(lo_j.z, lo_i.z)));
+    if (PERIODIC) d = min_image(d, box, inv_box);
+    return d;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
@@ -141,27 +195,37 @@ __global__ void k_bucket_rank(int n, int nz, const int32_t* __restrict__ key,
     perm[col_start[col] + (b - start[col * nz]) + rank] = i;
 }
 
+// Cluster order: anchors, anchored offsets and the parameters of every slot.
 __global__ void k_gather_sorted(int np, const int32_t* __restrict__ perm,
-                                const float4* __restrict__ xq, const float4* __restrict__ p0,
+                                const float4* __restrict__ xq, const double* __restrict__ x,
+                                const double* __restrict__ y, const double* __restrict__ z, BoxD bd,
+                                const float4* __restrict__ p0,
                                 const float4* __restrict__ p1, const uint32_t* __restrict__ lab,
                                 int32_t* __restrict__ slot, float4* __restrict__ xs,
+                                float4* __restrict__ anc,
                                 float4* __restrict__ p0s, float4* __restrict__ p1s,
-                                uint32_t* __restrict__ labs, float4* __restrict__ ref,
-                                uint32_t* __restrict__ maxdisp) {
+                                uint32_t* __restrict__ labs, float4* __restrict__ ref) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) *maxdisp = 0u;
     if (k >= np) return;
     const int o = perm[k];
+    const int o0 = perm[k & ~31];
+    const float nan = __int_as_float(0x7fc00000);
+    const float4 a = o0 >= 0 ? xq[o0] : make_float4(nan, nan, nan, 0.f);
+    if ((k & 31) == 0) anc[k >> 5] = a;
     if (o >= 0) {
         slot[o] = k;
         const float4 p = xq[o];
-        xs[k] = p;
+        double w[3] = {x[o], y[o], z[o]};
+        if (bd.periodic)
+            for (int c = 0; c < 3; ++c) w[c] = wrap_coord(w[c], bd.L[c], bd.iL[c]);
+        xs[k] = make_float4(anchor_offset(w[0], a.x, bd.L[0], bd.iL[0], bd.periodic),
+                            anchor_offset(w[1], a.y, bd.L[1], bd.iL[1], bd.periodic),
+                            anchor_offset(w[2], a.z, bd.L[2], bd.iL[2], bd.periodic), 0.f);
         ref[o] = p;
         p0s[k] = p0[o];
         p1s[k] = p1[o];
         labs[k] = lab[o];
     } else {
-        const float nan = __int_as_float(0x7fc00000);
         xs[k] = make_float4(nan, nan, nan, 0.f);
         p0s[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         p1s[k] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -169,32 +233,35 @@ __global__ void k_gather_sorted(int np, const int32_t* __restrict__ perm,
     }
 }
 
-template <bool PERIODIC>
-__global__ void k_bbox(int nc, const float4* __restrict__ xs, const int32_t* __restrict__ perm,
-                       float3 box, float3 inv_box, float4* __restrict__ bc,
+// Bounding box of each cluster from the offsets to its first bead: centre
+// (FP32 box frame, the cluster's anchor from here on) and half widths (w < 0
+// marks a cluster of padding slots only).
+__global__ void k_bbox(int nc, const float4* __restrict__ xs, const float4* __restrict__ anc,
+                       const int32_t* __restrict__ perm, float4* __restrict__ bc,
                        float4* __restrict__ bh) {
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (I >= nc) return;
-    const float4 base = xs[I * 32];
     const bool valid = perm[I * 32 + lane] >= 0;
-    float3 d = make_float3(0.f, 0.f, 0.f);
-    if (valid) d = separation<PERIODIC>(base, xs[I * 32 + lane], box, inv_box);
+    const float4 o = xs[I * 32 + lane];
+    const float4 o0 = make_float4(__shfl_sync(kFull, o.x, 0), __shfl_sync(kFull, o.y, 0),
+                                  __shfl_sync(kFull, o.z, 0), 0.f);
+    const float4 d = valid ? o : o0;  // slot 0 holds a bead whenever any slot does
     float lx = d.x, ly = d.y, lz = d.z, hx = d.x, hy = d.y, hz = d.z;
     const bool any = __ballot_sync(kFull, valid) != 0u;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        lx = fminf(lx, __shfl_xor_sync(kFull, lx, o));
-        ly = fminf(ly, __shfl_xor_sync(kFull, ly, o));
-        lz = fminf(lz, __shfl_xor_sync(kFull, lz, o));
-        hx = fmaxf(hx, __shfl_xor_sync(kFull, hx, o));
-        hy = fmaxf(hy, __shfl_xor_sync(kFull, hy, o));
-        hz = fmaxf(hz, __shfl_xor_sync(kFull, hz, o));
+    for (int s = 16; s > 0; s >>= 1) {
+        lx = fminf(lx, __shfl_xor_sync(kFull, lx, s));
+        ly = fminf(ly, __shfl_xor_sync(kFull, ly, s));
+        lz = fminf(lz, __shfl_xor_sync(kFull, lz, s));
+        hx = fmaxf(hx, __shfl_xor_sync(kFull, hx, s));
+        hy = fmaxf(hy, __shfl_xor_sync(kFull, hy, s));
+        hz = fmaxf(hz, __shfl_xor_sync(kFull, hz, s));
     }
     if (lane == 0) {
-        bc[I] = make_float4(base.x + 0.5f * (lx + hx), base.y + 0.5f * (ly + hy),
-                            base.z + 0.5f * (lz + hz), 0.f);
-        // w < 0 marks a cluster of padding slots only
+        const float4 a = anc[I];
+        bc[I] = make_float4(__fadd_rn(a.x, 0.5f * __fadd_rn(lx, hx)), __fadd_rn(a.y, 0.5f * __fadd_rn(ly, hy)),
+                            __fadd_rn(a.z, 0.5f * __fadd_rn(lz, hz)), 0.f);
         bh[I] = make_float4(0.5f * (hx - lx), 0.5f * (hy - ly), 0.5f * (hz - lz), any ? 0.f : -1.f);
     }
 }
@@ -219,6 +286,41 @@ __device__ __forceinline__ bool boxes_close(float4 ci, float4 hi, float4 cj, flo
         gz = fmaxf(0.f, fabsf(dz) - hi.z - hj.z);
     }
     return gx * gx + gy * gy + gz * gz < cut2;
+}
+
+// Offsets again, now from the bounding-box centres (the anchors), and the
+// largest |offset| per axis of every cluster.  One warp per cluster.
+__global__ void k_reanchor(int np, const int32_t* __restrict__ perm, const double* __restrict__ x,
+                           const double* __restrict__ y, const double* __restrict__ z, BoxD bd,
+                           const float4* __restrict__ bc, float4* __restrict__ anc, float4* __restrict__ xs,
+                           float4* __restrict__ ext) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;  // np is a multiple of 32: whole warps
+    const int o = perm[k];
+    const float4 a = bc[k >> 5];
+    float ex = 0.f, ey = 0.f, ez = 0.f;
+    if (o >= 0) {
+        double w[3] = {x[o], y[o], z[o]};
+        if (bd.periodic)
+            for (int c = 0; c < 3; ++c) w[c] = wrap_coord(w[c], bd.L[c], bd.iL[c]);
+        const float4 v = make_float4(anchor_offset(w[0], a.x, bd.L[0], bd.iL[0], bd.periodic),
+                                     anchor_offset(w[1], a.y, bd.L[1], bd.iL[1], bd.periodic),
+                                     anchor_offset(w[2], a.z, bd.L[2], bd.iL[2], bd.periodic), 0.f);
+        xs[k] = v;
+        ex = fabsf(v.x);
+        ey = fabsf(v.y);
+        ez = fabsf(v.z);
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        ex = fmaxf(ex, __shfl_xor_sync(kFull, ex, s));
+        ey = fmaxf(ey, __shfl_xor_sync(kFull, ey, s));
+        ez = fmaxf(ez, __shfl_xor_sync(kFull, ez, s));
+    }
+    if ((k & 31) == 0) {
+        anc[k >> 5] = a;
+        ext[k >> 5] = make_float4(ex, ey, ez, 0.f);
+    }
 }
 
 template <bool PERIODIC, bool FILL>
@@ -259,7 +361,8 @@ __global__ void k_tiles(int nc, const float4* __restrict__ bc, const float4* __r
 // beads broadcast one at a time; a tile is kept if any pair is within range
 // (the diagonal tile always).  kept_count[I] counts the kept tiles of row I.
 template <bool PERIODIC>
-__global__ void k_prune(int nc, const float4* __restrict__ xs, const int32_t* __restrict__ raw_start,
+__global__ void k_prune(int nc, const float4* __restrict__ xs, const float4* __restrict__ anc, BoxD bd,
+                        const int32_t* __restrict__ raw_start,
                         const int32_t* __restrict__ raw_i, const int32_t* __restrict__ raw_j, int cap,
                         float3 box, float3 inv_box, float cut2, uint8_t* __restrict__ keep_flag,
                         int32_t* __restrict__ kept_count) {
@@ -271,8 +374,15 @@ __global__ void k_prune(int nc, const float4* __restrict__ xs, const int32_t* __
     bool keep = I == J;
     if (!keep) {
         const float4 xi = xs[I * 32 + lane];
+        // FP32 anchor shift: the pruning cutoff carries the skin and a
+        // 1e-4 nm margin, far above this rounding
+        const float4 ai = anc[I], aj = anc[J];
+        float3 A = make_float3(__fsub_rn(aj.x, ai.x), __fsub_rn(aj.y, ai.y), __fsub_rn(aj.z, ai.z));
+        if (PERIODIC) A = min_image(A, box, inv_box);
         for (int k = 0; k < 32 && !keep; ++k) {
-            const float r2 = norm2(separation<PERIODIC>(xi, xs[J * 32 + k], box, inv_box));
+            float3 d = anchored_sep(xi, xs[J * 32 + k], A);
+            if (PERIODIC) d = min_image(d, box, inv_box);
+            const float r2 = norm2(d);
             keep = __ballot_sync(kFull, r2 < cut2) != 0u;
         }
     }
@@ -283,14 +393,21 @@ __global__ void k_prune(int nc, const float4* __restrict__ xs, const int32_t* __
 }
 
 // Kept tiles of every row, in their order, into the final list (exclusion
-// masks cleared): one warp per row, compacted by ballot.
+// masks cleared): one warp per row, compacted by ballot.  Each tile also
+// gets its anchor shift a_J - a_I and, in w, whether its pairs need the FP32
+// minimum image: not when |shift| + both clusters' largest offsets + pad
+// (the offsets' growth allowance until the next build) stays under half the
+// box, where the minimum image leaves every separation unchanged anyway.
 __global__ void k_compact_tiles(int nc, const int32_t* __restrict__ raw_start, const int32_t* __restrict__ raw_j,
                                 const uint8_t* __restrict__ keep_flag, int cap, const int32_t* __restrict__ start,
-                                int32_t* __restrict__ tile_j, int32_t* __restrict__ tile_mask) {
+                                const float4* __restrict__ anc, const float4* __restrict__ ext, BoxD bd,
+                                float3 box, float pad, int32_t* __restrict__ tile_j, int32_t* __restrict__ tile_mask,
+                                float4* __restrict__ tile_shift) {
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (I >= nc || raw_start[nc] > cap) return;
     const int r0 = raw_start[I], r1 = raw_start[I + 1];
+    const float4 ai = anc[I], ei = ext[I];
     int at = start[I];
     for (int q0 = r0; q0 < r1; q0 += 32) {
         const int q = q0 + lane;
@@ -298,8 +415,15 @@ __global__ void k_compact_tiles(int nc, const int32_t* __restrict__ raw_start, c
         const unsigned b = __ballot_sync(kFull, keep);
         if (keep) {
             const int k = at + __popc(b & ((1u << lane) - 1u));
-            tile_j[k] = raw_j[q];
+            const int J = raw_j[q];
+            tile_j[k] = J;
             tile_mask[k] = -1;
+            const float3 A = anchor_shift(ai, anc[J], bd);
+            const float4 ej = ext[J];
+            const bool wrap = bd.periodic && (fabsf(A.x) + ei.x + ej.x + pad >= 0.5f * box.x ||
+                                              fabsf(A.y) + ei.y + ej.y + pad >= 0.5f * box.y ||
+                                              fabsf(A.z) + ei.z + ej.z + pad >= 0.5f * box.z);
+            tile_shift[k] = make_float4(A.x, A.y, A.z, wrap ? 1.f : 0.f);
         }
         at += __popc(b);
     }
@@ -474,8 +598,9 @@ __global__ void k_chg_rows(int m, const int32_t* __restrict__ idx, const int32_t
 // below the Debye-Hueckel cutoff squared.
 __global__ void k_chg_list_pairs(int m, const int32_t* __restrict__ idx, const int32_t* __restrict__ rows,
                                  const int32_t* __restrict__ row_len, int row_cap,
-                                 const float4* __restrict__ xq, float3 box, float3 inv_box, float rc2,
-                                 long long* out, long long out_cap, unsigned long long* count) {
+                                 const float4* __restrict__ xq, const float4* __restrict__ xlo, float3 box,
+                                 float3 inv_box, float rc2, long long* out, long long out_cap,
+                                 unsigned long long* count) {
     const int t = blockIdx.x;
     if (t >= m) return;
     const int i = idx[t];
@@ -483,7 +608,7 @@ __global__ void k_chg_list_pairs(int m, const int32_t* __restrict__ idx, const i
     for (int p = threadIdx.x; p < len; p += blockDim.x) {
         const int j = rows[(size_t)t * row_cap + p];
         if (j < i) continue;
-        const float r2 = norm2(separation<true>(xq[i], xq[j], box, inv_box));
+        const float r2 = norm2(ff_separation<true>(xq[i], xlo[i], xq[j], xlo[j], box, inv_box));
         if (r2 < rc2) {
             const unsigned long long at = atomicAdd(count, 1ull);
             if ((long long)at < out_cap) {
@@ -518,8 +643,9 @@ struct ForceArgs {
     uint32_t slots_enabled;
     uint32_t excl_all;
     double* energy;
+    const float4* tile_shift;  // per tile: anchor shift a_J - a_I, w != 0: minimum image needed
     // charged-pair rows (blocks_chg > 0)
-    const float4 *xq, *p0;
+    const float4 *xq, *xlo, *p0;
     const int32_t *chg_idx, *chg_rows, *chg_len;
     int n_chg, chg_row_cap;
 };
@@ -593,6 +719,9 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                 const int m = a.tile_mask[t];
                 const int kj = J * 32 + lane;
                 float4 xj = a.xs[kj];
+                const float4 sh = a.tile_shift[t];  // anchor shift, w: minimum image needed
+                const float3 A = make_float3(sh.x, sh.y, sh.z);
+                const bool wrap = PERIODIC && sh.w != 0.f;
                 float4 p0j = a.p0s[kj];
                 float4 p1j = (TERMS & kTermLJA) ? a.p1s[kj] : make_float4(0.f, 0.f, 0.f, 0.f);
                 uint32_t labj = a.labs[kj];
@@ -609,7 +738,8 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                 for (int r = 0; r < 32; ++r) {
                     const bool do_pair = !diag || (r > 0 && (r < 16 || (r == 16 && lane < 16)));
                     if (do_pair) {
-                        const float3 d = separation<PERIODIC>(xi, xj, a.box, a.inv_box);
+                        float3 d = anchored_sep(xi, xj, A);
+                        if (wrap) d = min_image(d, a.box, a.inv_box);
                         const float r2 = norm2(d);
                         if (r2 < a.pc.list_rc2) {
                             uint32_t ex = a.excl_all;
@@ -644,7 +774,7 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                     }
                     if (TERMS & kTermLJA) {
                         p1j.x = __shfl_sync(kFull, p1j.x, src);
-                        p1j.y = __shfl_sync(kFull, p1j.y, src);
+                        if (!(TERMS & kLJSameSigma)) p1j.y = __shfl_sync(kFull, p1j.y, src);
                     }
                     if (labels) labj = __shfl_sync(kFull, labj, src);
                     fj.x = __shfl_sync(kFull, fj.x, src);
@@ -777,14 +907,14 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
             const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
             for (int t = blk * kWarpsPerForceBlock + warp; t < a.n_chg; t += a.blocks_chg * kWarpsPerForceBlock) {
                 const int i = a.chg_idx[t];
-                const float4 xi = a.xq[i];
+                const float4 xi = a.xq[i], li = a.xlo[i];
                 const float4 pi = a.p0[i];
                 const int len = min(a.chg_len[t], a.chg_row_cap);
                 const int32_t* row = a.chg_rows + (size_t)t * a.chg_row_cap;
                 long long fx = 0, fy = 0, fz = 0;
                 for (int p = lane; p < len; p += 32) {
                     const int j = row[p];
-                    const float3 d = separation<PERIODIC>(xi, a.xq[j], a.box, a.inv_box);
+                    const float3 d = ff_separation<PERIODIC>(xi, li, a.xq[j], a.xlo[j], a.box, a.inv_box);
                     const float r2 = norm2(d);
                     if (r2 < a.pc.dh_rc2) {
                         PairEnergy e;
@@ -826,7 +956,8 @@ struct IntegrateArgs {
     float *vx, *vy, *vz;
     double *x, *y, *z;
     const float* invm;
-    float4 *xq, *xs;
+    float4 *xq, *xlo, *xs;
+    const float4* anc;
     const int32_t* slot;
     const float4* ref;
     LangevinConsts lc;
@@ -836,14 +967,9 @@ struct IntegrateArgs {
     double box[3], inv_box[3];
     float3 fbox, finv_box;
     float disp_limit2;
-    uint32_t* maxdisp;
     int32_t* flags;
 };
 
-__device__ __forceinline__ double wrap_coord(double x, double L, double invL) {
-    const double k = floor(__dmul_rn(x, invL));
-    return __dsub_rn(x, __dmul_rn(k, L));
-}
 
 __global__ void k_integrate(IntegrateArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -874,37 +1000,44 @@ __global__ void k_integrate(IntegrateArgs a) {
         a.y[i] = y;
         a.z[i] = z;
     }
-    float4 p;
-    if (a.periodic) {
-        p = make_float4(__double2float_rn(wrap_coord(x, a.box[0], a.inv_box[0])),
-                        __double2float_rn(wrap_coord(y, a.box[1], a.inv_box[1])),
-                        __double2float_rn(wrap_coord(z, a.box[2], a.inv_box[2])), 0.f);
-    } else {
-        p = make_float4(__double2float_rn(x), __double2float_rn(y), __double2float_rn(z), 0.f);
-    }
+    double w[3] = {x, y, z};
+    if (a.periodic)
+        for (int c = 0; c < 3; ++c) w[c] = wrap_coord(w[c], a.box[c], a.inv_box[c]);
+    const float4 p = make_float4(__double2float_rn(w[0]), __double2float_rn(w[1]), __double2float_rn(w[2]), 0.f);
     a.xq[i] = p;
-    a.xs[a.slot[i]] = p;
+    a.xlo[i] = make_float4(__double2float_rn(__dsub_rn(w[0], (double)p.x)),
+                           __double2float_rn(__dsub_rn(w[1], (double)p.y)),
+                           __double2float_rn(__dsub_rn(w[2], (double)p.z)), 0.f);
+    const int k = a.slot[i];
+    const float4 an = a.anc[k >> 5];
+    a.xs[k] = make_float4(anchor_offset(w[0], an.x, a.box[0], a.inv_box[0], a.periodic),
+                          anchor_offset(w[1], an.y, a.box[1], a.inv_box[1], a.periodic),
+                          anchor_offset(w[2], an.z, a.box[2], a.inv_box[2], a.periodic), 0.f);
     const float4 q = a.ref[i];
     float3 d = a.periodic ? separation<true>(q, p, a.fbox, a.finv_box)
                           : separation<false>(q, p, a.fbox, a.finv_box);
     const float d2 = norm2(d);
     if (d2 > a.disp_limit2) atomicOr(a.flags, ListFlags::kSkinViolation);
-    atomicMax(a.maxdisp, __float_as_uint(d2));
 }
 
 __global__ void k_positions_to_float(int n, const double* __restrict__ x,
                                      const double* __restrict__ y, const double* __restrict__ z,
                                      int periodic, double bx, double by, double bz, double ibx,
-                                     double iby, double ibz, float4* __restrict__ xq) {
+                                     double iby, double ibz, float4* __restrict__ xq,
+                                     float4* __restrict__ xlo) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (periodic)
-        xq[i] = make_float4(__double2float_rn(wrap_coord(x[i], bx, ibx)),
-                            __double2float_rn(wrap_coord(y[i], by, iby)),
-                            __double2float_rn(wrap_coord(z[i], bz, ibz)), 0.f);
-    else
-        xq[i] = make_float4(__double2float_rn(x[i]), __double2float_rn(y[i]),
-                            __double2float_rn(z[i]), 0.f);
+    double w[3] = {x[i], y[i], z[i]};
+    if (periodic) {
+        w[0] = wrap_coord(w[0], bx, ibx);
+        w[1] = wrap_coord(w[1], by, iby);
+        w[2] = wrap_coord(w[2], bz, ibz);
+    }
+    const float4 p = make_float4(__double2float_rn(w[0]), __double2float_rn(w[1]), __double2float_rn(w[2]), 0.f);
+    xq[i] = p;
+    xlo[i] = make_float4(__double2float_rn(__dsub_rn(w[0], (double)p.x)),
+                         __double2float_rn(__dsub_rn(w[1], (double)p.y)),
+                         __double2float_rn(__dsub_rn(w[2], (double)p.z)), 0.f);
 }
 
 __global__ void k_advance(unsigned long long* step_base, int k) { *step_base += (unsigned long long)k; }
@@ -936,7 +1069,8 @@ __global__ void k_kinetic(int n, const float* __restrict__ invm, const float* __
 // Verification: emit every pair the tiles make the kernel test whose FP32
 // r^2 is below the largest cutoff squared.
 template <bool PERIODIC>
-__global__ void k_list_pairs(int nc, const float4* __restrict__ xs, const int32_t* __restrict__ perm,
+__global__ void k_list_pairs(int nc, const float4* __restrict__ xs, const float4* __restrict__ tile_shift,
+                             const int32_t* __restrict__ perm,
                              const int32_t* __restrict__ tile_start, const int32_t* __restrict__ tile_j,
                              float3 box, float3 inv_box, float rc2, long long* out, long long cap,
                              unsigned long long* count, long long tile_cap) {
@@ -949,13 +1083,16 @@ __global__ void k_list_pairs(int nc, const float4* __restrict__ xs, const int32_
     for (int t = tile_start[I]; t < tile_start[I + 1]; ++t) {
         const int J = tile_j[t];
         const bool diag = J == I;
+        const float3 A = make_float3(tile_shift[t].x, tile_shift[t].y, tile_shift[t].z);
         for (int r = 0; r < 32; ++r) {
             const int jl = (lane + r) & 31;
             const bool do_pair = !diag || (r > 0 && (r < 16 || (r == 16 && lane < 16)));
             const float4 xj = xs[J * 32 + jl];
             const int oj = perm[J * 32 + jl];
             if (do_pair && oi >= 0 && oj >= 0) {
-                const float r2 = norm2(separation<PERIODIC>(xi, xj, box, inv_box));
+                float3 d = anchored_sep(xi, xj, A);
+                if (PERIODIC) d = min_image(d, box, inv_box);
+                const float r2 = norm2(d);
                 if (r2 < rc2) {
                     const unsigned long long at = atomicAdd(count, 1ull);
                     if ((long long)at < cap) {
@@ -1041,7 +1178,7 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
     invm_.upload(cs.inv_mass, s);
     F_.alloc(3 * n);
     OCM_CK(cudaMemsetAsync(F_.p, 0, 3 * n * sizeof(unsigned long long), s));
-    xq_.alloc(n); ref_.alloc(n);
+    xq_.alloc(n); xlo_.alloc(n); ref_.alloc(n);
     {
         std::vector<float4> p0(n), p1(n);
         for (int64_t i = 0; i < n; ++i) {
@@ -1060,10 +1197,10 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
         perm_.upload(id, s);
     }
     xs_.alloc(np); p0s_.alloc(np); p1s_.alloc(np); labs_.alloc(np);
-    bb_c_.alloc(nc); bb_h_.alloc(nc);
+    bb_c_.alloc(nc); bb_h_.alloc(nc); anc_.alloc(nc); ext_.alloc(nc);
     tile_count_.alloc(nc); tile_start_.alloc(nc + 1); raw_start_.alloc(nc + 1);
     tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, std::max<int64_t>(4096, nc * 48));
-    tile_j_.alloc(tile_cap_); tile_mask_.alloc(tile_cap_); raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_);
+    tile_j_.alloc(tile_cap_); tile_mask_.alloc(tile_cap_); raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_);
     mask_cap_ = std::max<int64_t>(256, std::min<int64_t>(tile_cap_, nc * 8));
     masks_.alloc(mask_cap_ * 128);
     mask_count_.alloc(1);
@@ -1124,7 +1261,6 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
     energy_.alloc(kNumSlots);
     flags_.alloc(1);
     OCM_CK(cudaMemsetAsync(flags_.p, 0, sizeof(int32_t), s));
-    maxdisp_.alloc(1);
     step_base_.alloc(1);
     OCM_CK(cudaMemsetAsync(step_base_.p, 0, sizeof(unsigned long long), s));
     ke_.alloc(1);
@@ -1188,7 +1324,7 @@ void PlainContext::set_positions(const double* xyz) {
     k_positions_to_float<<<div_up(n, 256), 256, 0, stream_>>>(
         (int)n, x_.p, y_.p, z_.p, cs.periodic ? 1 : 0, cs.box[0], cs.box[1], cs.box[2],
         cs.box[0] > 0 ? 1.0 / cs.box[0] : 0.0, cs.box[1] > 0 ? 1.0 / cs.box[1] : 0.0,
-        cs.box[2] > 0 ? 1.0 / cs.box[2] : 0.0, xq_.p);
+        cs.box[2] > 0 ? 1.0 / cs.box[2] : 0.0, xq_.p, xlo_.p);
     OCM_CK(cudaGetLastError());
     OCM_CK(cudaStreamSynchronize(stream_));
     positions_set_ = true;
@@ -1273,13 +1409,15 @@ void PlainContext::rebuild(cudaStream_t s) {
         k_bucket_rank<<<div_up(n, 256), 256, 0, s>>>(n_i, cell_dims_[2], cell_key_.p, cell_start_.p,
                                                      col_start_.p, bucket_.p, perm_.p);
     }
-    k_gather_sorted<<<div_up(np, 256), 256, 0, s>>>(np_i, perm_.p, xq_.p, p0_.p, p1_.p, lab_.p,
-                                                    slot_.p, xs_.p, p0s_.p, p1s_.p, labs_.p,
-                                                    ref_.p, maxdisp_.p);
+    const BoxD bd = box_d();
+    k_gather_sorted<<<div_up(np, 256), 256, 0, s>>>(np_i, perm_.p, xq_.p, x_.p, y_.p, z_.p, bd, p0_.p, p1_.p,
+                                                    lab_.p, slot_.p, xs_.p, anc_.p, p0s_.p, p1s_.p, labs_.p,
+                                                    ref_.p);
     const bool per = cs.periodic;
     const int wblocks = div_up(nc * 32, 128);
-    if (per) k_bbox<true><<<wblocks, 128, 0, s>>>(nc_i, xs_.p, perm_.p, box_, inv_box_, bb_c_.p, bb_h_.p);
-    else k_bbox<false><<<wblocks, 128, 0, s>>>(nc_i, xs_.p, perm_.p, box_, inv_box_, bb_c_.p, bb_h_.p);
+    k_bbox<<<wblocks, 128, 0, s>>>(nc_i, xs_.p, anc_.p, perm_.p, bb_c_.p, bb_h_.p);
+    k_reanchor<<<div_up(np, 128), 128, 0, s>>>(np_i, perm_.p, x_.p, y_.p, z_.p, bd, bb_c_.p, anc_.p, xs_.p,
+                                               ext_.p);
     const float cut = (float)(tile_cutoff_ + skin) * 1.0001f + 1e-4f;
     const float cut2 = cut * cut;
     if (per) {
@@ -1295,18 +1433,19 @@ void PlainContext::rebuild(cudaStream_t s) {
     if (per) {
         k_tiles<true, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2, nullptr,
                                                     raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_, flags_.p);
-        k_prune<true><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
+        k_prune<true><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, anc_.p, bd, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
                                               box_, inv_box_, cut2, keep_.p, tile_count_.p);
     } else {
         k_tiles<false, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2,
                                                      nullptr, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
                                                      flags_.p);
-        k_prune<false><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
+        k_prune<false><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, anc_.p, bd, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
                                                box_, inv_box_, cut2, keep_.p, tile_count_.p);
     }
     k_scan<<<1, 1024, 0, s>>>(nc_i, tile_count_.p, tile_start_.p);
     k_compact_tiles<<<wblocks, 128, 0, s>>>(nc_i, raw_start_.p, raw_j_.p, keep_.p, (int)tile_cap_,
-                                            tile_start_.p, tile_j_.p, tile_mask_.p);
+                                            tile_start_.p, anc_.p, ext_.p, bd, box_, wrap_pad(), tile_j_.p,
+                                            tile_mask_.p, tile_shift_.p);
     const int nnz = (int)cs.ex_j.size();
     OCM_CK(cudaMemsetAsync(mask_count_.p, 0, sizeof(int32_t), s));
     if (nnz > 0) {
@@ -1374,7 +1513,9 @@ void PlainContext::launch_forces(cudaStream_t s, bool energy, uint32_t slots_ena
     }
     a.excl_all = excl_all;
     a.xq = xq_.p;
+    a.xlo = xlo_.p;
     a.p0 = p0_.p;
+    a.tile_shift = tile_shift_.p;
     a.chg_idx = chg_idx_.p;
     a.chg_rows = chg_rows_.p;
     a.chg_len = chg_len_.p;
@@ -1393,6 +1534,8 @@ void PlainContext::launch_forces(cudaStream_t s, bool energy, uint32_t slots_ena
     const int terms = cs.pc.terms & ~(charged_split_ ? kTermDH : 0);
     const bool per = cs.periodic;
     if ((terms & ~(kTermEXV | kTermDH)) == 0) launch_forces_t<kTermEXV | kTermDH>(a, grid, s, per, energy);
+    else if (terms == (kTermLJR | kTermLJA) && cs.lj_same_sigma)
+        launch_forces_t<kTermLJR | kTermLJA | kLJSameSigma>(a, grid, s, per, energy);
     else if ((terms & ~(kTermLJR | kTermLJA)) == 0) launch_forces_t<kTermLJR | kTermLJA>(a, grid, s, per, energy);
     else if ((terms & ~(kTermLJR | kTermLJA | kTermDH)) == 0)
         launch_forces_t<kTermLJR | kTermLJA | kTermDH>(a, grid, s, per, energy);
@@ -1407,7 +1550,7 @@ void PlainContext::launch_integrate(cudaStream_t s, int r) {
     a.vx = vx_.p; a.vy = vy_.p; a.vz = vz_.p;
     a.x = x_.p; a.y = y_.p; a.z = z_.p;
     a.invm = invm_.p;
-    a.xq = xq_.p; a.xs = xs_.p; a.slot = slot_.p; a.ref = ref_.p;
+    a.xq = xq_.p; a.xlo = xlo_.p; a.xs = xs_.p; a.anc = anc_.p; a.slot = slot_.p; a.ref = ref_.p;
     a.lc = lc_;
     a.step_base = step_base_.p;
     a.r = r;
@@ -1420,9 +1563,8 @@ void PlainContext::launch_integrate(cudaStream_t s, int r) {
     a.finv_box = inv_box_;
     const float half = (float)(0.5 * skin);
     a.disp_limit2 = half * half;
-    a.maxdisp = maxdisp_.p;
     a.flags = flags_.p;
-    k_integrate<<<div_up(n, 256), 256, 0, s>>>(a);
+    k_integrate<<<div_up(n, 64), 64, 0, s>>>(a);  // small blocks: every SM gets some
     OCM_CK(cudaGetLastError());
 }
 
@@ -1450,7 +1592,7 @@ void PlainContext::ensure_capacity() {
                 tile_cap_ = want;
                 tile_j_.alloc(tile_cap_);
                 tile_mask_.alloc(tile_cap_);
-                raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_);
+                raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_);
                 realloced = true;
                 clear_graphs();
             }
@@ -1609,7 +1751,7 @@ void PlainContext::step(int64_t nsteps) {
         k_positions_to_float<<<div_up(n, 256), 256, 0, s>>>(
             (int)n, x_.p, y_.p, z_.p, cs.periodic ? 1 : 0, cs.box[0], cs.box[1], cs.box[2],
             cs.box[0] > 0 ? 1.0 / cs.box[0] : 0.0, cs.box[1] > 0 ? 1.0 / cs.box[1] : 0.0,
-            cs.box[2] > 0 ? 1.0 / cs.box[2] : 0.0, xq_.p);
+            cs.box[2] > 0 ? 1.0 / cs.box[2] : 0.0, xq_.p, xlo_.p);
         OCM_CK(cudaStreamSynchronize(s));
         if (flags & ListFlags::kSkinViolation) {
             if (rebuild_interval == 1)
@@ -1624,7 +1766,7 @@ void PlainContext::step(int64_t nsteps) {
             tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, tile_cap_ * 2);
             tile_j_.alloc(tile_cap_);
             tile_mask_.alloc(tile_cap_);
-            raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_);
+            raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_);
             mask_cap_ = std::min<int64_t>(tile_cap_, mask_cap_ * 2);
             masks_.alloc(mask_cap_ * 128);
         }
@@ -1640,6 +1782,21 @@ void PlainContext::set_list_options(int32_t interval, double sk) {
     if (sk > 0) skin = sk;
     setup_charged_cells();  // cells must stay at least cutoff + skin wide
     clear_graphs();
+}
+
+float PlainContext::wrap_pad() const {
+    // two beads' displacement allowance between builds, plus rounding
+    return (float)(skin * 1.001 + 1e-3);
+}
+
+BoxD PlainContext::box_d() const {
+    BoxD b{};
+    for (int k = 0; k < 3; ++k) {
+        b.L[k] = cs.box[k];
+        b.iL[k] = cs.box[k] > 0 ? 1.0 / cs.box[k] : 0.0;
+    }
+    b.periodic = cs.periodic ? 1 : 0;
+    return b;
 }
 
 void PlainContext::setup_columns(double width) {
@@ -1693,16 +1850,16 @@ void PlainContext::list_pairs(int64_t* out, int64_t cap, int64_t* n_out) {
     const int wblocks = div_up(nc * 32, 128);
     const float tile_rc2 = charged_split_ ? (float)(tile_cutoff_ * tile_cutoff_) : cs.pc.list_rc2;
     if (cs.periodic)
-        k_list_pairs<true><<<wblocks, 128, 0, stream_>>>((int)nc, xs_.p, perm_.p, tile_start_.p,
+        k_list_pairs<true><<<wblocks, 128, 0, stream_>>>((int)nc, xs_.p, tile_shift_.p, perm_.p, tile_start_.p,
                                                         tile_j_.p, box_, inv_box_, tile_rc2,
                                                         buf.p, cap, cnt.p, tile_cap_);
     else
-        k_list_pairs<false><<<wblocks, 128, 0, stream_>>>((int)nc, xs_.p, perm_.p, tile_start_.p,
+        k_list_pairs<false><<<wblocks, 128, 0, stream_>>>((int)nc, xs_.p, tile_shift_.p, perm_.p, tile_start_.p,
                                                          tile_j_.p, box_, inv_box_, tile_rc2,
                                                          buf.p, cap, cnt.p, tile_cap_);
     if (charged_split_)
         k_chg_list_pairs<<<(int)n_charged_, 128, 0, stream_>>>(
-            (int)n_charged_, chg_idx_.p, chg_rows_.p, chg_len_.p, (int)chg_row_cap_, xq_.p, box_, inv_box_,
+            (int)n_charged_, chg_idx_.p, chg_rows_.p, chg_len_.p, (int)chg_row_cap_, xq_.p, xlo_.p, box_, inv_box_,
             cs.pc.dh_rc2, buf.p, cap,
             cnt.p);
     OCM_CK(cudaGetLastError());

@@ -89,10 +89,11 @@ def test_group_masks(gpu, kind):
 
 def test_pair_set_bit_exact(gpu):
     """The pairs the tile list makes the kernel test within the cutoff the
-    tiles serve equal a brute-force FP32 enumeration with the same r^2
-    formula; with a separate charged-pair list (Debye-Hueckel cutoff well
-    above the others) its pairs equal the charged pairs within the
-    Debye-Hueckel cutoff that its exclusions keep."""
+    tiles serve equal a brute-force enumeration with the kernel's arithmetic
+    (cluster-anchored FP32 offsets, the anchor shift rounded once from FP64,
+    canonical r^2); with a separate charged-pair list (Debye-Hueckel cutoff
+    well above the others) its pairs equal the charged pairs within the
+    Debye-Hueckel cutoff (float-float separations) that its exclusions keep."""
     from collections import Counter
 
     from opencafemol_gb300 import synth
@@ -100,11 +101,12 @@ def test_pair_set_bit_exact(gpu):
     spec = synth.hps_slab(30, chain_len, (15.0, 15.0, 60.0), slab_width=20.0, seed=6)
     system, ctx = _ctx(gpu, spec)
     pairs = ctx.list_pairs()  # builds the lists
+    order = ctx.cluster_order()
     st = ctx.stats()
     assert st["charged_split"] == 1  # DH 3.5 nm against a 2.0 nm HPS cutoff
     assert st["tile_cutoff"] < st["max_cutoff"]
     got = Counter(map(tuple, pairs.tolist()))
-    ref = Counter(brute_force_pairs(spec.pos, spec.box, st["tile_cutoff"]))
+    ref = Counter(brute_force_pairs(spec.pos, spec.box, st["tile_cutoff"], order=order))
     q = spec.dh.p0
     charged = ~np.isnan(q) & (np.nan_to_num(q) != 0)
     dh_excluded = lambda i, j: i // chain_len == j // chain_len and abs(i - j) <= 3  # ign_bond=3
@@ -116,24 +118,63 @@ def test_pair_set_bit_exact(gpu):
     assert got == ref
 
 
-def brute_force_pairs(pos, box, rc, mask=None):
+def _fp32_min_image(d, Lf, iLf):
+    # d - L*rint(d/L) with FP32 roundings; L*k is exact for |k| <= 1, so the
+    # separate rounding equals the kernel's fma
+    return (d - Lf * np.rint((d * iLf).astype(np.float32))).astype(np.float32)
+
+
+def _fp32_r2(d):
+    # fmaf(dz, dz, fmaf(dy, dy, dx * dx)), each fma rounded once
+    dx2 = (d[:, 0] * d[:, 0]).astype(np.float32)
+    s1 = (d[:, 1].astype(np.float64) * d[:, 1] + dx2).astype(np.float32)
+    return (d[:, 2].astype(np.float64) * d[:, 2] + s1).astype(np.float32)
+
+
+def brute_force_pairs(pos, box, rc, order=None, mask=None):
+    """Pairs (i < j) with FP32 r^2 < rc^2 under the kernels' arithmetic:
+    with `order` (slot -> bead, -1 padding, clusters of 32) the anchored
+    offsets of the tile kernel, otherwise the float-float separation of the
+    charged rows; `mask` restricts both beads."""
     L = np.asarray(box, np.float64)
+    iL = 1.0 / L
     x = np.asarray(pos, np.float64)
-    w = x - L * np.floor(x * (1.0 / L))
-    xf = w.astype(np.float32)
-    Lf, iLf = L.astype(np.float32), (1.0 / L).astype(np.float32)
+    w = x - np.floor(x * iL) * L                     # wrap_coord, FP64
+    hi = w.astype(np.float32)                        # FP32 box-frame position
+    Lf, iLf = L.astype(np.float32), iL.astype(np.float32)
     rc2 = np.float32(rc * rc)
+    n = len(x)
+    if order is not None:
+        order = np.asarray(order)
+        cl = np.zeros(n, np.int64)
+        valid = order >= 0
+        cl[order[valid]] = np.nonzero(valid)[0] // 32
+        first = order.reshape(-1, 32)[:, 0]
+
+        def minimg64(e):  # the minimum image only beyond half a box
+            return np.where(np.abs(e) > 0.5 * L, e - L * np.rint(e * iL), e)
+        # anchors: bounding-box centres of the offsets to each first bead
+        a0 = np.full((len(first), 3), np.nan, np.float32)
+        a0[first >= 0] = hi[first[first >= 0]]
+        off0 = minimg64(w - a0[cl].astype(np.float64)).astype(np.float32)
+        lo_b = np.full_like(a0, np.inf)
+        hi_b = np.full_like(a0, -np.inf)
+        np.minimum.at(lo_b, cl, off0)
+        np.maximum.at(hi_b, cl, off0)
+        anc = (a0 + np.float32(0.5) * (lo_b + hi_b).astype(np.float32)).astype(np.float32)
+        off = minimg64(w - anc[cl].astype(np.float64)).astype(np.float32)
+    else:
+        lo = (w - hi.astype(np.float64)).astype(np.float32)
     out = set()
-    n = len(xf)
     for i in range(n - 1):
         if mask is not None and not mask[i]:
             continue
-        d = xf[i + 1:] - xf[i]
-        d = (d - Lf * np.rint(d * iLf)).astype(np.float32)  # separate rounding, equals the fma result
-        # emulate fmaf(dz,dz,fmaf(dy,dy,dx*dx)) exactly in float64 then round once per fma
-        dx2 = (d[:, 0] * d[:, 0]).astype(np.float32)
-        s1 = (d[:, 1].astype(np.float64) * d[:, 1] + dx2).astype(np.float32)
-        r2 = (d[:, 2].astype(np.float64) * d[:, 2] + s1).astype(np.float32)
+        if order is not None:
+            A = minimg64(anc[cl[i + 1:]].astype(np.float64) - anc[cl[i]].astype(np.float64)).astype(np.float32)
+            d = ((off[i + 1:] - off[i]).astype(np.float32) + A).astype(np.float32)
+        else:
+            d = ((hi[i + 1:] - hi[i]).astype(np.float32) + (lo[i + 1:] - lo[i]).astype(np.float32)).astype(np.float32)
+        r2 = _fp32_r2(_fp32_min_image(d, Lf, iLf))
         hit = r2 < rc2
         if mask is not None:
             hit &= mask[i + 1:]
@@ -250,3 +291,26 @@ def test_first_evaluation_after_list_growth(gpu):
     f3, _ = ctx.getState(energy=False)
     f_ref3, _ = oracle.evaluate(spec, pos=x, cells=1)
     assert rel_force_err(f3, f_ref3) <= FORCE_TOL
+
+
+def test_lj_same_sigma_path_bit_identical(gpu):
+    """When both HPS terms carry the same per-particle sigma the kernel forms
+    the sigma mixing and the s^6, s^12 powers once per pair.  Perturbing one
+    bead's attractive sigma selects the general path; every bead out of that
+    bead's reach gets bit-identical forces from both."""
+    from opencafemol_gb300 import synth
+    spec = synth.hps_slab(30, 100, (15.0, 15.0, 60.0), slab_width=20.0, seed=12)
+    _, ctx = _ctx(gpu, spec)
+    f_same, _ = ctx.getState(energy=False)
+    k = int(np.argmin(spec.lja.p1))
+    spec.lja.p1 = spec.lja.p1.copy()
+    spec.lja.p1[k] *= 1.000001
+    _, ctx2 = _ctx(gpu, spec)
+    f_gen, _ = ctx2.getState(energy=False)
+    L = np.asarray(spec.box)
+    d = spec.pos - spec.pos[k]
+    d -= L * np.rint(d / L)
+    far = np.linalg.norm(d, axis=1) > 2.5
+    assert far.sum() > 0.9 * spec.n
+    assert np.array_equal(f_same[far], f_gen[far])
+    assert not np.array_equal(f_same[k], f_gen[k])
