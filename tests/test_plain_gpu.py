@@ -161,7 +161,8 @@ def brute_force_pairs(pos, box, rc, order=None, mask=None):
         hi_b = np.full_like(a0, -np.inf)
         np.minimum.at(lo_b, cl, off0)
         np.maximum.at(hi_b, cl, off0)
-        anc = (a0 + np.float32(0.5) * (lo_b + hi_b).astype(np.float32)).astype(np.float32)
+        with np.errstate(invalid="ignore"):  # padding-only clusters: NaN anchors
+            anc = (a0 + np.float32(0.5) * (lo_b + hi_b).astype(np.float32)).astype(np.float32)
         off = minimg64(w - anc[cl].astype(np.float64)).astype(np.float32)
     else:
         lo = (w - hi.astype(np.float64)).astype(np.float32)
