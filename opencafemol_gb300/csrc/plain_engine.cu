@@ -103,23 +103,9 @@ __device__ __forceinline__ double warp_sum(double v) {
 // ---------------------------------------------------------------------------
 // Rebuild kernels
 // ---------------------------------------------------------------------------
-__global__ void k_cell_keys(int n, const float4* __restrict__ xq, int nx, int ny, int nz,
-                            float3 box, int32_t* __restrict__ key, int32_t* __restrict__ count) {
-    // cell = (column, z slice); cells of one column are consecutive
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 p = xq[i];
-    const int cx = min(nx - 1, max(0, (int)(p.x * ((float)nx / box.x))));
-    const int cy = min(ny - 1, max(0, (int)(p.y * ((float)ny / box.y))));
-    const int cz = min(nz - 1, max(0, (int)(p.z * ((float)nz / box.z))));
-    const int k = (cy * nx + cx) * nz + cz;
-    key[i] = k;
-    atomicAdd(&count[k], 1);
-}
 
 // Exclusive scan of m ints into out[0..m] by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan(int m, const int32_t* __restrict__ in,
-                                               int32_t* __restrict__ out) {
+__device__ __forceinline__ void block_scan(int m, const int32_t* __restrict__ in, int32_t* __restrict__ out) {
     __shared__ int32_t part[1024];
     const int t = threadIdx.x;
     const int per = (m + 1023) / 1024;
@@ -141,6 +127,45 @@ __global__ void __launch_bounds__(1024) k_scan(int m, const int32_t* __restrict_
         run += v;
     }
     if (t == 1023) out[m] = part[1023];
+}
+
+__global__ void __launch_bounds__(1024) k_scan(int m, const int32_t* __restrict__ in,
+                                               int32_t* __restrict__ out) {
+    block_scan(m, in, out);
+}
+
+// Two independent scans in one launch, one block each.
+__global__ void __launch_bounds__(1024) k_scan2(int m0, const int32_t* __restrict__ in0, int32_t* __restrict__ out0,
+                                                int m1, const int32_t* __restrict__ in1, int32_t* __restrict__ out1) {
+    if (blockIdx.x == 0) block_scan(m0, in0, out0);
+    else block_scan(m1, in1, out1);
+}
+
+// Cell keys of the beads (columns) and, in the same launch, of the charged
+// beads (their own grid): threads [0, n) and [n, n + m).
+__global__ void k_keys_both(int n, const float4* __restrict__ xq, int nx, int ny, int nz, float3 box,
+                            int32_t* __restrict__ key, int32_t* __restrict__ count, int m,
+                            const int32_t* __restrict__ cidx, int cnx, int cny, int cnz,
+                            int32_t* __restrict__ ckey, int32_t* __restrict__ ccount) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {
+        const float4 p = xq[t];
+        const int cx = min(nx - 1, max(0, (int)(p.x * ((float)nx / box.x))));
+        const int cy = min(ny - 1, max(0, (int)(p.y * ((float)ny / box.y))));
+        const int cz = min(nz - 1, max(0, (int)(p.z * ((float)nz / box.z))));
+        const int k = (cy * nx + cx) * nz + cz;
+        key[t] = k;
+        atomicAdd(&count[k], 1);
+    } else if (t < n + m) {
+        const int c = t - n;
+        const float4 p = xq[cidx[c]];
+        const int cx = min(cnx - 1, max(0, (int)(p.x * ((float)cnx / box.x))));
+        const int cy = min(cny - 1, max(0, (int)(p.y * ((float)cny / box.y))));
+        const int cz = min(cnz - 1, max(0, (int)(p.z * ((float)cnz / box.z))));
+        const int k = (cz * cny + cy) * cnx + cx;
+        ckey[c] = k;
+        atomicAdd(&ccount[k], 1);
+    }
 }
 
 // Start slot of every column (exclusive scan of its bead count rounded up to
@@ -170,14 +195,6 @@ __global__ void __launch_bounds__(1024) k_col_scan(int ncols, int nz, const int3
     if (t == 1023) col_start[ncols] = part[1023];
 }
 
-__global__ void k_bucket_scatter(int n, const int32_t* __restrict__ key,
-                                 const int32_t* __restrict__ start, int32_t* __restrict__ fill,
-                                 int32_t* __restrict__ bucket) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int k = key[i];
-    bucket[start[k] + atomicAdd(&fill[k], 1)] = i;
-}
 
 // Cluster order: columns one after another (each padded to whole clusters),
 // inside a column the z slices bottom-up, inside a slice ascending index.
@@ -502,30 +519,26 @@ __global__ void k_excl(int nnz, int nc, int tile_cap, const int32_t* __restrict_
 // not, because each pair's force is rounded to fixed point before it is
 // summed.
 // ---------------------------------------------------------------------------
-__global__ void k_chg_keys(int m, const int32_t* __restrict__ idx, const float4* __restrict__ xq,
-                           int nx, int ny, int nz, float3 box, int32_t* __restrict__ key,
-                           int32_t* __restrict__ count) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= m) return;
-    const float4 p = xq[idx[t]];
-    const int cx = min(nx - 1, max(0, (int)(p.x * ((float)nx / box.x))));
-    const int cy = min(ny - 1, max(0, (int)(p.y * ((float)ny / box.y))));
-    const int cz = min(nz - 1, max(0, (int)(p.z * ((float)nz / box.z))));
-    const int k = (cz * ny + cy) * nx + cx;
-    key[t] = k;
-    atomicAdd(&count[k], 1);
-}
 
-// Charged beads grouped by cell: position and bead index (in w) together,
-// so the row build reads one contiguous record per candidate.
-__global__ void k_chg_scatter(int m, const int32_t* __restrict__ idx, const int32_t* __restrict__ key,
-                              const float4* __restrict__ xq, const int32_t* __restrict__ start,
-                              int32_t* __restrict__ fill, float4* __restrict__ sorted) {
+// Bucket scatter of the beads and, in the same launch, of the charged
+// beads, whose records (position, bead index in w) are grouped by cell so
+// the row build reads one contiguous record per candidate: threads [0, n)
+// and [n, n + m).
+__global__ void k_scatter_both(int n, const int32_t* __restrict__ key, const int32_t* __restrict__ start,
+                               int32_t* __restrict__ fill, int32_t* __restrict__ bucket, int m,
+                               const int32_t* __restrict__ cidx, const int32_t* __restrict__ ckey,
+                               const float4* __restrict__ xq, const int32_t* __restrict__ cstart,
+                               int32_t* __restrict__ cfill, float4* __restrict__ sorted) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= m) return;
-    const int k = key[t], i = idx[t];
-    const float4 p = xq[i];
-    sorted[start[k] + atomicAdd(&fill[k], 1)] = make_float4(p.x, p.y, p.z, __int_as_float(i));
+    if (t < n) {
+        const int k = key[t];
+        bucket[start[k] + atomicAdd(&fill[k], 1)] = t;
+    } else if (t < n + m) {
+        const int c = t - n;
+        const int k = ckey[c], i = cidx[c];
+        const float4 p = xq[i];
+        sorted[cstart[k] + atomicAdd(&cfill[k], 1)] = make_float4(p.x, p.y, p.z, __int_as_float(i));
+    }
 }
 
 // One warp per charged bead: the 27 neighbour cells (the three cells of a
@@ -547,6 +560,9 @@ __global__ void k_chg_rows(int m, const int32_t* __restrict__ idx, const int32_t
     const int k = key[t];
     const int cx = k % nx, cy = (k / nx) % ny, cz = k / (nx * ny);
     const int e0 = ex_csr[i], e1 = ex_csr[i + 1];
+    // the row's excluded partners span [ex_lo, ex_hi] (sorted): candidates
+    // outside skip the search
+    const int ex_lo = e0 < e1 ? ex_j[e0] : 1, ex_hi = e0 < e1 ? ex_j[e1 - 1] : 0;
     int32_t* row = rows + (size_t)t * row_cap;
     int len = 0;
     for (int dz = -1; dz <= 1; ++dz)
@@ -566,7 +582,7 @@ __global__ void k_chg_rows(int m, const int32_t* __restrict__ idx, const int32_t
                         if (j != i) {
                             const float r2 = norm2(separation<true>(xi, c, box, inv_box));
                             keep = r2 < cut2;
-                            if (keep && e0 < e1) {
+                            if (keep && j >= ex_lo && j <= ex_hi) {
                                 int lo = e0, hi = e1;  // this row's exclusions, sorted by j
                                 while (lo < hi) {
                                     const int mid = (lo + hi) >> 1;
@@ -1397,15 +1413,29 @@ void PlainContext::rebuild(cudaStream_t s) {
     const int np_i = (int)np, n_i = (int)n, nc_i = (int)nc;
     if (reorder) {
         const int ncols = cell_dims_[0] * cell_dims_[1];
+        // the charged beads' cell sort rides along in the same launches
+        const int m = charged_split_ ? (int)n_charged_ : 0;
         OCM_CK(cudaMemsetAsync(cell_count_.p, 0, n_cells_ * sizeof(int32_t), s));
         OCM_CK(cudaMemsetAsync(cell_fill_.p, 0, n_cells_ * sizeof(int32_t), s));
         OCM_CK(cudaMemsetAsync(perm_.p, 0xff, np * sizeof(int32_t), s));
-        k_cell_keys<<<div_up(n, 256), 256, 0, s>>>(n_i, xq_.p, cell_dims_[0], cell_dims_[1],
-                                                   cell_dims_[2], box_, cell_key_.p, cell_count_.p);
-        k_scan<<<1, 1024, 0, s>>>((int)n_cells_, cell_count_.p, cell_start_.p);
+        if (m > 0) {
+            OCM_CK(cudaMemsetAsync(chg_count_.p, 0, n_charged_cells_ * sizeof(int32_t), s));
+            OCM_CK(cudaMemsetAsync(chg_fill_.p, 0, n_charged_cells_ * sizeof(int32_t), s));
+            OCM_CK(cudaMemsetAsync(chg_stats_.p, 0, 2 * sizeof(int32_t), s));
+        }
+        k_keys_both<<<div_up(n + m, 256), 256, 0, s>>>(n_i, xq_.p, cell_dims_[0], cell_dims_[1], cell_dims_[2],
+                                                       box_, cell_key_.p, cell_count_.p, m, chg_idx_.p,
+                                                       charged_cells_[0], charged_cells_[1], charged_cells_[2],
+                                                       chg_key_.p, chg_count_.p);
+        if (m > 0)
+            k_scan2<<<2, 1024, 0, s>>>((int)n_cells_, cell_count_.p, cell_start_.p, (int)n_charged_cells_,
+                                       chg_count_.p, chg_start_.p);
+        else
+            k_scan<<<1, 1024, 0, s>>>((int)n_cells_, cell_count_.p, cell_start_.p);
         k_col_scan<<<1, 1024, 0, s>>>(ncols, cell_dims_[2], cell_start_.p, col_start_.p);
-        k_bucket_scatter<<<div_up(n, 256), 256, 0, s>>>(n_i, cell_key_.p, cell_start_.p,
-                                                        cell_fill_.p, bucket_.p);
+        k_scatter_both<<<div_up(n + m, 256), 256, 0, s>>>(n_i, cell_key_.p, cell_start_.p, cell_fill_.p,
+                                                          bucket_.p, m, chg_idx_.p, chg_key_.p, xq_.p,
+                                                          chg_start_.p, chg_fill_.p, chg_sorted_.p);
         k_bucket_rank<<<div_up(n, 256), 256, 0, s>>>(n_i, cell_dims_[2], cell_key_.p, cell_start_.p,
                                                      col_start_.p, bucket_.p, perm_.p);
     }
@@ -1460,15 +1490,8 @@ void PlainContext::rebuild(cudaStream_t s) {
     }
     OCM_CK(cudaGetLastError());
     if (charged_split_) {
+        // cell sort done with the beads' (the split implies the reordered layout)
         const int m = (int)n_charged_;
-        OCM_CK(cudaMemsetAsync(chg_count_.p, 0, n_charged_cells_ * sizeof(int32_t), s));
-        OCM_CK(cudaMemsetAsync(chg_fill_.p, 0, n_charged_cells_ * sizeof(int32_t), s));
-        OCM_CK(cudaMemsetAsync(chg_stats_.p, 0, 2 * sizeof(int32_t), s));
-        k_chg_keys<<<div_up(m, 256), 256, 0, s>>>(m, chg_idx_.p, xq_.p, charged_cells_[0], charged_cells_[1],
-                                                  charged_cells_[2], box_, chg_key_.p, chg_count_.p);
-        k_scan<<<1, 1024, 0, s>>>((int)n_charged_cells_, chg_count_.p, chg_start_.p);
-        k_chg_scatter<<<div_up(m, 256), 256, 0, s>>>(m, chg_idx_.p, chg_key_.p, xq_.p, chg_start_.p, chg_fill_.p,
-                                                     chg_sorted_.p);
         const float ccut = (float)(std::sqrt((double)cs.pc.dh_rc2) + skin) * 1.0001f + 1e-4f;
         k_chg_rows<<<div_up((int64_t)m * 32, 128), 128, 0, s>>>(
             m, chg_idx_.p, chg_key_.p, xq_.p, charged_cells_[0], charged_cells_[1], charged_cells_[2], box_,
