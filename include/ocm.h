@@ -188,6 +188,55 @@ int ocm_add_lennard_jones_attractive(ocm_system* sys, double cutoff_ratio,
                                      const int32_t* ignore_group_pairs,
                                      const int32_t* group_vec, int* group_out);
 
+/* WeeksChandlerAndersenForceFieldGenerator(sigmas, epsilons, ignore_list,
+ * use_periodic, ignore_group_pairs, group_vec)
+ * (WeeksChandlerAndersenForceFieldGenerator.cpp:9-113):
+ * step(2^(1/6) s - r) (4 e ((s/r)^12 - (s/r)^6) + e), s the arithmetic and e
+ * the geometric mean, cutoff 2^(1/6) (s_max + s_2nd) / 2.  It shares the
+ * repulsive Lennard-Jones pair slot: a system holds at most one of
+ * LennardJonesRepulsive, WeeksChandlerAndersen, UniformWeeksChadlerAndersen
+ * (else OCM_ERR_UNSUPPORTED).  NaN sigma and epsilon = no participation. */
+int ocm_add_weeks_chandler_andersen(ocm_system* sys, const double* sigmas, const double* epsilons,
+                                    int64_t n_ignore, const int64_t* ignore_pairs, int use_periodic,
+                                    int64_t n_ignore_groups, const int32_t* ignore_group_pairs,
+                                    const int32_t* group_vec, int* group_out);
+/* UniformWeeksChandlerAndersenForceFieldGenerator(system_size, eps, sigma,
+ * former_group_vec, latter_group_vec, ignore_list, use_periodic,
+ * ignore_group_pairs, group_vec)
+ * (UniformWeeksChandlerAndersenForceFieldGenerator.cpp:9-185):
+ * 4 eps ((sigma/r)^12 - (sigma/r)^6 + 1/4) for pairs between the `former`
+ * and `latter` particle lists, cutoff 2^(1/6) sigma; force group
+ * "UniformWeeksChadlerAndersen" (the reference's spelling). */
+int ocm_add_uniform_weeks_chandler_andersen(ocm_system* sys, double eps, double sigma,
+                                            int64_t n_former, const int64_t* former,
+                                            int64_t n_latter, const int64_t* latter,
+                                            int64_t n_ignore, const int64_t* ignore_pairs,
+                                            int use_periodic, int64_t n_ignore_groups,
+                                            const int32_t* ignore_group_pairs,
+                                            const int32_t* group_vec, int* group_out);
+/* UniformLennardJonesAttractiveForceFieldGenerator(system_size, eps, sigma,
+ * cutoff_ratio, former_group_vec, latter_group_vec, ...)
+ * (UniformLennardJonesAttractiveForceFieldGenerator.cpp:11-189): the
+ * attractive Lennard-Jones form with one sigma and epsilon, cutoff
+ * sigma * cutoff_ratio, switched from 0.9 cutoff; shares the attractive
+ * Lennard-Jones pair slot (one per system). */
+int ocm_add_uniform_lennard_jones_attractive(ocm_system* sys, double eps, double sigma,
+                                             double cutoff_ratio, int64_t n_former,
+                                             const int64_t* former, int64_t n_latter,
+                                             const int64_t* latter, int64_t n_ignore,
+                                             const int64_t* ignore_pairs, int use_periodic,
+                                             int64_t n_ignore_groups,
+                                             const int32_t* ignore_group_pairs,
+                                             const int32_t* group_vec, int* group_out);
+/* CappedGoContactForceFieldGenerator(indices, ks, r0s, capping_ratio,
+ * use_periodic) (CappedGoContactForceFieldGenerator.hpp:14-47, .cpp:5-31):
+ * k (5 (r0/r)^12 - 6 (r0/r)^10) for r > cap r0, below it the linear
+ * continuation k (slope r / r0 + intercept) with slope = -60 (cap^-13 -
+ * cap^-11), intercept = 65 cap^-12 - 66 cap^-10. */
+int ocm_add_capped_go_contact(ocm_system* sys, int64_t n, const int64_t* indices, const double* ks,
+                              const double* r0s, double capping_ratio, int use_periodic,
+                              int* group_out);
+
 /* ---------------------------------------------------------------------------
  * Plain single-system path.  ocm_context_create replaces
  * LangevinIntegratorGenerator::generate (IntegratorGenerator.cpp:5-14:
@@ -225,7 +274,7 @@ typedef struct ocm_context_stats {
     int64_t tiles;            /* cluster-pair tiles in the current list */
     int64_t masked_tiles;     /* tiles carrying exclusion masks */
     int32_t rebuild_interval; /* steps between list builds */
-    int32_t reordered;        /* 1 if beads are Morton-sorted into clusters */
+    int32_t reordered;        /* 1 if beads are sorted into column clusters */
     double  skin;             /* nm */
     double  max_cutoff;       /* nm */
     double  tile_cutoff;      /* nm: largest cutoff the cluster-pair tiles serve */

@@ -79,6 +79,15 @@ SIGNATURES = {
                                                   C.c_int64, _I32P, _I32P, _I32P]),
     "ocm_add_lennard_jones_attractive": (C.c_int, [_P, C.c_double, _DP, _DP, C.c_int64, _I64P, C.c_int,
                                                    C.c_int64, _I32P, _I32P, _I32P]),
+    "ocm_add_weeks_chandler_andersen": (C.c_int, [_P, _DP, _DP, C.c_int64, _I64P, C.c_int,
+                                                  C.c_int64, _I32P, _I32P, _I32P]),
+    "ocm_add_uniform_weeks_chandler_andersen": (C.c_int, [_P, C.c_double, C.c_double, C.c_int64, _I64P,
+                                                          C.c_int64, _I64P, C.c_int64, _I64P, C.c_int,
+                                                          C.c_int64, _I32P, _I32P, _I32P]),
+    "ocm_add_uniform_lennard_jones_attractive": (C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int64,
+                                                           _I64P, C.c_int64, _I64P, C.c_int64, _I64P, C.c_int,
+                                                           C.c_int64, _I32P, _I32P, _I32P]),
+    "ocm_add_capped_go_contact": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP, C.c_double, C.c_int, _I32P]),
     "ocm_context_create": (C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int,
                                      C.POINTER(_P)]),
     "ocm_context_destroy": (None, [_P]),

@@ -655,7 +655,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                         const int b = t - n_ad;
                         const uint32_t ij = bij[b];
                         const int kind = (int)(ij >> 30);
-                        const int sl = kind == kBondHarmonic ? kSlotHB : (kind == kBondGo ? kSlotGO : kSlotGB);
+                        const int sl = bond_slot(kind);
                         if (!(slots_en & (1u << sl))) continue;
                         const int bi = ij & 0xFFFF, bj = (ij >> 16) & 0x3FFF;
                         const float4 bp = bpar[b];

@@ -390,6 +390,70 @@ int ocm_add_lennard_jones_attractive(ocm_system* s, double ratio, const double* 
     return add_lj(true, s, ratio, eps, sig, n_ignore, ignore, use_periodic, n_ig, igp, gv, group_out);
 }
 
+int ocm_add_weeks_chandler_andersen(ocm_system* s, const double* sig, const double* eps, int64_t n_ignore,
+                                    const int64_t* ignore, int use_periodic, int64_t n_ig,
+                                    const int32_t* igp, const int32_t* gv, int* group_out) {
+    return guard([&] {
+        need(s, "system");
+        const int64_t n = (int64_t)s->g.desc().masses.size();
+        auto g = std::make_unique<ocm::WeeksChandlerAndersenForceFieldGenerator>(
+            copy_vec(sig, n, "sigmas"), copy_vec(eps, n, "epsilons"),
+            common_args(s, n_ignore, ignore, use_periodic, n_ig, igp, gv));
+        const int grp = s->g.add_ff_generator(std::move(g));
+        if (group_out) *group_out = grp;
+    });
+}
+
+static std::vector<int64_t> index_list(int64_t n, const int64_t* v, const char* what) {
+    if (n < 0) throw ocm::Error(1, "[error] negative count");
+    if (n) need(v, what);
+    return std::vector<int64_t>(v, v + n);
+}
+
+static int add_uniform(bool attr, ocm_system* s, double eps, double sigma, double ratio, int64_t n_former,
+                       const int64_t* former, int64_t n_latter, const int64_t* latter, int64_t n_ignore,
+                       const int64_t* ignore, int use_periodic, int64_t n_ig, const int32_t* igp,
+                       const int32_t* gv, int* group_out) {
+    return guard([&] {
+        need(s, "system");
+        const int64_t n = (int64_t)s->g.desc().masses.size();
+        auto g = std::make_unique<ocm::UniformPairForceFieldGenerator>(
+            attr, n, eps, sigma, ratio, index_list(n_former, former, "former"),
+            index_list(n_latter, latter, "latter"),
+            common_args(s, n_ignore, ignore, use_periodic, n_ig, igp, gv));
+        const int grp = s->g.add_ff_generator(std::move(g));
+        if (group_out) *group_out = grp;
+    });
+}
+int ocm_add_uniform_weeks_chandler_andersen(ocm_system* s, double eps, double sigma, int64_t n_former,
+                                            const int64_t* former, int64_t n_latter, const int64_t* latter,
+                                            int64_t n_ignore, const int64_t* ignore, int use_periodic,
+                                            int64_t n_ig, const int32_t* igp, const int32_t* gv,
+                                            int* group_out) {
+    return add_uniform(false, s, eps, sigma, 0.0, n_former, former, n_latter, latter, n_ignore, ignore,
+                       use_periodic, n_ig, igp, gv, group_out);
+}
+int ocm_add_uniform_lennard_jones_attractive(ocm_system* s, double eps, double sigma, double cutoff_ratio,
+                                             int64_t n_former, const int64_t* former, int64_t n_latter,
+                                             const int64_t* latter, int64_t n_ignore, const int64_t* ignore,
+                                             int use_periodic, int64_t n_ig, const int32_t* igp,
+                                             const int32_t* gv, int* group_out) {
+    return add_uniform(true, s, eps, sigma, cutoff_ratio, n_former, former, n_latter, latter, n_ignore,
+                       ignore, use_periodic, n_ig, igp, gv, group_out);
+}
+
+int ocm_add_capped_go_contact(ocm_system* s, int64_t n, const int64_t* idx, const double* ks,
+                              const double* r0s, double capping_ratio, int use_periodic, int* group_out) {
+    return guard([&] {
+        need(s, "system");
+        auto g = std::make_unique<ocm::CappedGoContactForceFieldGenerator>(
+            pairs_of(idx, n), copy_vec(ks, n, "ks"), copy_vec(r0s, n, "r0s"), capping_ratio,
+            use_periodic != 0);
+        const int grp = s->g.add_ff_generator(std::move(g));
+        if (group_out) *group_out = grp;
+    });
+}
+
 // ---------------- plain context ----------------
 int ocm_context_create(const ocm_system* s, double T, double friction, double dt, int32_t seed,
                        int device, ocm_context** out) {

@@ -113,7 +113,9 @@ __device__ __forceinline__ float pair_scalar(float r2, float4 pi, float4 pj, flo
             sig2 = sig * sig;
         }
         if (r2 <= sig2 * kTwoPow1_3) {
-            const float eps = 0.5f * (pi.z + pj.z);
+            // arithmetic epsilon (LennardJonesRepulsive) or geometric (WCA:
+            // p0.z holds sqrt(eps))
+            const float eps = pc.ljr_geometric ? pi.z * pj.z : 0.5f * (pi.z + pj.z);
             float s6 = sh_s6, s12 = sh_s12;
             if (!(TERMS & kLJSameSigma)) {
                 const float s2 = sig2 * r2inv;
@@ -171,7 +173,8 @@ __device__ __forceinline__ float pair_scalar(float r2, float4 pi, float4 pj, flo
 // (GaussianBondForceFieldGenerator.cpp:5-7).
 // `delta` = r^2 - r0^2 (v0^2 for the Gaussian) evaluated without
 // cancellation by the caller: all three forces are proportional to it near
-// the centre, where an FP32 r - r0 would lose its digits.  For a Gaussian
+// the centre, where an FP32 r - r0 would lose its digits.  For a capped Go
+// contact p1 = 1 / cap and p2 = the high part of r0^2.  For a Gaussian
 // bond p1 = 1 / (2 sigma^2) and p2 = the high part of v0^2 (v0 enters only
 // the r + v0 denominator).  Returns s with F_a = s * (x_a - x_b).
 __device__ __forceinline__ float bond_scalar(int kind, float r2, float delta, float p0, float p1,
@@ -187,9 +190,26 @@ __device__ __forceinline__ float bond_scalar(int kind, float r2, float delta, fl
         const float e = p0 * expf(-dr * dr * p1);
         energy = e;
         return 2.f * p1 * dr * e / r;
-    } else {  // Go: p0 = k, p1 = r0;  t^2 - 1 = -delta / r^2
+    } else if (kind == kBondGo) {  // Go: p0 = k, p1 = r0;  t^2 - 1 = -delta / r^2
         const float inv = 1.f / r2;
         const float t2 = p1 * p1 * inv;
+        const float t10 = t2 * t2 * t2 * t2 * t2;
+        energy = p0 * t10 * (5.f * t2 - 6.f);
+        return -60.f * p0 * t10 * delta * inv * inv;
+    } else {  // capped Go: p0 = k, p1 = u = 1 / cap, p2 ~ r0^2
+        // r <= cap r0: the linear continuation k (slope r / r0 + intercept),
+        // slope = -60 (u^13 - u^11), intercept = 65 u^12 - 66 u^10, which
+        // meets the Go form with its first derivative at r = cap r0
+        // (CappedGoContactForceFieldGenerator.cpp); beyond it the Go form.
+        if (r2 * p1 * p1 <= p2) {
+            const float r = sqrtf(r2), r0 = sqrtf(p2);
+            const float u2 = p1 * p1, u10 = u2 * u2 * u2 * u2 * u2;
+            const float slope = -60.f * u10 * p1 * (u2 - 1.f);
+            energy = p0 * (slope * r / r0 + u10 * (65.f * u2 - 66.f));
+            return -p0 * slope / (r0 * r);
+        }
+        const float inv = 1.f / r2;
+        const float t2 = p2 * inv;
         const float t10 = t2 * t2 * t2 * t2 * t2;
         energy = p0 * t10 * (5.f * t2 - 6.f);
         return -60.f * p0 * t10 * delta * inv * inv;

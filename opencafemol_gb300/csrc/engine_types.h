@@ -32,12 +32,22 @@ enum EnergySlot {
     kSlotFLD = 7,
     kSlotGB = 8,   // Gaussian bond (AICG2+)
     kSlotGD = 9,   // Gaussian dihedral (AICG2+)
-    kNumSlots = 10
+    kSlotCGO = 10, // capped Go contact
+    kNumSlots = 11
 };
 
 constexpr int kBondHarmonic = 0;
 constexpr int kBondGo = 1;
 constexpr int kBondGauss = 2;
+constexpr int kBondCappedGo = 3;
+
+// Energy slot of a bond kind.
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline int bond_slot(int kind) {
+    return kind == kBondHarmonic ? kSlotHB : kind == kBondGo ? kSlotGO : kind == kBondGauss ? kSlotGB : kSlotCGO;
+}
 
 constexpr int kDihFLD = 0;
 constexpr int kDihGauss = 1;
@@ -60,7 +70,7 @@ struct PairConsts {
     float list_rc2;  // largest pair cutoff squared
     int terms;       // kTerm* bits present
     int uses_labels; // bit t: term t has interaction groups
-    int pad_;
+    int ljr_geometric;  // repulsive LJ slot mixes epsilon geometrically (WCA): p0.z holds sqrt(eps)
     unsigned long long allow[kNumPairTerms];  // label-pair matrix per term (8x8 bits)
 };
 
@@ -80,9 +90,9 @@ struct FldTable {
 // Explicit bond-like term (harmonic bond, Go contact or Gaussian bond).
 struct BondTerm {
     int32_t i, j;
-    int32_t kind;      // kBondHarmonic / kBondGo / kBondGauss
+    int32_t kind;      // kBondHarmonic / kBondGo / kBondGauss / kBondCappedGo
     int32_t periodic;  // minimum image when nonzero
-    float p0, p1;      // (r0, k) harmonic; (k, r0) Go; (k, 1 / (2 sigma^2)) Gaussian
+    float p0, p1;      // (r0, k) harmonic; (k, r0) Go; (k, 1 / (2 sigma^2)) Gaussian; (k, 1 / cap) capped Go
     float r0sq_hi, r0sq_lo;  // r0^2 (v0^2 for the Gaussian) as an unevaluated float sum
 };
 struct AngleTerm {

@@ -460,6 +460,160 @@ GeneratedForce LennardJonesForceFieldGenerator::generate() const {
     return f;
 }
 
+// Largest and second-largest value of the defined entries (the reference's
+// scan, which starts both from the smallest positive double).
+static std::pair<double, double> two_largest(const std::vector<double>& v) {
+    double m1 = std::numeric_limits<double>::min(), m2 = std::numeric_limits<double>::min();
+    for (double s : v) {
+        if (std::isnan(s)) continue;
+        if (m1 <= s) {
+            m2 = m1;
+            m1 = s;
+        } else if (m2 <= s) {
+            m2 = s;
+        }
+    }
+    return {m1, m2};
+}
+
+WeeksChandlerAndersenForceFieldGenerator::WeeksChandlerAndersenForceFieldGenerator(
+    std::vector<double> sigmas, std::vector<double> eps, PairGeneratorCommon common)
+    : sigma_(std::move(sigmas)), eps_(std::move(eps)), c_(std::move(common)) {
+    if (sigma_.size() != eps_.size())
+        throw Error(1, "WCA: sigma.size(=" + sz(sigma_.size()) + ") must be the same as epsilon.size(=" +
+                           sz(eps_.size()) + ")");
+    for (std::size_t i = 0; i < sigma_.size(); ++i) {
+        if (std::isnan(sigma_[i]) != std::isnan(eps_[i]))
+            throw Error(1, "WCA: if particle i(=" + sz(i) +
+                               ") has sigma, it should have epsilon too, and vice versa.");
+        if (eps_[i] < 0) throw Error(1, "WCA: epsilon of particle " + sz(i) + " is negative");
+    }
+    groups_ = extract_interaction_group(has_values(sigma_), c_.ignore_group_pairs, c_.group_vec);
+}
+GeneratedForce WeeksChandlerAndersenForceFieldGenerator::generate() const {
+    GeneratedForce f;
+    f.kind = ForceKind::WeeksChandlerAndersen;
+    f.name = name();
+    f.periodic = c_.use_periodic;
+    const auto m = two_largest(sigma_);
+    f.cutoff = (m.first + m.second) * 0.5 * std::pow(2.0, 1.0 / 6.0);
+    f.pp0 = eps_;
+    f.pp1 = sigma_;
+    f.exclusions = c_.ignore_list;
+    f.groups = groups_;
+    return f;
+}
+
+// Interaction groups of a uniform generator between `former` and `latter`
+// (UniformLennardJonesAttractiveForceFieldGenerator.cpp:28-138): without
+// group-based ignores the one group (former, latter).  Otherwise each side
+// splits into the members of every group named in an ignored pair and the
+// rest ("others"); the groups are (others, named), (others, others),
+// (named, others) and (named a, named b) unless (a, b) is ignored.
+static GroupPairs uniform_groups(const std::vector<int64_t>& former, const std::vector<int64_t>& latter,
+                                 const std::vector<std::pair<int, int>>& ignore_pairs,
+                                 const std::vector<int>& group_vec) {
+    GroupPairs out;
+    auto as_set = [](const std::vector<int64_t>& v) {
+        std::set<int> r;
+        for (int64_t i : v) r.insert((int)i);
+        return r;
+    };
+    if (ignore_pairs.empty()) {
+        out.emplace_back(as_set(former), as_set(latter));
+        return out;
+    }
+    std::set<int> related;
+    for (const auto& p : ignore_pairs) {
+        related.insert(p.first);
+        related.insert(p.second);
+    }
+    auto split = [&](const std::vector<int64_t>& side, std::map<int, std::set<int>>& named,
+                     std::set<int>& others) {
+        for (int g : related) named[g];
+        for (int64_t i : side) {
+            const int g = group_vec.empty() ? -1 : group_vec[i];
+            if (g >= 0 && related.count(g)) named[g].insert((int)i);
+            else others.insert((int)i);
+        }
+    };
+    std::map<int, std::set<int>> fnamed, lnamed;
+    std::set<int> fothers, lothers;
+    split(former, fnamed, fothers);
+    split(latter, lnamed, lothers);
+    auto push = [&](const std::set<int>& a, const std::set<int>& b) {
+        if (!a.empty() && !b.empty()) out.emplace_back(a, b);  // an empty side adds no pair
+    };
+    if (!fothers.empty()) {
+        for (const auto& l : lnamed) push(fothers, l.second);
+        push(fothers, lothers);
+    }
+    for (const auto& f : fnamed) {
+        push(f.second, lothers);
+        for (const auto& l : lnamed) {
+            const bool ignored = std::find(ignore_pairs.begin(), ignore_pairs.end(),
+                                           std::make_pair(f.first, l.first)) != ignore_pairs.end();
+            if (!ignored) push(f.second, l.second);
+        }
+    }
+    return out;
+}
+
+UniformPairForceFieldGenerator::UniformPairForceFieldGenerator(bool attractive, int64_t system_size,
+                                                               double eps, double sigma, double ratio,
+                                                               std::vector<int64_t> former,
+                                                               std::vector<int64_t> latter,
+                                                               PairGeneratorCommon common)
+    : attractive_(attractive), n_(system_size), eps_(eps), sigma_(sigma), ratio_(ratio),
+      c_(std::move(common)) {
+    if (!(sigma_ > 0)) throw Error(1, "[error] " + name() + ": sigma must be positive");
+    if (!(eps_ >= 0)) throw Error(1, "[error] " + name() + ": epsilon must be >= 0");
+    if (attractive_ && !(ratio_ > 0)) throw Error(1, "[error] " + name() + ": cutoff ratio must be positive");
+    for (const auto* side : {&former, &latter})
+        for (int64_t i : *side)
+            if (i < 0 || i >= n_)
+                throw Error(1, "[error] " + name() + " : index " + std::to_string(i) +
+                                   " exceeds the system's largest index " + std::to_string(n_ - 1) + ".");
+    groups_ = uniform_groups(former, latter, c_.ignore_group_pairs, c_.group_vec);
+}
+GeneratedForce UniformPairForceFieldGenerator::generate() const {
+    GeneratedForce f;
+    f.kind = attractive_ ? ForceKind::LennardJonesAttractive : ForceKind::LennardJonesRepulsive;
+    f.name = name();
+    f.periodic = c_.use_periodic;
+    f.cutoff = attractive_ ? sigma_ * ratio_ : sigma_ * std::pow(2.0, 1.0 / 6.0);
+    if (attractive_) f.switch_distance = 0.9 * f.cutoff;
+    f.pp0.assign(n_, eps_);
+    f.pp1.assign(n_, sigma_);
+    f.exclusions = c_.ignore_list;
+    f.groups = groups_;
+    if (f.groups.empty()) f.groups.emplace_back(std::set<int>(), std::set<int>());  // nobody interacts
+    return f;
+}
+
+CappedGoContactForceFieldGenerator::CappedGoContactForceFieldGenerator(
+    std::vector<std::pair<int64_t, int64_t>> idx, std::vector<double> ks, std::vector<double> r0s,
+    double capping_ratio, bool use_periodic)
+    : idx_(std::move(idx)), ks_(std::move(ks)), r0s_(std::move(r0s)), cap_(capping_ratio),
+      periodic_(use_periodic) {
+    if (!(idx_.size() == ks_.size() && ks_.size() == r0s_.size()))
+        throw Error(1, "[error] CappedGoContactForceFieldGenerator : parameter number of indices_vec (" +
+                           sz(idx_.size()) + "), k (" + sz(ks_.size()) + ") and r0 (" + sz(r0s_.size()) +
+                           ") is not matched.The number of these parameters must be same.");
+    if (!(cap_ > 0)) throw Error(1, "[error] CappedGoContactForceFieldGenerator : capping ratio must be positive");
+}
+GeneratedForce CappedGoContactForceFieldGenerator::generate() const {
+    GeneratedForce f;
+    f.kind = ForceKind::CappedGoContact;
+    f.name = name();
+    f.periodic = periodic_;
+    for (std::size_t i = 0; i < idx_.size(); ++i) {
+        f.idx.push_back({idx_[i].first, idx_[i].second, -1, -1});
+        f.par.push_back({ks_[i], r0s_[i], cap_});
+    }
+    return f;
+}
+
 // ---------------------------------------------------------------------------
 // SystemGenerator
 // ---------------------------------------------------------------------------
@@ -636,6 +790,8 @@ CompiledSystem compile_system(const SystemDesc& d) {
             case ForceKind::ExcludedVolume: term = 0; slot = kSlotEXV; break;
             case ForceKind::DebyeHuckel: term = 1; slot = kSlotDH; break;
             case ForceKind::LennardJonesRepulsive: term = 2; slot = kSlotLJR; break;
+            case ForceKind::WeeksChandlerAndersen: term = 2; slot = kSlotLJR; break;
+            case ForceKind::CappedGoContact: slot = kSlotCGO; break;
             case ForceKind::LennardJonesAttractive: term = 3; slot = kSlotLJA; break;
             case ForceKind::HarmonicBond: slot = kSlotHB; break;
             case ForceKind::GoContact: slot = kSlotGO; break;
@@ -646,8 +802,12 @@ CompiledSystem compile_system(const SystemDesc& d) {
         }
         if (term >= 0) {
             const int bit = 1 << term;
+            if ((c.pc.terms & bit) && term == 2)
+                throw Error(6, "[error] " + f.name + ": LennardJonesRepulsive, WeeksChandlerAndersen and "
+                               "UniformWeeksChadlerAndersen share one pair slot; a system holds at most one of them");
             if (c.pc.terms & bit)
                 throw Error(6, "[error] more than one " + f.name + " force in one system");
+            if (f.kind == ForceKind::WeeksChandlerAndersen) c.pc.ljr_geometric = 1;
             c.pc.terms |= bit;
             if (pair_periodic >= 0 && pair_periodic != (int)f.periodic)
                 throw Error(6, "[error] pair forces mix periodic and non-periodic cutoffs");
@@ -693,6 +853,10 @@ CompiledSystem compile_system(const SystemDesc& d) {
                         c.p0[4 * i + 2] = part ? (float)a : 0.f;
                         c.p0[4 * i + 3] = part ? (float)b : 0.f;
                         break;
+                    case ForceKind::WeeksChandlerAndersen:  // sqrt(eps): the kernel multiplies
+                        c.p0[4 * i + 2] = part ? (float)std::sqrt(a) : 0.f;
+                        c.p0[4 * i + 3] = part ? (float)b : 0.f;
+                        break;
                     case ForceKind::LennardJonesAttractive:
                         c.p1[4 * i + 0] = part ? (float)a : 0.f;
                         c.p1[4 * i + 1] = part ? (float)b : 0.f;
@@ -717,7 +881,8 @@ CompiledSystem compile_system(const SystemDesc& d) {
                     c.pc.dh_rc2 = rc2;
                     c.pc.dh_corr = (float)f.cutoff_correction;
                     break;
-                case ForceKind::LennardJonesRepulsive: c.pc.ljr_rc2 = rc2; break;
+                case ForceKind::LennardJonesRepulsive:
+                case ForceKind::WeeksChandlerAndersen: c.pc.ljr_rc2 = rc2; break;
                 case ForceKind::LennardJonesAttractive:
                     c.pc.lja_rc2 = rc2;
                     c.pc.lja_rs = (float)f.switch_distance;
@@ -742,6 +907,21 @@ CompiledSystem compile_system(const SystemDesc& d) {
                 b.p1 = (float)f.par[t][1];
                 const double r0 = f.kind == ForceKind::HarmonicBond ? f.par[t][0] : f.par[t][1];
                 const double r0sq = r0 * r0;
+                b.r0sq_hi = (float)r0sq;
+                b.r0sq_lo = (float)(r0sq - (double)b.r0sq_hi);
+                if (b.i < 0 || b.j < 0) throw Error(1, "[error] negative particle index");
+                c.bonds.push_back(b);
+            }
+        } else if (f.kind == ForceKind::CappedGoContact) {
+            for (std::size_t t = 0; t < f.idx.size(); ++t) {
+                BondTerm b{};
+                b.i = (int32_t)f.idx[t][0];
+                b.j = (int32_t)f.idx[t][1];
+                b.kind = kBondCappedGo;
+                b.periodic = f.periodic ? 1 : 0;
+                b.p0 = (float)f.par[t][0];                // k
+                b.p1 = (float)(1.0 / f.par[t][2]);        // 1 / capping ratio
+                const double r0sq = f.par[t][1] * f.par[t][1];
                 b.r0sq_hi = (float)r0sq;
                 b.r0sq_lo = (float)(r0sq - (double)b.r0sq_hi);
                 if (b.i < 0 || b.j < 0) throw Error(1, "[error] negative particle index");

@@ -86,7 +86,8 @@ GroupPairs extract_interaction_group(const std::vector<bool>& has_value,
 // ---------------------------------------------------------------------------
 enum class ForceKind { HarmonicBond, GoContact, FlexibleLocalAngle, FlexibleLocalDihedral,
                        ExcludedVolume, DebyeHuckel, LennardJonesRepulsive,
-                       LennardJonesAttractive, GaussianBond, GaussianDihedral };
+                       LennardJonesAttractive, GaussianBond, GaussianDihedral,
+                       WeeksChandlerAndersen, CappedGoContact };
 
 struct GeneratedForce {
     ForceKind kind;
@@ -260,6 +261,63 @@ class LennardJonesForceFieldGenerator final : public ForceFieldGeneratorBase {
     std::vector<double> eps_, sigma_;
     PairGeneratorCommon c_;
     GroupPairs groups_;
+};
+
+// WeeksChandlerAndersenForceFieldGenerator (WeeksChandlerAndersenForceFieldGenerator.cpp:9-113):
+// step(2^(1/6) s - r) (4 e ((s/r)^12 - (s/r)^6) + e) with s the arithmetic and
+// e the geometric mean of the pair's parameters; cutoff 2^(1/6) (s_max + s_2nd) / 2.
+class WeeksChandlerAndersenForceFieldGenerator final : public ForceFieldGeneratorBase {
+  public:
+    WeeksChandlerAndersenForceFieldGenerator(std::vector<double> sigmas, std::vector<double> eps,
+                                             PairGeneratorCommon common);
+    GeneratedForce generate() const override;
+    std::string name() const override { return "WeeksChandlerAndersen"; }
+  private:
+    std::vector<double> sigma_, eps_;
+    PairGeneratorCommon c_;
+    GroupPairs groups_;
+};
+
+// Uniform pair generators: one sigma and epsilon for every pair between the
+// particle sets `former` and `latter`.
+//  * UniformWeeksChandlerAndersenForceFieldGenerator (UniformWeeksChandlerAndersenForceFieldGenerator.cpp:9-185):
+//    4 e ((s/r)^12 - (s/r)^6 + 1/4), cutoff 2^(1/6) s;
+//  * UniformLennardJonesAttractiveForceFieldGenerator (UniformLennardJonesAttractiveForceFieldGenerator.cpp:11-189):
+//    e (step(r - t) 4 ((s/r)^12 - (s/r)^6) - step(t - r)), t = 2^(1/6) s,
+//    cutoff s * cutoff_ratio, switched from 0.9 cutoff.
+class UniformPairForceFieldGenerator final : public ForceFieldGeneratorBase {
+  public:
+    UniformPairForceFieldGenerator(bool attractive, int64_t system_size, double eps, double sigma,
+                                   double cutoff_ratio, std::vector<int64_t> former,
+                                   std::vector<int64_t> latter, PairGeneratorCommon common);
+    GeneratedForce generate() const override;
+    // the reference's own spelling of the WCA name
+    std::string name() const override {
+        return attractive_ ? "UniformLennardJonesAttractive" : "UniformWeeksChadlerAndersen";
+    }
+  private:
+    bool attractive_;
+    int64_t n_;
+    double eps_, sigma_, ratio_;
+    PairGeneratorCommon c_;
+    GroupPairs groups_;
+};
+
+// CappedGoContactForceFieldGenerator (CappedGoContactForceFieldGenerator.hpp:14-47,
+// .cpp:5-31): the Go 10-12 form beyond cap * r0, its linear continuation
+// k (slope r / r0 + intercept) below.
+class CappedGoContactForceFieldGenerator final : public ForceFieldGeneratorBase {
+  public:
+    CappedGoContactForceFieldGenerator(std::vector<std::pair<int64_t, int64_t>> idx,
+                                       std::vector<double> ks, std::vector<double> r0s,
+                                       double capping_ratio, bool use_periodic);
+    GeneratedForce generate() const override;
+    std::string name() const override { return "CappedGoContact"; }
+  private:
+    std::vector<std::pair<int64_t, int64_t>> idx_;
+    std::vector<double> ks_, r0s_;
+    double cap_;
+    bool periodic_;
 };
 
 // ---------------------------------------------------------------------------

@@ -823,10 +823,10 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
     if (blk < a.blocks_bonds) {
         // ------------ harmonic bonds, Go contacts, Gaussian bonds ------------
         const int t = blk * kForceThreads + threadIdx.x;
-        float eh = 0.f, eg = 0.f, eb = 0.f;
+        float eh = 0.f, eg = 0.f, eb = 0.f, ec = 0.f;
         if (t < a.n_bonds) {
             const BondTerm b = a.bonds[t];
-            const int slot = b.kind == kBondHarmonic ? kSlotHB : (b.kind == kBondGo ? kSlotGO : kSlotGB);
+            const int slot = bond_slot(b.kind);
             if (a.slots_enabled & (1u << slot)) {
                 double dx = a.x[b.j] - a.x[b.i], dy = a.y[b.j] - a.y[b.i], dz = a.z[b.j] - a.z[b.i];
                 if (b.periodic) {
@@ -843,15 +843,18 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                 add_force(a.F, a.n, b.j, make_float3(s * d.x, s * d.y, s * d.z));
                 if (b.kind == kBondHarmonic) eh = en;
                 else if (b.kind == kBondGo) eg = en;
-                else eb = en;
+                else if (b.kind == kBondGauss) eb = en;
+                else ec = en;
             }
         }
         if (ENERGY) {
-            const double vh = warp_sum((double)eh), vg = warp_sum((double)eg), vb = warp_sum((double)eb);
+            const double vh = warp_sum((double)eh), vg = warp_sum((double)eg), vb = warp_sum((double)eb),
+                         vc = warp_sum((double)ec);
             if (lane == 0) {
                 if (vh != 0.0) atomicAdd(&a.energy[kSlotHB], vh);
                 if (vg != 0.0) atomicAdd(&a.energy[kSlotGO], vg);
                 if (vb != 0.0) atomicAdd(&a.energy[kSlotGB], vb);
+                if (vc != 0.0) atomicAdd(&a.energy[kSlotCGO], vc);
             }
         }
         return;

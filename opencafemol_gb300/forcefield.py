@@ -25,6 +25,8 @@ __all__ = [
     "FlexibleLocalAngleForceFieldGenerator", "FlexibleLocalDihedralForceFieldGenerator",
     "ExcludedVolumeForceFieldGenerator", "DebyeHuckelForceFieldGenerator",
     "LennardJonesRepulsiveForceFieldGenerator", "LennardJonesAttractiveForceFieldGenerator",
+    "WeeksChandlerAndersenForceFieldGenerator", "UniformWeeksChandlerAndersenForceFieldGenerator",
+    "UniformLennardJonesAttractiveForceFieldGenerator", "CappedGoContactForceFieldGenerator",
     "SystemGenerator", "System", "LangevinIntegratorGenerator", "LangevinIntegrator",
     "fla_spline_table", "fla_second_derivative_table", "fld_fourier_table", "fld_table_keys",
     "AMINO_ACIDS",
@@ -357,6 +359,102 @@ class LennardJonesAttractiveForceFieldGenerator(LennardJonesRepulsiveForceFieldG
         check(lib.ocm_add_lennard_jones_attractive(h, self.cutoff_ratio, dptr(self.epsilons),
                                                    dptr(self.sigmas), *self._tail(len(self.sigmas)),
                                                    C.byref(g)))
+        return g.value
+
+
+class WeeksChandlerAndersenForceFieldGenerator(_PairGenerator):
+    """step(2^(1/6) s - r) (4 e ((s/r)^12 - (s/r)^6) + e); s arithmetic, e
+    geometric mean; cutoff 2^(1/6) (s_max + s_2nd) / 2."""
+
+    def __init__(self, sigmas, epsilons, ignore_list, use_periodic: bool, ignore_group_pairs=(), group_vec=()):
+        self.sigmas, self.epsilons = as_f64(sigmas), as_f64(epsilons)
+        if len(self.sigmas) != len(self.epsilons):
+            raise OCMError(1, f"WCA: sigma.size(={len(self.sigmas)}) must be the same as "
+                              f"epsilon.size(={len(self.epsilons)})")
+        self._common(ignore_list, use_periodic, ignore_group_pairs, group_vec)
+
+    def name(self) -> str:
+        return "WeeksChandlerAndersen"
+
+    def add_to(self, h) -> int:
+        g = C.c_int32()
+        check(lib.ocm_add_weeks_chandler_andersen(h, dptr(self.sigmas), dptr(self.epsilons),
+                                                  *self._tail(len(self.sigmas)), C.byref(g)))
+        return g.value
+
+
+class _UniformPairGenerator(_PairGenerator):
+    def _uniform(self, system_size, eps, sigma, former_group_vec, latter_group_vec):
+        self.system_size = int(system_size)
+        self.eps, self.sigma = float(eps), float(sigma)
+        self.former = np.ascontiguousarray(former_group_vec, np.int64).reshape(-1)
+        self.latter = np.ascontiguousarray(latter_group_vec, np.int64).reshape(-1)
+
+
+class UniformWeeksChandlerAndersenForceFieldGenerator(_UniformPairGenerator):
+    """4 eps ((sigma/r)^12 - (sigma/r)^6 + 1/4) between `former` and `latter`,
+    cutoff 2^(1/6) sigma."""
+
+    def __init__(self, system_size, eps, sigma, former_group_vec, latter_group_vec, ignore_list,
+                 use_periodic: bool, ignore_group_pairs=(), group_vec=()):
+        self._uniform(system_size, eps, sigma, former_group_vec, latter_group_vec)
+        self._common(ignore_list, use_periodic, ignore_group_pairs, group_vec)
+
+    def name(self) -> str:
+        return "UniformWeeksChadlerAndersen"  # the reference's spelling
+
+    def add_to(self, h) -> int:
+        g = C.c_int32()
+        check(lib.ocm_add_uniform_weeks_chandler_andersen(
+            h, self.eps, self.sigma, len(self.former), i64ptr(self.former), len(self.latter),
+            i64ptr(self.latter), *self._tail(self.system_size), C.byref(g)))
+        return g.value
+
+
+class UniformLennardJonesAttractiveForceFieldGenerator(_UniformPairGenerator):
+    """The attractive Lennard-Jones form with one sigma and epsilon between
+    `former` and `latter`; cutoff sigma * cutoff_ratio, switched from 0.9
+    cutoff."""
+
+    def __init__(self, system_size, eps, sigma, cutoff_ratio, former_group_vec, latter_group_vec,
+                 ignore_list, use_periodic: bool, ignore_group_pairs=(), group_vec=()):
+        self._uniform(system_size, eps, sigma, former_group_vec, latter_group_vec)
+        self.cutoff_ratio = float(cutoff_ratio)
+        self._common(ignore_list, use_periodic, ignore_group_pairs, group_vec)
+
+    def name(self) -> str:
+        return "UniformLennardJonesAttractive"
+
+    def add_to(self, h) -> int:
+        g = C.c_int32()
+        check(lib.ocm_add_uniform_lennard_jones_attractive(
+            h, self.eps, self.sigma, self.cutoff_ratio, len(self.former), i64ptr(self.former),
+            len(self.latter), i64ptr(self.latter), *self._tail(self.system_size), C.byref(g)))
+        return g.value
+
+
+class CappedGoContactForceFieldGenerator(_Generator):
+    """The Go 10-12 form beyond capping_ratio * r0, its linear continuation
+    (value and slope matched) below."""
+
+    def __init__(self, indices_vec, ks, r0s, capping_ratio: float, use_periodic: bool):
+        self.indices = _pairs_arg(indices_vec, 2)
+        self.ks, self.r0s = as_f64(ks), as_f64(r0s)
+        self.capping_ratio = float(capping_ratio)
+        self.use_periodic = bool(use_periodic)
+        if not (len(self.indices) == len(self.ks) == len(self.r0s)):
+            raise OCMError(1, "[error] CappedGoContactForceFieldGenerator : parameter number of "
+                              f"indices_vec ({len(self.indices)}), k ({len(self.ks)}) and "
+                              f"r0 ({len(self.r0s)}) is not matched.The number of these parameters must be same.")
+
+    def name(self) -> str:
+        return "CappedGoContact"
+
+    def add_to(self, h) -> int:
+        g = C.c_int32()
+        check(lib.ocm_add_capped_go_contact(h, len(self.indices), i64ptr(self.indices), dptr(self.ks),
+                                            dptr(self.r0s), self.capping_ratio, int(self.use_periodic),
+                                            C.byref(g)))
         return g.value
 
 

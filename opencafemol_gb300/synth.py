@@ -21,13 +21,16 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .forcefield import (AMINO_ACIDS, DebyeHuckelForceFieldGenerator,
+from .forcefield import (AMINO_ACIDS, CappedGoContactForceFieldGenerator, DebyeHuckelForceFieldGenerator,
                          ExcludedVolumeForceFieldGenerator, FlexibleLocalAngleForceFieldGenerator,
                          FlexibleLocalDihedralForceFieldGenerator, GaussianBondForceFieldGenerator,
                          GaussianDihedralForceFieldGenerator, GoContactForceFieldGenerator,
                          HarmonicBondForceFieldGenerator, LennardJonesAttractiveForceFieldGenerator,
                          LennardJonesRepulsiveForceFieldGenerator, System, SystemGenerator,
-                         Topology, fla_spline_table, fld_fourier_table, fld_table_keys)
+                         Topology, UniformLennardJonesAttractiveForceFieldGenerator,
+                         UniformWeeksChandlerAndersenForceFieldGenerator,
+                         WeeksChandlerAndersenForceFieldGenerator, fla_spline_table, fld_fourier_table,
+                         fld_table_keys)
 
 KJ_PER_KCAL = 4.184
 ANGSTROM_PER_NM = 10.0
@@ -49,6 +52,12 @@ class PairTerm:
     temperature: float = 300.0
     ign_bond: int = -1                 # exclusions within this many bonds (-1: none)
     ign_contact: int = -1              # exclusions within this many contacts
+    # Lennard-Jones slot variants: "" (the HPS generators), "wca"
+    # (WeeksChandlerAndersen, repulsive slot), "uniform" (the uniform
+    # generators: p0 / p1 hold one epsilon / sigma, `side` marks the
+    # former (bit 1) and latter (bit 2) particle lists)
+    kind: str = ""
+    side: np.ndarray | None = None
 
 
 @dataclass
@@ -81,6 +90,11 @@ class CGSpec:
     gd_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
     gd_theta0: np.ndarray = field(default_factory=lambda: np.zeros(0))
     gd_sigma: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    # capped Go contacts (one capping ratio for all)
+    cgo_idx: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int64))
+    cgo_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    cgo_r0: np.ndarray = field(default_factory=lambda: np.zeros(0))
+    cgo_cap: float = 0.8
     exv: PairTerm | None = None
     dh: PairTerm | None = None
     ljr: PairTerm | None = None
@@ -386,6 +400,9 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
         sg.add_ff_generator(HarmonicBondForceFieldGenerator(spec.bonds, spec.bond_v0, spec.bond_k, per))
     if len(spec.contacts):
         sg.add_ff_generator(GoContactForceFieldGenerator(spec.contacts, spec.go_k, spec.go_r0, per))
+    if len(spec.cgo_idx):
+        sg.add_ff_generator(CappedGoContactForceFieldGenerator(spec.cgo_idx, spec.cgo_k, spec.cgo_r0,
+                                                               spec.cgo_cap, per))
     if len(spec.gb_idx):
         sg.add_ff_generator(GaussianBondForceFieldGenerator(spec.gb_idx, spec.gb_k, spec.gb_v0,
                                                             spec.gb_sigma, per))
@@ -410,12 +427,23 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
             t.eps, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact), per))
     if spec.ljr is not None:
         t = spec.ljr
-        sg.add_ff_generator(LennardJonesRepulsiveForceFieldGenerator(
-            t.ratio, t.p0, t.p1, _ignore(topo, t.ign_bond, t.ign_contact), per))
+        ign = _ignore(topo, t.ign_bond, t.ign_contact)
+        if t.kind == "wca":
+            sg.add_ff_generator(WeeksChandlerAndersenForceFieldGenerator(t.p1, t.p0, ign, per))
+        elif t.kind == "uniform":
+            sg.add_ff_generator(UniformWeeksChandlerAndersenForceFieldGenerator(
+                spec.n, t.p0[0], t.p1[0], np.nonzero(t.side & 1)[0], np.nonzero(t.side & 2)[0], ign, per))
+        else:
+            sg.add_ff_generator(LennardJonesRepulsiveForceFieldGenerator(t.ratio, t.p0, t.p1, ign, per))
     if spec.lja is not None:
         t = spec.lja
-        sg.add_ff_generator(LennardJonesAttractiveForceFieldGenerator(
-            t.ratio, t.p0, t.p1, _ignore(topo, t.ign_bond, t.ign_contact), per))
+        ign = _ignore(topo, t.ign_bond, t.ign_contact)
+        if t.kind == "uniform":
+            sg.add_ff_generator(UniformLennardJonesAttractiveForceFieldGenerator(
+                spec.n, t.p0[0], t.p1[0], t.ratio, np.nonzero(t.side & 1)[0], np.nonzero(t.side & 2)[0],
+                ign, per))
+        else:
+            sg.add_ff_generator(LennardJonesAttractiveForceFieldGenerator(t.ratio, t.p0, t.p1, ign, per))
     if spec.dh is not None:
         t = spec.dh
         sg.add_ff_generator(DebyeHuckelForceFieldGenerator(
@@ -431,7 +459,7 @@ def build_system(spec: CGSpec) -> System:
 _PAIR_KEYS = ("exv", "dh", "ljr", "lja")
 _ARRAY_KEYS = ("pos", "masses", "bonds", "bond_v0", "bond_k", "contacts", "go_k", "go_r0", "fla_idx",
                "fla_k", "fla_aa", "fld_idx", "fld_k", "fld_aa1", "fld_aa2", "gb_idx", "gb_k", "gb_v0",
-               "gb_sigma", "gd_idx", "gd_k", "gd_theta0", "gd_sigma")
+               "gb_sigma", "gd_idx", "gd_k", "gd_theta0", "gd_sigma", "cgo_idx", "cgo_k", "cgo_r0")
 
 
 def spec_to_arrays(spec: CGSpec) -> dict:
@@ -439,6 +467,7 @@ def spec_to_arrays(spec: CGSpec) -> dict:
     out = {k: np.asarray(getattr(spec, k)) for k in _ARRAY_KEYS}
     out["scalars"] = np.array([spec.n, int(spec.periodic), spec.temperature, spec.friction, spec.dt])
     out["box"] = np.asarray(spec.box if spec.box is not None else (0.0, 0.0, 0.0), float)
+    out["cgo_cap"] = np.array([spec.cgo_cap])
     for key in _PAIR_KEYS:
         t = getattr(spec, key)
         if t is None:
@@ -461,6 +490,8 @@ def spec_from_arrays(d) -> CGSpec:
     for k in _ARRAY_KEYS[2:]:
         if k in d:
             setattr(spec, k, np.array(d[k]))
+    if "cgo_cap" in d:
+        spec.cgo_cap = float(np.asarray(d["cgo_cap"])[0])
     for key in _PAIR_KEYS:
         if f"{key}_scalars" not in d:
             continue
@@ -496,10 +527,14 @@ def subset_spec(spec: CGSpec, n_keep: int) -> CGSpec:
     m = keep(spec.gd_idx)
     s.gd_idx, s.gd_k, s.gd_theta0, s.gd_sigma = (spec.gd_idx[m], spec.gd_k[m], spec.gd_theta0[m],
                                                  spec.gd_sigma[m])
+    m = keep(spec.cgo_idx)
+    s.cgo_idx, s.cgo_k, s.cgo_r0 = spec.cgo_idx[m], spec.cgo_k[m], spec.cgo_r0[m]
     for key in _PAIR_KEYS:
         t = getattr(s, key)
         if t is not None:
             t.p0 = t.p0[:n_keep].copy()
             if t.p1 is not None:
                 t.p1 = t.p1[:n_keep].copy()
+            if t.side is not None:
+                t.side = t.side[:n_keep].copy()
     return s

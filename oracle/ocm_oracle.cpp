@@ -374,9 +374,23 @@ typedef struct OracleSystem {
     const double* gd_theta0;
     const double* gd_sigma;
     int gd_periodic;
+    // WeeksChandlerAndersen in the repulsive LJ slot: geometric epsilon mean
+    // (WeeksChandlerAndersenForceFieldGenerator.cpp:38-45)
+    int ljr_geometric;
+    // uniform generators: per-particle side bits (1 former, 2 latter); a
+    // pair interacts if one is former and the other latter; null = all
+    const int8_t* ljr_side;
+    const int8_t* lja_side;
+    // capped Go contacts (CappedGoContactForceFieldGenerator.cpp:5-31)
+    int64_t n_cgo;
+    const int64_t* cgo_idx;
+    const double* cgo_k;
+    const double* cgo_r0;
+    double cgo_cap;
+    int cgo_periodic;
 } OracleSystem;
 
-// Energy slots: EXV, DH, LJR, LJA, HB, GO, FLA, FLD.
+// Energy slots: EXV, DH, LJR, LJA, HB, GO, FLA, FLD, GB, GD, capped Go.
 
 int oracle_dh_params(double I, double T, double ratio, double* out5) {
     const DHParams p = dh_params(I, T, ratio);
@@ -438,7 +452,7 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
     const int64_t n = s->n;
     std::vector<V3> x(n), f(n, V3{0, 0, 0});
     for (int64_t i = 0; i < n; ++i) x[i] = {s->pos[3 * i], s->pos[3 * i + 1], s->pos[3 * i + 2]};
-    double E[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double E[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const double L[3] = {s->box[0], s->box[1], s->box[2]};
     auto min_image = [&](V3 d, bool per) {
         if (!per) return d;
@@ -476,6 +490,31 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
         const double sc = -dEdr / r;
         add(i, scale(d, -sc));
         add(j, scale(d, sc));
+    }
+    // -------- capped Go contacts: linear below cap r0, Go 10-12 above --------
+    if (s->n_cgo) {
+        const double c = s->cgo_cap;
+        const double slope = -60 * (std::pow(1 / c, 13.0) - std::pow(1 / c, 11.0));
+        const double intercept = 65 * std::pow(1 / c, 12.0) - 66 * std::pow(1 / c, 10.0);
+        for (int64_t b = 0; b < s->n_cgo; ++b) {
+            const int64_t i = s->cgo_idx[2 * b], j = s->cgo_idx[2 * b + 1];
+            const V3 d = min_image(sub(x[j], x[i]), s->cgo_periodic);
+            const double r = std::sqrt(dot(d, d));
+            const double r0 = s->cgo_r0[b], k = s->cgo_k[b];
+            double dEdr;
+            if (r / r0 <= c) {
+                E[10] += k * (slope * r / r0 + intercept);
+                dEdr = k * slope / r0;
+            } else {
+                const double t = r0 / r;
+                const double t10 = std::pow(t, 10), t12 = std::pow(t, 12);
+                E[10] += k * (5 * t12 - 6 * t10);
+                dEdr = k * (-60 * t12 + 60 * t10) / r;
+            }
+            const double sc = -dEdr / r;
+            add(i, scale(d, -sc));
+            add(j, scale(d, sc));
+        }
     }
     // -------- Gaussian bonds (GaussianBondForceFieldGenerator.cpp:5-7) --------
     for (int64_t b = 0; b < s->n_gb; ++b) {
@@ -689,6 +728,9 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
     float rc2f[4];
     for (int t = 0; t < 4; ++t) rc2f[t] = (float)(T[t].rc * T[t].rc);
     const bool any_pair = s->exv_on || s->dh_on || s->ljr_on || s->lja_on;
+    auto sides = [](const int8_t* side, int64_t i, int64_t j) {
+        return !side || ((side[i] & 1) && (side[j] & 2)) || ((side[i] & 2) && (side[j] & 1));
+    };
     // One unordered pair (i < j): every pair term, exclusions and the
     // FP32 cutoff emulation; both enumerations below call it.
     auto pair = [&](int64_t i, int64_t j) {
@@ -726,9 +768,10 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
                     sc += qq * ex * (1.0 / dh.debye + 1.0 / r) / r2;
                 }
                 if (s->ljr_on && !(eb & 4) && !std::isnan(s->ljr_sigma[i]) &&
-                    !std::isnan(s->ljr_sigma[j]) && inside(2)) {
+                    !std::isnan(s->ljr_sigma[j]) && sides(s->ljr_side, i, j) && inside(2)) {
                     const double sig = (s->ljr_sigma[i] + s->ljr_sigma[j]) * 0.5;
-                    const double eps = (s->ljr_eps[i] + s->ljr_eps[j]) * 0.5;
+                    const double eps = s->ljr_geometric ? std::sqrt(s->ljr_eps[i] * s->ljr_eps[j])
+                                                        : (s->ljr_eps[i] + s->ljr_eps[j]) * 0.5;
                     if (r <= sig * std::pow(2.0, 1.0 / 6.0)) {
                         const double s6 = std::pow(sig / r, 6), s12 = s6 * s6;
                         E[2] += eps * (4 * (s12 - s6) + 1);
@@ -736,7 +779,7 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
                     }
                 }
                 if (s->lja_on && !(eb & 8) && !std::isnan(s->lja_sigma[i]) &&
-                    !std::isnan(s->lja_sigma[j]) && inside(3)) {
+                    !std::isnan(s->lja_sigma[j]) && sides(s->lja_side, i, j) && inside(3)) {
                     const double sig = (s->lja_sigma[i] + s->lja_sigma[j]) * 0.5;
                     const double eps = (s->lja_eps[i] + s->lja_eps[j]) * 0.5;
                     double e, dedr;
@@ -781,7 +824,7 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
             forces[3 * i + 2] = f[i].z;
         }
     if (energies)
-        for (int k = 0; k < 10; ++k) energies[k] = E[k];
+        for (int k = 0; k < 11; ++k) energies[k] = E[k];
     return 0;
 }
 

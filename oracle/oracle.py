@@ -16,6 +16,7 @@ from . import build as _build
 _D = C.POINTER(C.c_double)
 _I64 = C.POINTER(C.c_int64)
 _I32 = C.POINTER(C.c_int32)
+_I8 = C.POINTER(C.c_int8)
 
 
 class OracleSystem(C.Structure):
@@ -39,6 +40,9 @@ class OracleSystem(C.Structure):
         ("gb_periodic", C.c_int),
         ("n_gd", C.c_int64), ("gd_idx", _I64), ("gd_k", _D), ("gd_theta0", _D), ("gd_sigma", _D),
         ("gd_periodic", C.c_int),
+        ("ljr_geometric", C.c_int), ("ljr_side", _I8), ("lja_side", _I8),
+        ("n_cgo", C.c_int64), ("cgo_idx", _I64), ("cgo_k", _D), ("cgo_r0", _D), ("cgo_cap", C.c_double),
+        ("cgo_periodic", C.c_int),
     ]
 
 
@@ -94,6 +98,13 @@ class _Keep:
         self.items.append(arr)
         return arr.ctypes.data_as(_I64)
 
+    def i8(self, a):
+        if a is None:
+            return None
+        arr = np.ascontiguousarray(a, np.int8)
+        self.items.append(arr)
+        return arr.ctypes.data_as(_I8)
+
     def i32(self, a):
         arr = np.ascontiguousarray(a, np.int32)
         self.items.append(arr)
@@ -131,12 +142,18 @@ def make_system(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
         s.dh_ign_bond, s.dh_ign_contact = t.ign_bond, t.ign_contact
     if spec.ljr is not None:
         t = spec.ljr
-        s.ljr_on, s.ljr_ratio, s.ljr_eps, s.ljr_sigma = 1, t.ratio, k.d(t.p0), k.d(t.p1)
+        kind = getattr(t, "kind", "")
+        # WCA forms (per-particle and uniform) cut off at 2^(1/6) sigma
+        ratio = 2.0 ** (1.0 / 6.0) if kind in ("wca", "uniform") else t.ratio
+        s.ljr_on, s.ljr_ratio, s.ljr_eps, s.ljr_sigma = 1, ratio, k.d(t.p0), k.d(t.p1)
         s.ljr_ign_bond, s.ljr_ign_contact = t.ign_bond, t.ign_contact
+        s.ljr_geometric = int(kind == "wca")
+        s.ljr_side = k.i8(getattr(t, "side", None))
     if spec.lja is not None:
         t = spec.lja
         s.lja_on, s.lja_ratio, s.lja_eps, s.lja_sigma = 1, t.ratio, k.d(t.p0), k.d(t.p1)
         s.lja_ign_bond, s.lja_ign_contact = t.ign_bond, t.ign_contact
+        s.lja_side = k.i8(getattr(t, "side", None))
     s.fp32_cutoff = int(fp32_cutoff)
     s.pair_cells = int(cells)
     gb = getattr(spec, "gb_idx", np.zeros((0, 2), np.int64))
@@ -150,12 +167,33 @@ def make_system(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
         s.gd_idx, s.gd_k = k.i64(gd), k.d(spec.gd_k)
         s.gd_theta0, s.gd_sigma = k.d(spec.gd_theta0), k.d(spec.gd_sigma)
     s.gd_periodic = int(spec.periodic)
+    cgo = getattr(spec, "cgo_idx", np.zeros((0, 2), np.int64))
+    s.n_cgo = len(cgo)
+    if s.n_cgo:
+        s.cgo_idx, s.cgo_k, s.cgo_r0 = k.i64(cgo), k.d(spec.cgo_k), k.d(spec.cgo_r0)
+        s.cgo_cap = float(spec.cgo_cap)
+    s.cgo_periodic = int(spec.periodic)
     return s, k
 
 
 SLOTS = ("ExcludedVolume", "DebyeHuckel", "LennardJonesRepulsive", "LennardJonesAttractive",
          "HarmonicBond", "GoContact", "FlexibleLocalAngle", "FlexibleLocalDihedral", "GaussianBond",
-         "GaussianDihedral")
+         "GaussianDihedral", "CappedGoContact")
+
+
+def slot_names(spec):
+    """Force-group name of every energy slot for this spec (the Lennard-Jones
+    slots carry the WCA and uniform variants under their own names)."""
+    names = list(SLOTS)
+    kind_r = getattr(spec.ljr, "kind", "") if spec.ljr is not None else ""
+    kind_a = getattr(spec.lja, "kind", "") if spec.lja is not None else ""
+    if kind_r == "wca":
+        names[2] = "WeeksChandlerAndersen"
+    elif kind_r == "uniform":
+        names[2] = "UniformWeeksChadlerAndersen"
+    if kind_a == "uniform":
+        names[3] = "UniformLennardJonesAttractive"
+    return tuple(names)
 
 
 def evaluate(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
@@ -167,7 +205,7 @@ def evaluate(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
     e = np.zeros(len(SLOTS))
     lib().oracle_evaluate(C.byref(s), f.ctypes.data_as(_D), e.ctypes.data_as(_D))
     del keep
-    return f, dict(zip(SLOTS, e))
+    return f, dict(zip(slot_names(spec), e))
 
 
 def dh_params(ionic_strength, temperature, ratio):

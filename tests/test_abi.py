@@ -197,3 +197,49 @@ def test_interaction_group_names():
     d = sg.generate().describe()["forces"][0]
     # others-others, A-others, A-A, B-others, B-B (A-B ignored)
     assert d["interaction_groups"] == 5
+
+
+def test_wca_uniform_and_capped_go_generators():
+    """The reference's variants: names (force groups), cutoffs, groups and
+    error messages."""
+    n = 6
+    sig = np.array([0.5, 0.7, 0.6, 0.7, 0.4, np.nan])
+    eps = np.array([1.0, 2.0, 1.0, 1.0, 0.5, np.nan])
+    sg = ocm.SystemGenerator(np.ones(n))
+    sg.add_ff_generator(ocm.WeeksChandlerAndersenForceFieldGenerator(sig, eps, [], False))
+    sg.add_ff_generator(ocm.UniformLennardJonesAttractiveForceFieldGenerator(
+        n, 0.8, 0.45, 2.5, [0, 1, 2], [3, 4, 5], [], False))
+    sg.add_ff_generator(ocm.CappedGoContactForceFieldGenerator([[0, 3], [1, 4]], [1.0, 2.0], [0.6, 0.7],
+                                                               0.8, False))
+    system = sg.generate()
+    assert system.group_names() == ["WeeksChandlerAndersen", "UniformLennardJonesAttractive",
+                                    "CappedGoContact"]
+    d = system.describe()["forces"]
+    assert d[0]["cutoff"] == pytest.approx(2 ** (1 / 6) * 0.7, rel=1e-15)
+    assert d[0]["participants"] == 5
+    assert d[1]["cutoff"] == pytest.approx(0.45 * 2.5, rel=1e-15)
+    assert d[1]["switch_distance"] == pytest.approx(0.9 * 0.45 * 2.5, rel=1e-15)
+    assert d[1]["interaction_groups"] == 1
+    # the uniform WCA keeps the reference's spelling of its name
+    sg2 = ocm.SystemGenerator(np.ones(n))
+    sg2.add_ff_generator(ocm.UniformWeeksChandlerAndersenForceFieldGenerator(n, 1.0, 0.5, [0, 1], [2, 3], [],
+                                                                             False))
+    assert sg2.generate().group_names() == ["UniformWeeksChadlerAndersen"]
+    assert sg2.generate().describe()["forces"][0]["cutoff"] == pytest.approx(2 ** (1 / 6) * 0.5, rel=1e-15)
+    with pytest.raises(ocm.OCMError) as ei:
+        ocm.CappedGoContactForceFieldGenerator([[0, 1]], [1.0, 2.0], [0.5], 0.8, False)
+    assert "CappedGoContactForceFieldGenerator : parameter number of" in str(ei.value)
+
+
+def test_repulsive_slot_holds_one_generator():
+    """LennardJonesRepulsive, WeeksChandlerAndersen and the uniform WCA share
+    the repulsive pair slot: a second one in a system is refused."""
+    n = 4
+    sig, eps = np.full(n, 0.5), np.ones(n)
+    sg = ocm.SystemGenerator(np.ones(n))
+    sg.add_ff_generator(ocm.LennardJonesRepulsiveForceFieldGenerator(2.5, eps, sig, [], False))
+    sg.add_ff_generator(ocm.WeeksChandlerAndersenForceFieldGenerator(sig, eps, [], False))
+    system = sg.generate()
+    # compiling the system (done by the footprint query, no GPU needed) refuses it
+    assert system.footprint() == -1
+    assert "share one pair slot" in ocm.lib.ocm_last_error().decode()

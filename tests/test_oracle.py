@@ -293,3 +293,84 @@ def test_gaussian_forces_are_minus_gradient():
             xm[i, c] -= h
             fd = -(_total_energy(spec, xp) - _total_energy(spec, xm)) / (2 * h)
             assert fd == pytest.approx(f[i, c], rel=2e-5, abs=2e-4 * (1 + abs(f[i, c])))
+
+
+# --------------------------------------------------------------------------
+# WCA, uniform Lennard-Jones and capped Go (the reference's variants)
+# --------------------------------------------------------------------------
+def test_wca_geometric_mean_and_cutoff():
+    """WeeksChandlerAndersenForceFieldGenerator.cpp:38-45: sigma arithmetic,
+    epsilon geometric mean; E(sigma) = eps, E(2^(1/6) sigma) = 0; cutoff
+    2^(1/6) (sigma_max + sigma_2nd) / 2."""
+    sig, eps = np.array([0.5, 0.7]), np.array([1.0, 4.0])
+    wca = synth.PairTerm(ratio=0.0, p0=eps, p1=sig, kind="wca")
+    s = 0.6
+    _, e = oracle.evaluate(two_bead(s, ljr=wca), fp32_cutoff=False)
+    assert e["WeeksChandlerAndersen"] == pytest.approx(2.0, rel=1e-13)  # sqrt(1 * 4)
+    t = 2 ** (1 / 6) * s
+    f, e = oracle.evaluate(two_bead(t * (1 - 1e-9), ljr=wca), fp32_cutoff=False)
+    assert abs(e["WeeksChandlerAndersen"]) < 1e-7 and np.abs(f).max() < 1e-5
+    _, e = oracle.evaluate(two_bead(t * (1 + 1e-9), ljr=wca), fp32_cutoff=False)
+    assert e["WeeksChandlerAndersen"] == 0.0
+
+
+def test_uniform_pairs_only_between_former_and_latter():
+    """Uniform generators act on (former, latter) pairs only."""
+    n = 3
+    pos = np.array([[0.0, 0, 0], [0.6, 0, 0], [0.0, 0.6, 0]])
+    side = np.array([1, 2, 1], np.int8)  # 0 and 2 former, 1 latter
+    lja = synth.PairTerm(ratio=3.0, p0=np.full(n, 0.5), p1=np.full(n, 0.4), kind="uniform", side=side)
+    s = synth.CGSpec(n=n, pos=pos, masses=np.ones(n), lja=lja)
+    _, e = oracle.evaluate(s, fp32_cutoff=False)
+
+    def lj(r):  # below the 0.9 * 1.2 nm switch
+        return 4 * 0.5 * ((0.4 / r) ** 12 - (0.4 / r) ** 6)
+    # (0, 1) at 0.6 nm and (2, 1) at 0.6 sqrt(2) nm; (0, 2) are both former
+    assert e["UniformLennardJonesAttractive"] == pytest.approx(lj(0.6) + lj(0.6 * np.sqrt(2)), rel=1e-12)
+
+
+def test_capped_go_matches_go_above_cap_and_is_c1():
+    """Capped Go: the Go 10-12 value beyond cap r0, a straight line below,
+    equal value and slope at r = cap r0."""
+    k, r0, cap = 1.5, 0.6, 0.8
+
+    def energy(r):
+        s = two_bead(r)
+        s.cgo_idx, s.cgo_k, s.cgo_r0, s.cgo_cap = np.array([[0, 1]]), np.array([k]), np.array([r0]), cap
+        f, e = oracle.evaluate(s, fp32_cutoff=False)
+        return e["CappedGoContact"], f
+    e_min, f_min = energy(r0)
+    assert e_min == pytest.approx(-k, rel=1e-14) and np.abs(f_min).max() < 1e-12
+    rb = cap * r0
+    lo, _ = energy(rb * (1 - 1e-9))
+    hi, _ = energy(rb * (1 + 1e-9))
+    assert lo == pytest.approx(hi, rel=1e-7)
+    h = 1e-6
+    slope_lo = (energy(rb - h)[0] - energy(rb - 2 * h)[0]) / h
+    slope_hi = (energy(rb + 2 * h)[0] - energy(rb + h)[0]) / h
+    assert slope_lo == pytest.approx(slope_hi, rel=1e-4)
+    # linear below the cap
+    e1, e2, e3 = energy(0.2)[0], energy(0.3)[0], energy(0.4)[0]
+    assert (e3 - e2) == pytest.approx(e2 - e1, rel=1e-10)
+
+
+def test_variant_forces_are_minus_gradient():
+    rng = np.random.default_rng(4)
+    n = 6
+    pos = rng.normal(scale=0.45, size=(n, 3))
+    wca = synth.PairTerm(ratio=0.0, p0=rng.uniform(0.5, 2.0, n), p1=rng.uniform(0.5, 0.8, n), kind="wca")
+    side = np.array([1, 1, 3, 2, 2, 3], np.int8)
+    lja = synth.PairTerm(ratio=3.0, p0=np.full(n, 0.7), p1=np.full(n, 0.45), kind="uniform", side=side)
+    s = synth.CGSpec(n=n, pos=pos, masses=np.ones(n), ljr=wca, lja=lja)
+    s.cgo_idx = np.array([[0, 3], [1, 4], [2, 5]])
+    s.cgo_k, s.cgo_r0, s.cgo_cap = np.array([1.0, 2.0, 0.5]), np.array([0.9, 0.6, 1.2]), 0.8
+    f, _ = oracle.evaluate(s, fp32_cutoff=False)
+    h = 1e-6
+    for i in range(n):
+        for c in range(3):
+            xp, xm = pos.copy(), pos.copy()
+            xp[i, c] += h
+            xm[i, c] -= h
+            ep = sum(oracle.evaluate(s, fp32_cutoff=False, pos=xp)[1].values())
+            em = sum(oracle.evaluate(s, fp32_cutoff=False, pos=xm)[1].values())
+            assert f[i, c] == pytest.approx(-(ep - em) / (2 * h), rel=1e-5, abs=1e-5)

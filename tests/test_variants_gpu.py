@@ -1,0 +1,88 @@
+"""The reference's force-field variants on the GPU against the FP64 oracle:
+WeeksChandlerAndersen (geometric epsilon mean, in the repulsive
+Lennard-Jones slot), the uniform attractive Lennard-Jones and uniform WCA
+between two particle lists, and capped Go contacts, on the batched and the
+plain engine (non-periodic and periodic).
+
+Tolerances as everywhere: per-bead force error <= 1e-4 relative to
+max(|F_i|, 1e-3 F_rms); per-term energies <= 1e-5 relative."""
+import numpy as np
+import pytest
+
+from conftest import rel_force_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _with_variants(spec, seed, uniform_wca=False):
+    """Add WCA (or uniform WCA), uniform LJA between two halves, and capped
+    Go contacts, some of them compressed below cap r0."""
+    from opencafemol_gb300 import synth
+    rng = np.random.default_rng(seed)
+    n = spec.n
+    side = np.zeros(n, np.int8)
+    side[: n // 2] |= 1
+    side[n // 3:] |= 2
+    if uniform_wca:
+        spec.ljr = synth.PairTerm(ratio=0.0, p0=np.full(n, 0.9), p1=np.full(n, 0.58), kind="uniform",
+                                  side=side, ign_bond=1)
+    else:
+        spec.ljr = synth.PairTerm(ratio=0.0, p0=rng.uniform(0.3, 1.5, n), p1=rng.uniform(0.35, 0.55, n),
+                                  kind="wca", ign_bond=1)
+    spec.lja = synth.PairTerm(ratio=3.0, p0=np.full(n, 0.6), p1=np.full(n, 0.5), kind="uniform", side=side,
+                              ign_bond=1)
+    pairs = rng.choice(n, size=(n // 4, 2))
+    pairs = pairs[pairs[:, 0] != pairs[:, 1]]
+    d = spec.pos[pairs[:, 1]] - spec.pos[pairs[:, 0]]
+    if spec.periodic:
+        L = np.asarray(spec.box)
+        d -= L * np.rint(d / L)
+    r = np.linalg.norm(d, axis=1)
+    keep = r < 3.0
+    spec.cgo_idx = pairs[keep]
+    spec.cgo_r0 = r[keep] * rng.uniform(0.9, 1.6, keep.sum())  # r / r0 below 0.8 for part of them
+    spec.cgo_k = rng.uniform(0.5, 2.0, keep.sum())
+    spec.cgo_cap = 0.8
+    assert np.any(r[keep] / spec.cgo_r0 < spec.cgo_cap) and np.any(r[keep] / spec.cgo_r0 > spec.cgo_cap)
+    return spec
+
+
+def _check(system, f, e32, f_ref, e_ref):
+    assert rel_force_err(f, f_ref) <= 1e-4
+    for g, name in enumerate(system.group_names()):
+        assert abs(e32[g] - e_ref[name]) <= 1e-5 * max(1.0, abs(e_ref[name])), name
+
+
+@pytest.mark.parametrize("uniform_wca", [False, True])
+def test_variants_batched_and_plain(gpu, uniform_wca):
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    spec = _with_variants(synth.go_protein(400, 77), seed=5, uniform_wca=uniform_wca)
+    system = synth.build_system(spec)
+    names = system.group_names()
+    assert "CappedGoContact" in names and "UniformLennardJonesAttractive" in names
+    assert ("UniformWeeksChadlerAndersen" if uniform_wca else "WeeksChandlerAndersen") in names
+    f_ref, e_ref = oracle.evaluate(spec)
+    b = gpu.Batch(max_systems=1, max_total_beads=512, max_beads_per_system=512)
+    slot = b.admit(system, spec.pos, seed=1, n_steps=1)
+    f, e32 = b.state(slot)
+    _check(system, f, e32, f_ref, e_ref)
+    ctx = gpu.Context(system, gpu.LangevinIntegrator(300.0, 0.1, 0.01, 1))
+    ctx.setPositions(spec.pos)
+    fp, _ = ctx.getState()
+    _check(system, fp, ctx.getGroupEnergies(), f_ref, e_ref)
+
+
+def test_variants_periodic_plain(gpu):
+    """A periodic slab of 3,000 beads (cluster layout, charged rows) with WCA
+    in place of the HPS repulsion and the uniform attraction."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    spec = _with_variants(synth.hps_slab(30, 100, (15.0, 15.0, 60.0), slab_width=20.0, seed=21), seed=6)
+    system = synth.build_system(spec)
+    ctx = gpu.Context(system, gpu.LangevinIntegrator(300.0, 0.1, 0.01, 1))
+    ctx.setPositions(spec.pos)
+    f, _ = ctx.getState()
+    assert ctx.stats()["reordered"] == 1
+    f_ref, e_ref = oracle.evaluate(spec)
+    _check(system, f, ctx.getGroupEnergies(), f_ref, e_ref)
