@@ -267,6 +267,15 @@ int ocm_context_get_group_energies(ocm_context* ctx, double* energies);
 int ocm_context_get_kinetic_energy(ocm_context* ctx, double* kinetic_energy);
 /* LangevinIntegrator::step(steps) (Simulator.cpp:60). */
 int ocm_context_step(ocm_context* ctx, int64_t steps);
+/* OpenMM::LocalEnergyMinimizer::minimize(context, tolerance, maxIterations)
+ * as the reference's Simulator calls it (Simulator.cpp:41-46): a
+ * limited-memory BFGS on the potential energy until the RMS of all force
+ * components is <= tolerance (kJ/mol/nm; the reference uses OpenMM's
+ * default 10) or max_iterations (0: no limit) iterations are done.  The
+ * context keeps the minimised positions; velocities are untouched.
+ * iterations_out may be NULL. */
+int ocm_context_minimize(ocm_context* ctx, double tolerance, int64_t max_iterations,
+                         int64_t* iterations_out);
 
 typedef struct ocm_context_stats {
     int64_t steps_done;

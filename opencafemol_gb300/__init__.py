@@ -6,7 +6,7 @@ a Langevin integrator and a local energy minimiser, behind the C ABI in
 include/ocm.h.
 """
 from ._lib import LIB_PATH, OCMError, device_count, lib
-from .engine import ALL_GROUPS, Batch, Context
+from .engine import ALL_GROUPS, Batch, Context, LocalEnergyMinimizer
 from .forcefield import (AMINO_ACIDS, CappedGoContactForceFieldGenerator, DebyeHuckelForceFieldGenerator,
                          ExcludedVolumeForceFieldGenerator,
                          FlexibleLocalAngleForceFieldGenerator,
@@ -22,7 +22,7 @@ from .forcefield import (AMINO_ACIDS, CappedGoContactForceFieldGenerator, DebyeH
                          fld_table_keys)
 
 __all__ = [
-    "LIB_PATH", "OCMError", "device_count", "lib", "ALL_GROUPS", "Batch", "Context",
+    "LIB_PATH", "OCMError", "device_count", "lib", "ALL_GROUPS", "Batch", "Context", "LocalEnergyMinimizer",
     "AMINO_ACIDS", "DebyeHuckelForceFieldGenerator", "ExcludedVolumeForceFieldGenerator",
     "FlexibleLocalAngleForceFieldGenerator", "FlexibleLocalDihedralForceFieldGenerator",
     "GaussianBondForceFieldGenerator", "GaussianDihedralForceFieldGenerator",

@@ -35,7 +35,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
              "-I", str(CUDA_HOME / "include"), "-I", str(INCLUDE)]
 
 CU_SOURCES = ["plain_engine.cu", "batch_engine.cu"]
-CXX_SOURCES = ["host_system.cpp", "tables.cpp", "capi.cpp"]
+CXX_SOURCES = ["host_system.cpp", "tables.cpp", "capi.cpp", "minimize.cpp"]
 
 
 def _headers() -> list[Path]:

@@ -455,6 +455,7 @@ int ocm_add_capped_go_contact(ocm_system* s, int64_t n, const int64_t* idx, cons
 }
 
 // ---------------- plain context ----------------
+
 int ocm_context_create(const ocm_system* s, double T, double friction, double dt, int32_t seed,
                        int device, ocm_context** out) {
     return guard([&] {
@@ -498,6 +499,10 @@ int ocm_context_get_kinetic_energy(ocm_context* ctx, double* ke) {
     CTX_CALL(need(ke, "ke"); *ke = ctx->c->kinetic_energy());
 }
 int ocm_context_step(ocm_context* ctx, int64_t steps) { CTX_CALL(ctx->c->step(steps)); }
+int ocm_context_minimize(ocm_context* ctx, double tolerance, int64_t max_iterations, int64_t* iterations_out) {
+    CTX_CALL(const int64_t it = ctx->c->minimize(tolerance, max_iterations);
+             if (iterations_out) *iterations_out = it);
+}
 int ocm_context_get_stats(ocm_context* ctx, ocm_context_stats* out) {
     CTX_CALL(need(out, "out"); const auto& c = *ctx->c; out->steps_done = c.steps_done;
              out->list_builds = c.list_builds; out->tiles = c.tiles_last;

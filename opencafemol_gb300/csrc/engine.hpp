@@ -76,6 +76,8 @@ class PlainContext {
     void set_list_options(int32_t interval, double skin);
     void list_pairs(int64_t* out, int64_t cap, int64_t* n_out);
     void cluster_order(int64_t* out, int64_t cap, int64_t* n_out);
+    // L-BFGS local energy minimisation (minimize.cpp); returns the iterations
+    int64_t minimize(double tolerance, int64_t max_iterations);
     bool charged_split() const { return charged_split_; }
     double tile_cutoff() const { return tile_cutoff_; }
     int64_t charged_pairs() const { return charged_last_; }
@@ -103,6 +105,9 @@ class PlainContext {
     void eval(uint32_t groups, bool energy, double* forces, double* slot_energy);
     uint32_t slots_for_groups(uint32_t groups) const;
     void check_positions_set() const;
+    // positions from the minimiser: no re-estimate of the cluster column width
+    void set_positions_internal(const double* xyz);
+    void set_positions_impl(const double* xyz, bool retune);
 
     cudaStream_t stream_ = nullptr;
     std::map<int, cudaGraphExec_t> graphs_;

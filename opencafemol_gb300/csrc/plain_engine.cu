@@ -1306,7 +1306,10 @@ void PlainContext::check_positions_set() const {
     if (!positions_set_) throw Error(5, "[error] positions have not been set");
 }
 
-void PlainContext::set_positions(const double* xyz) {
+void PlainContext::set_positions(const double* xyz) { set_positions_impl(xyz, true); }
+void PlainContext::set_positions_internal(const double* xyz) { set_positions_impl(xyz, false); }
+
+void PlainContext::set_positions_impl(const double* xyz, bool retune) {
     OCM_CK(cudaSetDevice(device));
     std::vector<double> a(n), b(n), c(n);
     for (int64_t i = 0; i < n; ++i) {
@@ -1316,7 +1319,7 @@ void PlainContext::set_positions(const double* xyz) {
         if (!std::isfinite(a[i]) || !std::isfinite(b[i]) || !std::isfinite(c[i]))
             throw Error(7, "[error] non-finite position for particle " + std::to_string(i));
     }
-    if (reorder) {
+    if (reorder && retune) {
         // Bead density over the occupied 1 nm cells sets the column width:
         // clusters of 32 beads then come out about as tall as wide.
         int g[3];

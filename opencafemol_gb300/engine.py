@@ -14,7 +14,7 @@ import numpy as np
 from ._lib import OCM_MAX_GROUPS, ContextStats, OCMError, as_f64, check, dptr, i64ptr, lib
 from .forcefield import LangevinIntegrator, System
 
-__all__ = ["Context", "Batch", "ALL_GROUPS"]
+__all__ = ["Context", "Batch", "ALL_GROUPS", "LocalEnergyMinimizer"]
 
 ALL_GROUPS = 0xFFFFFFFF
 
@@ -112,6 +112,20 @@ class Context:
                     cap = n.value
                     continue
                 raise
+
+
+class LocalEnergyMinimizer:
+    """OpenMM's ``LocalEnergyMinimizer.minimize(context, tolerance,
+    maxIterations)`` as the reference's Simulator calls it before a run
+    (src/Simulator.cpp:41-46): L-BFGS on the potential energy until the RMS
+    of all force components is at most ``tolerance`` kJ/mol/nm, or
+    ``maxIterations`` iterations (0: no limit).  Returns the iterations."""
+
+    @staticmethod
+    def minimize(context: Context, tolerance: float = 10.0, maxIterations: int = 0) -> int:
+        it = C.c_int64()
+        check(lib.ocm_context_minimize(context._h, float(tolerance), int(maxIterations), C.byref(it)))
+        return it.value
 
 
 class Batch:

@@ -246,17 +246,26 @@ class PDBObserver(ObserverBase):
 
 
 class Simulator:
-    """The reference's run loop (src/Simulator.cpp:50-76) on a Context:
-    every ``save_step`` steps, each observer records the state, then the
-    integrator advances ``save_step`` steps; observer output is written by a
-    background thread."""
+    """The reference's run loop (src/Simulator.cpp:37-76) on a Context:
+    ``initialize`` sets the positions and, when asked, minimises the energy
+    first; ``run`` lets each observer record the state every ``save_step``
+    steps, then advances the integrator ``save_step`` steps; observer output
+    is written by a background thread."""
 
-    def __init__(self, context, total_step: int, save_step: int, observers=()):
+    def __init__(self, context, total_step: int, save_step: int, observers=(),
+                 energy_minimization: bool = False):
         if save_step <= 0:
             raise ValueError("save_step must be positive")
         self.context = context
         self.total_step, self.save_step = int(total_step), int(save_step)
         self.observers = list(observers)
+        self.energy_minimization = bool(energy_minimization)
+
+    def initialize(self, positions) -> None:
+        self.context.setPositions(positions)
+        if self.energy_minimization:
+            from .engine import LocalEnergyMinimizer
+            LocalEnergyMinimizer.minimize(self.context)
 
     def run(self) -> None:
         writer = _Writer()

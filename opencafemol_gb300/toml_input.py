@@ -61,6 +61,7 @@ class TomlSystem:
     velocities: np.ndarray | None          # nm/ps, None when the file has none
     total_step: int = 0
     save_step: int = 0
+    energy_minimization: bool = False      # [simulator] energy_minimization (ReadTOMLInput.cpp:1008)
     seed: int = 0
     group_vec: list = field(default_factory=list)
     skipped: list = field(default_factory=list)
@@ -297,4 +298,5 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
     integ = LangevinIntegratorGenerator(temperature, friction, dt, seed)
     return TomlSystem(spec=spec, integrator=integ, velocities=vel,
                       total_step=int(sim.get("total_step", 0)), save_step=int(sim.get("save_step", 0)),
+                      energy_minimization=bool(sim.get("energy_minimization", False)),
                       seed=seed, group_vec=group_vec, skipped=skipped)
