@@ -90,11 +90,13 @@ class CGSpec:
     gd_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
     gd_theta0: np.ndarray = field(default_factory=lambda: np.zeros(0))
     gd_sigma: np.ndarray = field(default_factory=lambda: np.zeros(0))
-    # capped Go contacts (one capping ratio for all)
+    # capped Go contacts: capping ratio (one for all, or one per contact),
+    # and whether they are "contact" edges of the topology (exclusions)
     cgo_idx: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int64))
     cgo_k: np.ndarray = field(default_factory=lambda: np.zeros(0))
     cgo_r0: np.ndarray = field(default_factory=lambda: np.zeros(0))
-    cgo_cap: float = 0.8
+    cgo_cap: float | np.ndarray = 0.8
+    cgo_topology: str = "none"
     exv: PairTerm | None = None
     dh: PairTerm | None = None
     ljr: PairTerm | None = None
@@ -393,6 +395,8 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
         topo.add_edges(spec.bonds, "bond")
     if len(spec.contacts):
         topo.add_edges(spec.contacts, "contact")
+    if len(spec.cgo_idx) and spec.cgo_topology == "contact":
+        topo.add_edges(spec.cgo_idx, "contact")
     sg = SystemGenerator(spec.masses)
     if per:
         sg.set_pbc(*spec.box)
@@ -401,8 +405,11 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
     if len(spec.contacts):
         sg.add_ff_generator(GoContactForceFieldGenerator(spec.contacts, spec.go_k, spec.go_r0, per))
     if len(spec.cgo_idx):
-        sg.add_ff_generator(CappedGoContactForceFieldGenerator(spec.cgo_idx, spec.cgo_k, spec.cgo_r0,
-                                                               spec.cgo_cap, per))
+        caps = np.broadcast_to(np.asarray(spec.cgo_cap, float), (len(spec.cgo_idx),))
+        for cap in np.unique(caps):  # one generator per capping ratio
+            sel = caps == cap
+            sg.add_ff_generator(CappedGoContactForceFieldGenerator(spec.cgo_idx[sel], spec.cgo_k[sel],
+                                                                   spec.cgo_r0[sel], float(cap), per))
     if len(spec.gb_idx):
         sg.add_ff_generator(GaussianBondForceFieldGenerator(spec.gb_idx, spec.gb_k, spec.gb_v0,
                                                             spec.gb_sigma, per))
@@ -467,7 +474,7 @@ def spec_to_arrays(spec: CGSpec) -> dict:
     out = {k: np.asarray(getattr(spec, k)) for k in _ARRAY_KEYS}
     out["scalars"] = np.array([spec.n, int(spec.periodic), spec.temperature, spec.friction, spec.dt])
     out["box"] = np.asarray(spec.box if spec.box is not None else (0.0, 0.0, 0.0), float)
-    out["cgo_cap"] = np.array([spec.cgo_cap])
+    out["cgo_cap"] = np.atleast_1d(np.asarray(spec.cgo_cap, float))
     for key in _PAIR_KEYS:
         t = getattr(spec, key)
         if t is None:
@@ -491,7 +498,8 @@ def spec_from_arrays(d) -> CGSpec:
         if k in d:
             setattr(spec, k, np.array(d[k]))
     if "cgo_cap" in d:
-        spec.cgo_cap = float(np.asarray(d["cgo_cap"])[0])
+        cap = np.asarray(d["cgo_cap"], float)
+        spec.cgo_cap = float(cap[0]) if cap.size == 1 else cap
     for key in _PAIR_KEYS:
         if f"{key}_scalars" not in d:
             continue
@@ -529,6 +537,8 @@ def subset_spec(spec: CGSpec, n_keep: int) -> CGSpec:
                                                  spec.gd_sigma[m])
     m = keep(spec.cgo_idx)
     s.cgo_idx, s.cgo_k, s.cgo_r0 = spec.cgo_idx[m], spec.cgo_k[m], spec.cgo_r0[m]
+    if np.ndim(spec.cgo_cap):
+        s.cgo_cap = np.asarray(spec.cgo_cap)[m]
     for key in _PAIR_KEYS:
         t = getattr(s, key)
         if t is not None:

@@ -51,7 +51,8 @@ NM_PER_ANGSTROM = 0.1
 CAFETIME_PS = math.sqrt(1.0 / KJ_PER_KCAL) * 0.1
 
 _PAIR_DEFAULT_RATIO = {"ExcludedVolume": 2.0, "DebyeHuckel": 5.5,
-                       "LennardJonesRepulsive": 2.5, "LennardJonesAttractive": 2.5}
+                       "LennardJonesRepulsive": 2.5, "LennardJonesAttractive": 2.5,
+                       "WCA": 0.0}  # the WCA cutoff is 2^(1/6) sigma, no ratio
 
 
 @dataclass
@@ -113,6 +114,39 @@ def _per_particle(ff: dict, n: int, keys: tuple[str, ...], what: str) -> list[np
         for arr, k in zip(out, keys):
             arr[i] = float(p[k])
     return out
+
+
+def _either(p: dict, a: str, b: str):
+    return p[a] if a in p else p[b]
+
+
+def _uniform_table(glob: dict, n: int, what: str):
+    """The one (sigma nm, epsilon kJ/mol, side bits) of a uniform-form type
+    table ([forcefields.global.table.A.B]); former = particles named A,
+    latter = particles named B (ReadTOMLInput.cpp:435-512, 546-621,
+    ReadTOMLForceFieldGenerator.cpp:1307-1357).  Pairs with an empty side are
+    skipped, as in the reference; more than one remaining pair type would
+    need one pair slot each and is reported as not covered."""
+    names = {}
+    for p in glob["parameters"]:
+        i = _index(p)
+        _check_range(i, n, "read_toml_uniform_ff_generator")
+        names.setdefault(str(p["name"]), []).append(i)
+    found = []
+    for first, sub in glob["table"].items():
+        for second, par in sub.items():
+            former, latter = names.get(first, []), names.get(second, [])
+            if not former or not latter:
+                continue
+            side = np.zeros(n, np.int8)
+            side[former] |= 1
+            side[latter] |= 2
+            found.append((float(_either(par, "sigma", "σ")) * NM_PER_ANGSTROM,
+                          float(_either(par, "epsilon", "ε")) * KJ_PER_KCAL, side))
+    if len(found) != 1:
+        raise ValueError(f"{what}: a type table with {len(found)} interacting pair types "
+                         "(one is covered: each needs its own pair slot)")
+    return found[0]
 
 
 def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlSystem:
@@ -180,6 +214,8 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
     fld_idx, fld_k, fld_aa1, fld_aa2 = [], [], [], []
     gb_idx, gb_k, gb_v0, gb_sigma = [], [], [], []
     gd_idx, gd_k, gd_theta0, gd_sigma = [], [], [], []
+    cgo_idx, cgo_k, cgo_r0, cgo_cap = [], [], [], []
+    cgo_topology = None
     ff = data["forcefields"][0]
     for loc in ff.get("local", []):
         inter, pot = loc["interaction"], loc["potential"]
@@ -202,6 +238,19 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                 go_r0.append(float(p["v0"]) * NM_PER_ANGSTROM)
             if loc.get("topology") != "contact":
                 unsupported(f"{what}: only topology = \"contact\" is covered")
+        elif inter == "BondLength" and pot == "CappedGoContact":
+            cap = float(loc.get("capping_ratio", 0.75))  # ReadTOMLForceFieldGenerator.cpp:237
+            for p in loc["parameters"]:
+                ij = _indices(p)
+                _check_range(ij, n, "read_toml_capped_go_contact_ff_generator")
+                cgo_idx.append(ij)
+                cgo_k.append(float(p["k"]) * KJ_PER_KCAL)
+                cgo_r0.append(float(p["v0"]) * NM_PER_ANGSTROM)
+                cgo_cap.append(cap)
+            topo = loc.get("topology", "none")
+            if topo not in ("none", "contact") or (cgo_topology is not None and topo != cgo_topology):
+                unsupported(f"{what}: only one topology (\"none\" or \"contact\") for all blocks is covered")
+            cgo_topology = topo
         elif inter == "BondLength" and pot == "Gaussian":
             for p in loc["parameters"]:
                 ij = _indices(p)
@@ -258,6 +307,10 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
     if fld_idx:
         spec.fld_idx, spec.fld_k = np.array(fld_idx, np.int64), np.array(fld_k)
         spec.fld_aa1, spec.fld_aa2 = np.array(fld_aa1, np.int32), np.array(fld_aa2, np.int32)
+    if cgo_idx:
+        spec.cgo_idx, spec.cgo_k, spec.cgo_r0 = np.array(cgo_idx, np.int64), np.array(cgo_k), np.array(cgo_r0)
+        spec.cgo_cap = np.array(cgo_cap)
+        spec.cgo_topology = cgo_topology or "none"
 
     for glob in ff.get("global", []):
         pot = glob["potential"]
@@ -265,7 +318,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
         if pot not in _PAIR_DEFAULT_RATIO:
             unsupported(f"global force {what} is not covered")
             continue
-        if "table" in glob:
+        if "table" in glob and pot not in ("WCA", "LennardJonesAttractive"):
             unsupported(f"global force {what} with a type table (uniform form) is not covered")
             continue
         try:
@@ -274,6 +327,19 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
             unsupported(str(e))
             continue
         ratio = float(glob.get("cutoff", _PAIR_DEFAULT_RATIO[pot]))
+        if "table" in glob:  # uniform WCA / uniform attractive LJ between two named particle sets
+            try:
+                sig, eps, side = _uniform_table(glob, n, what)
+            except ValueError as e:
+                unsupported(str(e))
+                continue
+            t = PairTerm(ratio=ratio, p0=np.full(n, eps), p1=np.full(n, sig), kind="uniform", side=side,
+                         ign_bond=ign_bond, ign_contact=ign_contact)
+            if pot == "WCA":
+                spec.ljr = t
+            else:
+                spec.lja = t
+            continue
         if pot == "ExcludedVolume":
             (radius,) = _per_particle(glob, n, ("radius",), "read_toml_excluded_volume_ff_generator")
             spec.exv = PairTerm(ratio=ratio, p0=radius * NM_PER_ANGSTROM,
@@ -285,6 +351,15 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                 raise ValueError("[error] attributes table must contains ionic_strength for DebyeHuckel potential.")
             spec.dh = PairTerm(ratio=ratio, p0=q, ionic_strength=float(attr["ionic_strength"]),
                                temperature=temperature, ign_bond=ign_bond, ign_contact=ign_contact)
+        elif pot == "WCA":
+            sig, eps = np.full(n, np.nan), np.full(n, np.nan)
+            for p in glob["parameters"]:
+                i = _index(p)
+                _check_range(i, n, "read_toml_weeks_chandler_andersen_ff_generator")
+                sig[i] = float(_either(p, "sigma", "σ"))
+                eps[i] = float(_either(p, "epsilon", "ε"))
+            spec.ljr = PairTerm(ratio=0.0, p0=eps * KJ_PER_KCAL, p1=sig * NM_PER_ANGSTROM, kind="wca",
+                                ign_bond=ign_bond, ign_contact=ign_contact)
         else:
             eps, sig = _per_particle(glob, n, ("epsilon", "sigma"),
                                      "read_toml_lennard_jones_ff_generator")

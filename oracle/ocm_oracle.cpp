@@ -386,8 +386,9 @@ typedef struct OracleSystem {
     const int64_t* cgo_idx;
     const double* cgo_k;
     const double* cgo_r0;
-    double cgo_cap;
+    const double* cgo_cap;   // capping ratio per contact
     int cgo_periodic;
+    int cgo_contact_edges;   // the contacts are "contact" edges of the topology
 } OracleSystem;
 
 // Energy slots: EXV, DH, LJR, LJA, HB, GO, FLA, FLD, GB, GD, capped Go.
@@ -493,10 +494,10 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
     }
     // -------- capped Go contacts: linear below cap r0, Go 10-12 above --------
     if (s->n_cgo) {
-        const double c = s->cgo_cap;
-        const double slope = -60 * (std::pow(1 / c, 13.0) - std::pow(1 / c, 11.0));
-        const double intercept = 65 * std::pow(1 / c, 12.0) - 66 * std::pow(1 / c, 10.0);
         for (int64_t b = 0; b < s->n_cgo; ++b) {
+            const double c = s->cgo_cap[b];
+            const double slope = -60 * (std::pow(1 / c, 13.0) - std::pow(1 / c, 11.0));
+            const double intercept = 65 * std::pow(1 / c, 12.0) - 66 * std::pow(1 / c, 10.0);
             const int64_t i = s->cgo_idx[2 * b], j = s->cgo_idx[2 * b + 1];
             const V3 d = min_image(sub(x[j], x[i]), s->cgo_periodic);
             const double r = std::sqrt(dot(d, d));
@@ -647,6 +648,8 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
     std::vector<std::pair<int64_t, int64_t>> bond_edges, contact_edges;
     for (int64_t b = 0; b < s->n_bonds; ++b) bond_edges.emplace_back(s->bond_idx[2 * b], s->bond_idx[2 * b + 1]);
     for (int64_t b = 0; b < s->n_go; ++b) contact_edges.emplace_back(s->go_idx[2 * b], s->go_idx[2 * b + 1]);
+    if (s->cgo_contact_edges)
+        for (int64_t b = 0; b < s->n_cgo; ++b) contact_edges.emplace_back(s->cgo_idx[2 * b], s->cgo_idx[2 * b + 1]);
     struct Term {
         int on, kind;
         int ign_bond, ign_contact;

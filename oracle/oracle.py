@@ -41,8 +41,8 @@ class OracleSystem(C.Structure):
         ("n_gd", C.c_int64), ("gd_idx", _I64), ("gd_k", _D), ("gd_theta0", _D), ("gd_sigma", _D),
         ("gd_periodic", C.c_int),
         ("ljr_geometric", C.c_int), ("ljr_side", _I8), ("lja_side", _I8),
-        ("n_cgo", C.c_int64), ("cgo_idx", _I64), ("cgo_k", _D), ("cgo_r0", _D), ("cgo_cap", C.c_double),
-        ("cgo_periodic", C.c_int),
+        ("n_cgo", C.c_int64), ("cgo_idx", _I64), ("cgo_k", _D), ("cgo_r0", _D), ("cgo_cap", _D),
+        ("cgo_periodic", C.c_int), ("cgo_contact_edges", C.c_int),
     ]
 
 
@@ -171,8 +171,9 @@ def make_system(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
     s.n_cgo = len(cgo)
     if s.n_cgo:
         s.cgo_idx, s.cgo_k, s.cgo_r0 = k.i64(cgo), k.d(spec.cgo_k), k.d(spec.cgo_r0)
-        s.cgo_cap = float(spec.cgo_cap)
+        s.cgo_cap = k.d(np.broadcast_to(np.asarray(spec.cgo_cap, float), (len(cgo),)))
     s.cgo_periodic = int(spec.periodic)
+    s.cgo_contact_edges = int(getattr(spec, "cgo_topology", "none") == "contact")
     return s, k
 
 

@@ -193,3 +193,55 @@ def test_read_system_matches_oracle_energies():
     for k, v in e.items():
         if v != 0.0:
             assert k in names
+
+
+def test_capped_go_wca_and_uniform_tables():
+    """CappedGoContact (default capping ratio 0.75, k kcal/mol, v0 Angstrom),
+    WCA with per-particle sigma / epsilon (Angstrom, kcal/mol), and the
+    uniform table form of the attractive Lennard-Jones between two named
+    particle sets (ReadTOMLInput.cpp:212-218, 435-621)."""
+    from opencafemol_gb300 import synth
+    text = BASE + """
+[[forcefields.local]]
+interaction = "BondLength"
+potential = "CappedGoContact"
+topology = "contact"
+parameters = [{indices = [0, 3], v0 = 5.5, k = 0.7}, {indices = [1, 4], v0 = 6.0, k = 0.3}]
+[[forcefields.global]]
+interaction = "Pair"
+potential = "WCA"
+ignore.particles_within.bond = 1
+parameters = [
+  {index = 0, sigma = 4.0, epsilon = 0.2}, {index = 1, "σ" = 5.0, "ε" = 0.3},
+  {index = 2, sigma = 4.5, epsilon = 0.25}, {index = 3, sigma = 4.0, epsilon = 0.2},
+  {index = 4, sigma = 6.0, epsilon = 0.1},
+]
+[[forcefields.global]]
+interaction = "Pair"
+potential = "LennardJonesAttractive"
+cutoff = 3.0
+ignore.particles_within.bond = 1
+table.A.B = {sigma = 5.0, epsilon = 0.4}
+table.A.C = {sigma = 5.0, epsilon = 0.4}
+parameters = [
+  {index = 0, name = "A"}, {index = 1, name = "A"}, {index = 2, name = "B"},
+  {index = 3, name = "B"}, {index = 4, name = "A"},
+]
+"""
+    t = _read(text)
+    s = t.spec
+    assert s.cgo_topology == "contact"
+    assert np.allclose(s.cgo_cap, 0.75) and np.allclose(s.cgo_r0, [0.55, 0.6])
+    assert np.allclose(s.cgo_k, [0.7 * 4.184, 0.3 * 4.184])
+    assert s.ljr.kind == "wca" and np.allclose(s.ljr.p1, [0.4, 0.5, 0.45, 0.4, 0.6])
+    assert np.allclose(s.ljr.p0, np.array([0.2, 0.3, 0.25, 0.2, 0.1]) * 4.184)
+    # A-C has no C particle and is skipped; A-B remains
+    assert s.lja.kind == "uniform" and s.lja.ratio == 3.0
+    assert s.lja.side.tolist() == [1, 1, 2, 2, 1]
+    assert np.allclose(s.lja.p1, 0.5) and np.allclose(s.lja.p0, 0.4 * 4.184)
+    names = synth.build_system(s).group_names()
+    assert {"CappedGoContact", "WeeksChandlerAndersen", "UniformLennardJonesAttractive"} <= set(names)
+    # two interacting pair types would need two pair slots
+    two = text.replace('table.A.C = {sigma = 5.0, epsilon = 0.4}', 'table.B.B = {sigma = 5.0, epsilon = 0.4}')
+    with pytest.raises(ValueError, match="2 interacting pair types"):
+        _read(two)

@@ -86,3 +86,74 @@ def test_variants_periodic_plain(gpu):
     assert ctx.stats()["reordered"] == 1
     f_ref, e_ref = oracle.evaluate(spec)
     _check(system, f, ctx.getGroupEnergies(), f_ref, e_ref)
+
+
+def test_toml_variants_match_oracle(gpu):
+    """The variants as the TOML reader builds them (capped Go contacts as
+    "contact" edges of the topology, WCA, a uniform table pair) on a
+    60-bead chain."""
+    from opencafemol_gb300 import synth
+    from opencafemol_gb300.toml_input import read_toml
+    from oracle import oracle
+    base = synth.go_protein(60, 40)
+    rng = np.random.default_rng(40)
+    parts = ",\n".join(f'  {{m = 120.0, pos = [{x[0] * 10:.4f}, {x[1] * 10:.4f}, {x[2] * 10:.4f}]}}'
+                       for x in base.pos)
+    bonds = ",\n".join(f"  {{indices = [{i}, {i + 1}], v0 = 3.8, k = 110.0}}" for i in range(59))
+    cgo = ",\n".join(f"  {{indices = [{i}, {i + 5}], v0 = {rng.uniform(5, 9):.3f}, k = 0.6}}"
+                     for i in range(0, 50, 3))
+    wca = ",\n".join(f'  {{index = {i}, sigma = {rng.uniform(3.5, 5.5):.3f}, epsilon = 0.3}}' for i in range(60))
+    names = ",\n".join(f'  {{index = {i}, name = "{"A" if i % 2 else "B"}"}}' for i in range(60))
+    text = f"""
+[simulator]
+boundary_type = "Unlimited"
+delta_t = 0.2
+total_step = 10
+save_step = 10
+[[systems]]
+attributes.temperature = 300.0
+particles = [
+{parts}
+]
+[[forcefields]]
+[[forcefields.local]]
+interaction = "BondLength"
+potential = "Harmonic"
+topology = "bond"
+parameters = [
+{bonds}
+]
+[[forcefields.local]]
+interaction = "BondLength"
+potential = "CappedGoContact"
+topology = "contact"
+capping_ratio = 0.85
+parameters = [
+{cgo}
+]
+[[forcefields.global]]
+interaction = "Pair"
+potential = "WCA"
+ignore.particles_within.bond = 1
+ignore.particles_within.contact = 1
+parameters = [
+{wca}
+]
+[[forcefields.global]]
+interaction = "Pair"
+potential = "LennardJonesAttractive"
+cutoff = 3.0
+ignore.particles_within.bond = 2
+table.A.B = {{sigma = 5.0, epsilon = 0.4}}
+parameters = [
+{names}
+]
+"""
+    spec = read_toml(text.encode()).spec
+    system = synth.build_system(spec)
+    f_ref, e_ref = oracle.evaluate(spec)
+    ctx = gpu.Context(system, gpu.LangevinIntegrator(300.0, 0.1, 0.01, 1))
+    ctx.setPositions(spec.pos)
+    f, _ = ctx.getState()
+    _check(system, f, ctx.getGroupEnergies(), f_ref, e_ref)
+    assert abs(e_ref["CappedGoContact"]) > 0 and abs(e_ref["UniformLennardJonesAttractive"]) > 0
