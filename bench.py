@@ -459,7 +459,7 @@ def run_reference(args, rank, world):
         return None
     specs = ensemble_specs()
     steps_cpu = []
-    K = max(1, args.cpu_steps)
+    K = max(1, args.ref_md_steps)  # a bounded sample per reference step
     for _ in range(args.warmup):
         run_cpu_baseline(specs, sample_systems=8, md_steps=2)
     for _ in range(args.steps):
@@ -493,7 +493,8 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=24)
     ap.add_argument("--plain-chunks", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=48)
-    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--cpu-steps", type=int, default=600)  # ~5 s of the 16-core host
+    ap.add_argument("--ref-md-steps", type=int, default=20)  # MD steps per reference-arm step
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--serve-requests", type=int, default=96)
     ap.add_argument("--traffic-bytes", type=float, default=K_BATCH_DRAM_BYTES,
