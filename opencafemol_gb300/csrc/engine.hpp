@@ -143,6 +143,7 @@ class PlainContext {
     DevBuf<float4> anc_, ext_;  // cluster anchors, largest anchored offset per axis
     DevBuf<int32_t> tile_count_, tile_start_, tile_j_, tile_mask_;
     DevBuf<float4> tile_shift_;  // per tile: anchor shift, w != 0 when the minimum image is needed
+    DevBuf<int32_t> tile_i_;     // per tile: its row cluster
     DevBuf<int32_t> raw_start_, raw_i_, raw_j_;  // candidate tiles before pruning
     DevBuf<uint8_t> keep_;
     DevBuf<uint32_t> masks_;

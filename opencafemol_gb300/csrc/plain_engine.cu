@@ -30,7 +30,7 @@ namespace {
 
 constexpr int kForceThreads = 128;
 constexpr int kWarpsPerForceBlock = kForceThreads / 32;
-constexpr int kTilesPerChunk = 4;
+constexpr int kTilesPerChunk = 1;  // measured on the 20k-bead slab: 1 -> 65, 2 -> 71, 4 -> 76 us per step
 constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ float4 shfl4(float4 v, int src) {
@@ -418,8 +418,8 @@ __global__ void k_prune(int nc, const float4* __restrict__ xs, const float4* __r
 __global__ void k_compact_tiles(int nc, const int32_t* __restrict__ raw_start, const int32_t* __restrict__ raw_j,
                                 const uint8_t* __restrict__ keep_flag, int cap, const int32_t* __restrict__ start,
                                 const float4* __restrict__ anc, const float4* __restrict__ ext, BoxD bd,
-                                float3 box, float pad, int32_t* __restrict__ tile_j, int32_t* __restrict__ tile_mask,
-                                float4* __restrict__ tile_shift) {
+                                float3 box, float pad, int32_t* __restrict__ tile_i, int32_t* __restrict__ tile_j,
+                                int32_t* __restrict__ tile_mask, float4* __restrict__ tile_shift) {
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (I >= nc || raw_start[nc] > cap) return;
@@ -433,6 +433,7 @@ __global__ void k_compact_tiles(int nc, const int32_t* __restrict__ raw_start, c
         if (keep) {
             const int k = at + __popc(b & ((1u << lane) - 1u));
             const int J = raw_j[q];
+            tile_i[k] = I;
             tile_j[k] = J;
             tile_mask[k] = -1;
             const float3 A = anchor_shift(ai, anc[J], bd);
@@ -644,7 +645,7 @@ struct ForceArgs {
     int n;
     const float4 *xs, *p0s, *p1s;
     const uint32_t* labs;
-    const int32_t *perm, *tile_start, *tile_j, *tile_mask;
+    const int32_t *perm, *tile_start, *tile_i, *tile_j, *tile_mask;
     const uint32_t* masks;
     const double *x, *y, *z;
     int n_bonds, n_angles, n_dih;
@@ -703,14 +704,7 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
         double eacc[4] = {0.0, 0.0, 0.0, 0.0};
         for (int c0 = gw * kTilesPerChunk; c0 < total; c0 += stride) {
             const int c1 = min(total, c0 + kTilesPerChunk);
-            // row of tile c0: the last I with tile_start[I] <= c0
-            int lo = 0, hi = a.nc - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (a.tile_start[mid] <= c0) lo = mid;
-                else hi = mid - 1;
-            }
-            int I = lo;
+            int I = a.tile_i[c0];  // row of the chunk's first tile
             int row_end = a.tile_start[I + 1];
             int ki = I * 32 + lane;
             float4 xi = a.xs[ki];
@@ -1219,7 +1213,7 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
     bb_c_.alloc(nc); bb_h_.alloc(nc); anc_.alloc(nc); ext_.alloc(nc);
     tile_count_.alloc(nc); tile_start_.alloc(nc + 1); raw_start_.alloc(nc + 1);
     tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, std::max<int64_t>(4096, nc * 48));
-    tile_j_.alloc(tile_cap_); tile_mask_.alloc(tile_cap_); raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_);
+    tile_j_.alloc(tile_cap_); tile_mask_.alloc(tile_cap_); raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_); tile_i_.alloc(tile_cap_);
     mask_cap_ = std::max<int64_t>(256, std::min<int64_t>(tile_cap_, nc * 8));
     masks_.alloc(mask_cap_ * 128);
     mask_count_.alloc(1);
@@ -1480,8 +1474,8 @@ void PlainContext::rebuild(cudaStream_t s) {
     }
     k_scan<<<1, 1024, 0, s>>>(nc_i, tile_count_.p, tile_start_.p);
     k_compact_tiles<<<wblocks, 128, 0, s>>>(nc_i, raw_start_.p, raw_j_.p, keep_.p, (int)tile_cap_,
-                                            tile_start_.p, anc_.p, ext_.p, bd, box_, wrap_pad(), tile_j_.p,
-                                            tile_mask_.p, tile_shift_.p);
+                                            tile_start_.p, anc_.p, ext_.p, bd, box_, wrap_pad(), tile_i_.p,
+                                            tile_j_.p, tile_mask_.p, tile_shift_.p);
     const int nnz = (int)cs.ex_j.size();
     OCM_CK(cudaMemsetAsync(mask_count_.p, 0, sizeof(int32_t), s));
     if (nnz > 0) {
@@ -1522,7 +1516,7 @@ void PlainContext::launch_forces(cudaStream_t s, bool energy, uint32_t slots_ena
     a.blocks_angles = div_up(a.n_angles, kForceThreads);
     a.blocks_dih = div_up(a.n_dih, kForceThreads);
     a.xs = xs_.p; a.p0s = p0s_.p; a.p1s = p1s_.p; a.labs = labs_.p; a.perm = perm_.p;
-    a.tile_start = tile_start_.p; a.tile_j = tile_j_.p; a.tile_mask = tile_mask_.p;
+    a.tile_start = tile_start_.p; a.tile_i = tile_i_.p; a.tile_j = tile_j_.p; a.tile_mask = tile_mask_.p;
     a.masks = masks_.p;
     a.x = x_.p; a.y = y_.p; a.z = z_.p;
     a.bonds = bonds_.p; a.angles = angles_.p; a.fla = fla_.p; a.dih = dihedrals_.p; a.fld = fld_.p;
@@ -1621,7 +1615,7 @@ void PlainContext::ensure_capacity() {
                 tile_cap_ = want;
                 tile_j_.alloc(tile_cap_);
                 tile_mask_.alloc(tile_cap_);
-                raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_);
+                raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_); tile_i_.alloc(tile_cap_);
                 realloced = true;
                 clear_graphs();
             }
@@ -1795,7 +1789,7 @@ void PlainContext::step(int64_t nsteps) {
             tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, tile_cap_ * 2);
             tile_j_.alloc(tile_cap_);
             tile_mask_.alloc(tile_cap_);
-            raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_);
+            raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_); tile_i_.alloc(tile_cap_);
             mask_cap_ = std::min<int64_t>(tile_cap_, mask_cap_ * 2);
             masks_.alloc(mask_cap_ * 128);
         }
