@@ -1,12 +1,16 @@
 // plain_engine.cu - the plain single-system path.
 //
-// Per step: one fused force kernel (cluster-pair tiles for every pair term,
-// plus bond, Go-contact, FLA and FLD segments in the same grid) and one
-// Langevin kernel that also zeroes the fixed-point force buffer.  Every
-// `rebuild_interval` steps the cluster layout and tile list are rebuilt:
-//   cell keys -> counting sort by Morton rank (periodic systems) ->
-//   gather into cluster order -> cluster bounding boxes -> tile count /
-//   scan / fill -> exclusion masks.
+// Per step: one fused force kernel (cluster-pair tiles for the pair terms,
+// segments for bonds / Go / Gaussian / capped-Go contacts, angles,
+// dihedrals and, when Debye-Hueckel reaches further than the other pair
+// terms, its per-bead charged rows, all in one grid) and one Langevin kernel
+// that also zeroes the fixed-point force buffer.  Every `rebuild_interval`
+// steps the cluster layout and the lists are rebuilt:
+//   cell keys (x-y columns, z slices; periodic systems) -> counting sort
+//   with in-cell ranks -> gather into cluster order with anchored offsets
+//   -> bounding boxes and anchors -> candidate tiles (count / scan / fill)
+//   -> exact pruning -> compaction with per-tile anchor shifts ->
+//   exclusion masks; charged-bead cells -> charged rows.
 // A chunk of steps (rebuild + steps) is captured once into a CUDA graph.
 #include <cuda_runtime.h>
 
@@ -378,7 +382,7 @@ __global__ void k_tiles(int nc, const float4* __restrict__ bc, const float4* __r
 // beads broadcast one at a time; a tile is kept if any pair is within range
 // (the diagonal tile always).  kept_count[I] counts the kept tiles of row I.
 template <bool PERIODIC>
-__global__ void k_prune(int nc, const float4* __restrict__ xs, const float4* __restrict__ anc, BoxD bd,
+__global__ void k_prune(int nc, const float4* __restrict__ xs, const float4* __restrict__ anc,
                         const int32_t* __restrict__ raw_start,
                         const int32_t* __restrict__ raw_i, const int32_t* __restrict__ raw_j, int cap,
                         float3 box, float3 inv_box, float cut2, uint8_t* __restrict__ keep_flag,
@@ -1463,13 +1467,13 @@ void PlainContext::rebuild(cudaStream_t s) {
     if (per) {
         k_tiles<true, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2, nullptr,
                                                     raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_, flags_.p);
-        k_prune<true><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, anc_.p, bd, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
+        k_prune<true><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, anc_.p, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
                                               box_, inv_box_, cut2, keep_.p, tile_count_.p);
     } else {
         k_tiles<false, true><<<wblocks, 128, 0, s>>>(nc_i, bb_c_.p, bb_h_.p, box_, inv_box_, cut, cut2,
                                                      nullptr, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
                                                      flags_.p);
-        k_prune<false><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, anc_.p, bd, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
+        k_prune<false><<<pblocks, 128, 0, s>>>(nc_i, xs_.p, anc_.p, raw_start_.p, raw_i_.p, raw_j_.p, (int)tile_cap_,
                                                box_, inv_box_, cut2, keep_.p, tile_count_.p);
     }
     k_scan<<<1, 1024, 0, s>>>(nc_i, tile_count_.p, tile_start_.p);

@@ -54,7 +54,7 @@ def test_go_protein_forces_energies(gpu, n, seed):
                                                     (30, 100, (15.0, 15.0, 60.0), 5)])
 def test_hps_slab_forces_energies(gpu, chains, length, box, seed):
     """Periodic HPS + DH system; the second case has > 2048 beads and runs
-    the Morton-ordered cluster layout."""
+    the column-sorted cluster layout and the charged rows."""
     from opencafemol_gb300 import synth
     from oracle import oracle
     spec = synth.hps_slab(chains, length, box, slab_width=box[2] / 3, seed=seed)
