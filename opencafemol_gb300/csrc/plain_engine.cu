@@ -108,29 +108,45 @@ __device__ __forceinline__ double warp_sum(double v) {
 // Rebuild kernels
 // ---------------------------------------------------------------------------
 
-// Exclusive scan of m ints into out[0..m] by one block of 1024 threads.
+// Exclusive scan of m ints into out[0..m] (out[m] = total) by one block of
+// 1024 threads: each of the 32 warps owns a contiguous segment and reads it
+// 32 consecutive values at a time (coalesced) - once for the segment total,
+// once more to write the prefixes with a shuffle scan.
 __device__ __forceinline__ void block_scan(int m, const int32_t* __restrict__ in, int32_t* __restrict__ out) {
-    __shared__ int32_t part[1024];
-    const int t = threadIdx.x;
-    const int per = (m + 1023) / 1024;
-    const int b = t * per, e = min(m, b + per);
+    __shared__ int32_t wsum[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int per = (m + 31) / 32;
+    const int b = w * per, e = min(m, b + per);
     int32_t s = 0;
-    for (int i = b; i < e; ++i) s += in[i];
-    part[t] = s;
+    for (int i = b + lane; i < e; i += 32) s += in[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
+    if (lane == 0) wsum[w] = s;
     __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const int32_t v = t >= o ? part[t - o] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
+    if (w == 0) {  // inclusive scan of the 32 segment totals
+        int32_t v = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t u = __shfl_up_sync(kFull, v, o);
+            if (lane >= o) v += u;
+        }
+        wsum[lane] = v;
     }
-    int32_t run = part[t] - s;
-    for (int i = b; i < e; ++i) {
-        const int32_t v = in[i];
-        out[i] = run;
-        run += v;
+    __syncthreads();
+    int32_t run = w > 0 ? wsum[w - 1] : 0;
+    for (int i0 = b; i0 < e; i0 += 32) {  // warp-uniform bounds
+        const int i = i0 + lane;
+        const int32_t v = i < e ? in[i] : 0;
+        int32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t u = __shfl_up_sync(kFull, x, o);
+            if (lane >= o) x += u;
+        }
+        if (i < e) out[i] = run + x - v;
+        run += __shfl_sync(kFull, x, 31);
     }
-    if (t == 1023) out[m] = part[1023];
+    if (threadIdx.x == 0) out[m] = wsum[31];
 }
 
 __global__ void __launch_bounds__(1024) k_scan(int m, const int32_t* __restrict__ in,
