@@ -243,3 +243,52 @@ def test_repulsive_slot_holds_one_generator():
     # compiling the system (done by the footprint query, no GPU needed) refuses it
     assert system.footprint() == -1
     assert "share one pair slot" in ocm.lib.ocm_last_error().decode()
+
+
+def _uniform_groups_ref(former, latter, ignore_pairs, group_vec):
+    """Python restatement of the uniform generators' group splitting
+    (UniformLennardJonesAttractiveForceFieldGenerator.cpp:28-138), empty
+    sides dropped."""
+    if not ignore_pairs:
+        return [(set(former), set(latter))]
+    related = {g for p in ignore_pairs for g in p}
+
+    def split(side):
+        named = {g: set() for g in sorted(related)}
+        others = set()
+        for i in side:
+            g = group_vec[i]
+            (named[g] if g in related else others).add(i)
+        return named, others
+    fn, fo = split(former)
+    ln, lo = split(latter)
+    out = []
+
+    def push(a, b):
+        if a and b:
+            out.append((a, b))
+    if fo:
+        for g in ln:
+            push(fo, ln[g])
+        push(fo, lo)
+    for fg, fs in fn.items():
+        push(fs, lo)
+        for lg, ls in ln.items():
+            if (fg, lg) not in ignore_pairs:
+                push(fs, ls)
+    return out
+
+
+def test_uniform_group_splitting_matches_restatement():
+    n = 8
+    former, latter = [0, 1, 2, 3], [4, 5, 6, 7]
+    group_vec = [0, 1, 0, -1, 1, -1, 0, 1]
+    ignore = [(0, 1)]
+    sg = ocm.SystemGenerator(np.ones(n))
+    sg.add_ff_generator(ocm.UniformLennardJonesAttractiveForceFieldGenerator(
+        n, 0.5, 0.4, 2.5, former, latter, [], False, ignore_group_pairs=ignore, group_vec=group_vec))
+    d = sg.generate().describe()["forces"][0]
+    ref = _uniform_groups_ref(former, latter, ignore, group_vec)
+    assert d["interaction_groups"] == len(ref) == 8
+    # the ignored (0, 1) combination: no group pairs former-group-0 with latter-group-1
+    assert ({0, 2}, {4, 7}) not in ref
