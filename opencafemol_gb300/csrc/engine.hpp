@@ -102,6 +102,7 @@ class PlainContext {
     void setup_columns(double width);
     BoxD box_d() const;
     float wrap_pad() const;
+    void alloc_tile_arrays();
     void eval(uint32_t groups, bool energy, double* forces, double* slot_energy);
     uint32_t slots_for_groups(uint32_t groups) const;
     void check_positions_set() const;

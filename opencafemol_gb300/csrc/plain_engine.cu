@@ -1233,7 +1233,7 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
     bb_c_.alloc(nc); bb_h_.alloc(nc); anc_.alloc(nc); ext_.alloc(nc);
     tile_count_.alloc(nc); tile_start_.alloc(nc + 1); raw_start_.alloc(nc + 1);
     tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, std::max<int64_t>(4096, nc * 48));
-    tile_j_.alloc(tile_cap_); tile_mask_.alloc(tile_cap_); raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_); tile_i_.alloc(tile_cap_);
+    alloc_tile_arrays();
     mask_cap_ = std::max<int64_t>(256, std::min<int64_t>(tile_cap_, nc * 8));
     masks_.alloc(mask_cap_ * 128);
     mask_count_.alloc(1);
@@ -1633,9 +1633,7 @@ void PlainContext::ensure_capacity() {
             const int64_t want = std::min<int64_t>(nc * (nc + 1) / 2, (int64_t)total * 2 + 1024);
             if (want > tile_cap_) {
                 tile_cap_ = want;
-                tile_j_.alloc(tile_cap_);
-                tile_mask_.alloc(tile_cap_);
-                raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_); tile_i_.alloc(tile_cap_);
+                alloc_tile_arrays();
                 realloced = true;
                 clear_graphs();
             }
@@ -1807,9 +1805,7 @@ void PlainContext::step(int64_t nsteps) {
         }
         if (flags & (ListFlags::kTileOverflow | ListFlags::kMaskOverflow)) {
             tile_cap_ = std::min<int64_t>(nc * (nc + 1) / 2, tile_cap_ * 2);
-            tile_j_.alloc(tile_cap_);
-            tile_mask_.alloc(tile_cap_);
-            raw_j_.alloc(tile_cap_); raw_i_.alloc(tile_cap_); keep_.alloc(tile_cap_); tile_shift_.alloc(tile_cap_); tile_i_.alloc(tile_cap_);
+            alloc_tile_arrays();
             mask_cap_ = std::min<int64_t>(tile_cap_, mask_cap_ * 2);
             masks_.alloc(mask_cap_ * 128);
         }
@@ -1825,6 +1821,17 @@ void PlainContext::set_list_options(int32_t interval, double sk) {
     if (sk > 0) skin = sk;
     setup_charged_cells();  // cells must stay at least cutoff + skin wide
     clear_graphs();
+}
+
+// Every per-tile array, at tile_cap_ entries (candidate and final lists).
+void PlainContext::alloc_tile_arrays() {
+    tile_i_.alloc(tile_cap_);
+    tile_j_.alloc(tile_cap_);
+    tile_mask_.alloc(tile_cap_);
+    tile_shift_.alloc(tile_cap_);
+    raw_i_.alloc(tile_cap_);
+    raw_j_.alloc(tile_cap_);
+    keep_.alloc(tile_cap_);
 }
 
 float PlainContext::wrap_pad() const {
