@@ -6,7 +6,7 @@ gamma = 0.1 /ps, FP32 pair arithmetic with 64-bit fixed-point forces.  One
 bench "step" is one persistent launch that advances every replica by
 `--md-steps` MD steps.  Inputs are seeded synthetic systems (no dataset).
 
-Printed JSON keys follow the driver contract: value (device-timed,
+Printed JSON keys: value (device-timed,
 state resident in HBM), e2e (through the public API with host buffers and
 H2D/D2H copies inside the timed region), roofline of the dominant kernel,
 cpu_baseline (the FP64 CPU oracle on a bounded sample), clocks sampled
