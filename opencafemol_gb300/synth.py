@@ -58,6 +58,9 @@ class PairTerm:
     # former (bit 1) and latter (bit 2) particle lists)
     kind: str = ""
     side: np.ndarray | None = None
+    # group-based ignores: (name, name) pairs of the particles' group names
+    # (CGSpec.group_names) whose pairs do not interact
+    ignore_groups: list | None = None
 
 
 @dataclass
@@ -97,6 +100,7 @@ class CGSpec:
     cgo_r0: np.ndarray = field(default_factory=lambda: np.zeros(0))
     cgo_cap: float | np.ndarray = 0.8
     cgo_topology: str = "none"
+    group_names: list | None = None  # per-particle group name (None: no group)
     exv: PairTerm | None = None
     dh: PairTerm | None = None
     ljr: PairTerm | None = None
@@ -428,33 +432,39 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
             sel = np.array([fld_selects(key, x, y) for x, y in zip(a1, a2)], bool)
             sg.add_ff_generator(FlexibleLocalDihedralForceFieldGenerator(
                 spec.fld_idx[sel], spec.fld_k[sel], fld_fourier_table(key), key, per))
+    def grp(t):  # group-based ignores of a pair term
+        return dict(ignore_group_pairs=list(t.ignore_groups or ()),
+                    group_vec=list(spec.group_names) if t.ignore_groups else ())
+
     if spec.exv is not None:
         t = spec.exv
         sg.add_ff_generator(ExcludedVolumeForceFieldGenerator(
-            t.eps, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact), per))
+            t.eps, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact), per, **grp(t)))
     if spec.ljr is not None:
         t = spec.ljr
         ign = _ignore(topo, t.ign_bond, t.ign_contact)
         if t.kind == "wca":
-            sg.add_ff_generator(WeeksChandlerAndersenForceFieldGenerator(t.p1, t.p0, ign, per))
+            sg.add_ff_generator(WeeksChandlerAndersenForceFieldGenerator(t.p1, t.p0, ign, per, **grp(t)))
         elif t.kind == "uniform":
             sg.add_ff_generator(UniformWeeksChandlerAndersenForceFieldGenerator(
-                spec.n, t.p0[0], t.p1[0], np.nonzero(t.side & 1)[0], np.nonzero(t.side & 2)[0], ign, per))
+                spec.n, t.p0[0], t.p1[0], np.nonzero(t.side & 1)[0], np.nonzero(t.side & 2)[0], ign, per,
+                **grp(t)))
         else:
-            sg.add_ff_generator(LennardJonesRepulsiveForceFieldGenerator(t.ratio, t.p0, t.p1, ign, per))
+            sg.add_ff_generator(LennardJonesRepulsiveForceFieldGenerator(t.ratio, t.p0, t.p1, ign, per, **grp(t)))
     if spec.lja is not None:
         t = spec.lja
         ign = _ignore(topo, t.ign_bond, t.ign_contact)
         if t.kind == "uniform":
             sg.add_ff_generator(UniformLennardJonesAttractiveForceFieldGenerator(
                 spec.n, t.p0[0], t.p1[0], t.ratio, np.nonzero(t.side & 1)[0], np.nonzero(t.side & 2)[0],
-                ign, per))
+                ign, per, **grp(t)))
         else:
-            sg.add_ff_generator(LennardJonesAttractiveForceFieldGenerator(t.ratio, t.p0, t.p1, ign, per))
+            sg.add_ff_generator(LennardJonesAttractiveForceFieldGenerator(t.ratio, t.p0, t.p1, ign, per, **grp(t)))
     if spec.dh is not None:
         t = spec.dh
         sg.add_ff_generator(DebyeHuckelForceFieldGenerator(
-            t.ionic_strength, t.temperature, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact), per))
+            t.ionic_strength, t.temperature, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact), per,
+            **grp(t)))
     return sg
 
 

@@ -90,10 +90,17 @@ def _check_range(idx, n: int, what: str) -> None:
             raise ValueError(f"[error] {what} : index {int(v)} exceeds the system's largest index {n - 1}.")
 
 
+def _ignore_groups(ff: dict) -> list[tuple[str, str]]:
+    """ignore.group.inter = [[A, B], ...] and ignore.group.intra = [A, ...]
+    (ReadTOMLForceFieldGenerator.cpp:1016-1050) as (name, name) pairs."""
+    grp = ff.get("ignore", {}).get("group", {})
+    pairs = [(str(a), str(b)) for a, b in grp.get("inter", [])]
+    pairs += [(str(a), str(a)) for a in grp.get("intra", [])]
+    return pairs
+
+
 def _ignore_within(ff: dict, what: str) -> tuple[int, int]:
     ign = ff.get("ignore", {})
-    if "group" in ign:
-        raise ValueError(f"{what}: group-based ignore lists are not supported")
     mol = ign.get("molecule", "Nothing")
     if mol in ("Intra", "Self"):
         raise ValueError(f"{what}: molecule-based ignore lists are not supported")
@@ -327,6 +334,9 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
             unsupported(str(e))
             continue
         ratio = float(glob.get("cutoff", _PAIR_DEFAULT_RATIO[pot]))
+        ign_groups = _ignore_groups(glob) or None
+        if ign_groups:
+            spec.group_names = list(group_vec)
         if "table" in glob:  # uniform WCA / uniform attractive LJ between two named particle sets
             try:
                 sig, eps, side = _uniform_table(glob, n, what)
@@ -334,7 +344,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                 unsupported(str(e))
                 continue
             t = PairTerm(ratio=ratio, p0=np.full(n, eps), p1=np.full(n, sig), kind="uniform", side=side,
-                         ign_bond=ign_bond, ign_contact=ign_contact)
+                         ign_bond=ign_bond, ign_contact=ign_contact, ignore_groups=ign_groups)
             if pot == "WCA":
                 spec.ljr = t
             else:
@@ -344,13 +354,14 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
             (radius,) = _per_particle(glob, n, ("radius",), "read_toml_excluded_volume_ff_generator")
             spec.exv = PairTerm(ratio=ratio, p0=radius * NM_PER_ANGSTROM,
                                 eps=float(glob["epsilon"]) * KJ_PER_KCAL, ign_bond=ign_bond,
-                                ign_contact=ign_contact)
+                                ign_contact=ign_contact, ignore_groups=ign_groups)
         elif pot == "DebyeHuckel":
             (q,) = _per_particle(glob, n, ("charge",), "read_toml_debye_huckel_ff_generator")
             if "ionic_strength" not in attr:
                 raise ValueError("[error] attributes table must contains ionic_strength for DebyeHuckel potential.")
             spec.dh = PairTerm(ratio=ratio, p0=q, ionic_strength=float(attr["ionic_strength"]),
-                               temperature=temperature, ign_bond=ign_bond, ign_contact=ign_contact)
+                               temperature=temperature, ign_bond=ign_bond, ign_contact=ign_contact,
+                               ignore_groups=ign_groups)
         elif pot == "WCA":
             sig, eps = np.full(n, np.nan), np.full(n, np.nan)
             for p in glob["parameters"]:
@@ -359,12 +370,12 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                 sig[i] = float(_either(p, "sigma", "σ"))
                 eps[i] = float(_either(p, "epsilon", "ε"))
             spec.ljr = PairTerm(ratio=0.0, p0=eps * KJ_PER_KCAL, p1=sig * NM_PER_ANGSTROM, kind="wca",
-                                ign_bond=ign_bond, ign_contact=ign_contact)
+                                ign_bond=ign_bond, ign_contact=ign_contact, ignore_groups=ign_groups)
         else:
             eps, sig = _per_particle(glob, n, ("epsilon", "sigma"),
                                      "read_toml_lennard_jones_ff_generator")
             t = PairTerm(ratio=ratio, p0=eps * KJ_PER_KCAL, p1=sig * NM_PER_ANGSTROM, ign_bond=ign_bond,
-                         ign_contact=ign_contact)
+                         ign_contact=ign_contact, ignore_groups=ign_groups)
             if pot == "LennardJonesRepulsive":
                 spec.ljr = t
             else:

@@ -43,6 +43,7 @@ class OracleSystem(C.Structure):
         ("ljr_geometric", C.c_int), ("ljr_side", _I8), ("lja_side", _I8),
         ("n_cgo", C.c_int64), ("cgo_idx", _I64), ("cgo_k", _D), ("cgo_r0", _D), ("cgo_cap", _D),
         ("cgo_periodic", C.c_int), ("cgo_contact_edges", C.c_int),
+        ("grp", _I32), ("n_igp", C.c_int64 * 4), ("igp", _I32 * 4),
     ]
 
 
@@ -174,6 +175,17 @@ def make_system(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
         s.cgo_cap = k.d(np.broadcast_to(np.asarray(spec.cgo_cap, float), (len(cgo),)))
     s.cgo_periodic = int(spec.periodic)
     s.cgo_contact_edges = int(getattr(spec, "cgo_topology", "none") == "contact")
+    names = getattr(spec, "group_names", None)
+    terms = (spec.exv, spec.dh, spec.ljr, spec.lja)
+    if names is not None and any(t is not None and getattr(t, "ignore_groups", None) for t in terms):
+        ids = {nm: q for q, nm in enumerate(sorted({g for g in names if g is not None}))}
+        s.grp = k.i32([ids[g] if g is not None else -1 for g in names])
+        for q, t in enumerate(terms):
+            pairs = list(getattr(t, "ignore_groups", None) or []) if t is not None else []
+            pairs = [(a, b) for a, b in pairs if a in ids and b in ids]  # a name nobody has ignores nothing
+            s.n_igp[q] = len(pairs)
+            if pairs:
+                s.igp[q] = k.i32([ids[v] for p in pairs for v in p])
     return s, k
 
 

@@ -374,3 +374,27 @@ def test_variant_forces_are_minus_gradient():
             ep = sum(oracle.evaluate(s, fp32_cutoff=False, pos=xp)[1].values())
             em = sum(oracle.evaluate(s, fp32_cutoff=False, pos=xm)[1].values())
             assert f[i, c] == pytest.approx(-(ep - em) / (2 * h), rel=1e-5, abs=1e-5)
+
+
+def test_group_based_ignores():
+    """ignore.group: pairs whose (group, group) is ignored do not interact
+    (either order); particles without a group, or in a group no ignore names,
+    interact with everyone."""
+    pos = np.array([[0.0, 0, 0], [0.5, 0, 0], [0.0, 0.5, 0], [0.5, 0.5, 0]])
+    rad = np.full(4, 0.3)
+    names = ["A", "B", None, "A"]
+
+    def energy(ignore):
+        exv = synth.PairTerm(ratio=2.0, p0=rad, eps=1.0, ignore_groups=ignore)
+        s = synth.CGSpec(n=4, pos=pos, masses=np.ones(4), exv=exv, group_names=names)
+        return oracle.evaluate(s, fp32_cutoff=False)[1]["ExcludedVolume"]
+
+    def pair(i, j):
+        r = np.linalg.norm(pos[i] - pos[j])
+        return 0.6 ** 12 * (r ** -12 - 1.2 ** -12)
+    every = sum(pair(i, j) for i in range(4) for j in range(i + 1, 4))
+    assert energy(None) == pytest.approx(every, rel=1e-12)
+    # A-B ignored: (0, 1) and (3, 1) drop out
+    assert energy([("B", "A")]) == pytest.approx(every - pair(0, 1) - pair(1, 3), rel=1e-12)
+    # intra A: (0, 3) drops out
+    assert energy([("A", "A")]) == pytest.approx(every - pair(0, 3), rel=1e-12)

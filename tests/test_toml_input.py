@@ -245,3 +245,40 @@ parameters = [
     two = text.replace('table.A.C = {sigma = 5.0, epsilon = 0.4}', 'table.B.B = {sigma = 5.0, epsilon = 0.4}')
     with pytest.raises(ValueError, match="2 interacting pair types"):
         _read(two)
+
+
+def test_group_based_ignores():
+    """ignore.group.inter / intra (ReadTOMLForceFieldGenerator.cpp:1016-1050)
+    reach the generators and the oracle alike."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    text = BASE.replace('vel = [0.0, 0.0, 1.0], group = "A"}', 'vel = [0.0, 0.0, 1.0], group = "B"}') + """
+[[forcefields.global]]
+interaction = "Pair"
+potential = "ExcludedVolume"
+epsilon = 0.6
+ignore.particles_within.bond = 1
+ignore.group.inter = [["A", "B"]]
+ignore.group.intra = ["B"]
+parameters = [
+  {index = 0, radius = 2.0}, {index = 1, radius = 2.0}, {index = 2, radius = 2.0},
+  {index = 3, radius = 2.0}, {index = 4, radius = 2.0},
+]
+"""
+    t = _read(text)
+    s = t.spec
+    assert s.exv.ignore_groups == [("A", "B"), ("B", "B")]
+    assert s.group_names == ["A", "A", "B", "A", "A"]
+    d = synth.build_system(s).describe()["forces"]
+    exv = next(f for f in d if f["name"] == "ExcludedVolume")
+    # (others, others), (A, others), (A, A), (B, others); A-B and B-B ignored
+    # (the sides without particles add no pair, as in the reference)
+    assert exv["interaction_groups"] == 4
+    _, e = oracle.evaluate(s, fp32_cutoff=False)
+    # only A-A pairs beyond one bond remain: (0, 3), (0, 4), (1, 3), (1, 4)
+    x = s.pos
+    rc = 2.0 * 0.4
+    want = 0.6 * 4.184 * sum(0.4 ** 12 * (np.linalg.norm(x[i] - x[j]) ** -12 - rc ** -12)
+                             for i, j in [(0, 3), (0, 4), (1, 3), (1, 4)]
+                             if np.linalg.norm(x[i] - x[j]) < rc)
+    assert e["ExcludedVolume"] == pytest.approx(want, rel=1e-12, abs=1e-12)

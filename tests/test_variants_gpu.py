@@ -157,3 +157,24 @@ parameters = [
     f, _ = ctx.getState()
     _check(system, f, ctx.getGroupEnergies(), f_ref, e_ref)
     assert abs(e_ref["CappedGoContact"]) > 0 and abs(e_ref["UniformLennardJonesAttractive"]) > 0
+
+
+def test_group_based_ignores_both_engines(gpu):
+    """Group-based ignores (ignore.group.inter / intra of the reference's
+    inputs): excluded volume skips A-B pairs, Debye-Hueckel skips A-A pairs."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    spec = synth.go_protein(240, 91)
+    spec.group_names = ["A" if i < 120 else ("B" if i < 200 else None) for i in range(spec.n)]
+    spec.exv.ignore_groups = [("A", "B")]
+    spec.dh.ignore_groups = [("A", "A")]
+    system = synth.build_system(spec)
+    f_ref, e_ref = oracle.evaluate(spec)
+    b = gpu.Batch(max_systems=1, max_total_beads=256, max_beads_per_system=256)
+    slot = b.admit(system, spec.pos, seed=1, n_steps=1)
+    f, e32 = b.state(slot)
+    _check(system, f, e32, f_ref, e_ref)
+    ctx = gpu.Context(system, gpu.LangevinIntegrator(300.0, 0.1, 0.01, 1))
+    ctx.setPositions(spec.pos)
+    fp, _ = ctx.getState()
+    _check(system, fp, ctx.getGroupEnergies(), f_ref, e_ref)
