@@ -52,6 +52,7 @@ class PairTerm:
     temperature: float = 300.0
     ign_bond: int = -1                 # exclusions within this many bonds (-1: none)
     ign_contact: int = -1              # exclusions within this many contacts
+    ign_molecule: bool = False         # exclude every pair inside one molecule (bond-connected)
     # Lennard-Jones slot variants: "" (the HPS generators), "wca"
     # (WeeksChandlerAndersen, repulsive slot), "uniform" (the uniform
     # generators: p0 / p1 hold one epsilon / sigma, `side` marks the
@@ -377,8 +378,11 @@ def fld_selects(key: str, a1: str, a2: str) -> bool:
     return a2 not in ("GLY", "PRO") and a1 == first
 
 
-def _ignore(topo: Topology, bond: int, contact: int) -> np.ndarray:
+def _ignore(topo: Topology, bond: int, contact: int, molecule: bool = False) -> np.ndarray:
     parts = []
+    if molecule:  # ignore.molecule = "Intra" / "Self": molecules from the bond edges
+        topo.make_molecule("bond")
+        parts.append(topo.ignore_list_within_molecule())
     if bond >= 0:
         parts.append(topo.ignore_list_within_edge(bond, "bond"))
     if contact >= 0:
@@ -439,10 +443,10 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
     if spec.exv is not None:
         t = spec.exv
         sg.add_ff_generator(ExcludedVolumeForceFieldGenerator(
-            t.eps, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact), per, **grp(t)))
+            t.eps, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact, t.ign_molecule), per, **grp(t)))
     if spec.ljr is not None:
         t = spec.ljr
-        ign = _ignore(topo, t.ign_bond, t.ign_contact)
+        ign = _ignore(topo, t.ign_bond, t.ign_contact, t.ign_molecule)
         if t.kind == "wca":
             sg.add_ff_generator(WeeksChandlerAndersenForceFieldGenerator(t.p1, t.p0, ign, per, **grp(t)))
         elif t.kind == "uniform":
@@ -453,7 +457,7 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
             sg.add_ff_generator(LennardJonesRepulsiveForceFieldGenerator(t.ratio, t.p0, t.p1, ign, per, **grp(t)))
     if spec.lja is not None:
         t = spec.lja
-        ign = _ignore(topo, t.ign_bond, t.ign_contact)
+        ign = _ignore(topo, t.ign_bond, t.ign_contact, t.ign_molecule)
         if t.kind == "uniform":
             sg.add_ff_generator(UniformLennardJonesAttractiveForceFieldGenerator(
                 spec.n, t.p0[0], t.p1[0], t.ratio, np.nonzero(t.side & 1)[0], np.nonzero(t.side & 2)[0],
@@ -463,7 +467,7 @@ def build_generator(spec: CGSpec) -> SystemGenerator:
     if spec.dh is not None:
         t = spec.dh
         sg.add_ff_generator(DebyeHuckelForceFieldGenerator(
-            t.ionic_strength, t.temperature, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact), per,
+            t.ionic_strength, t.temperature, t.ratio, t.p0, _ignore(topo, t.ign_bond, t.ign_contact, t.ign_molecule), per,
             **grp(t)))
     return sg
 

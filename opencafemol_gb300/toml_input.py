@@ -99,11 +99,15 @@ def _ignore_groups(ff: dict) -> list[tuple[str, str]]:
     return pairs
 
 
+def _ignore_molecule(ff: dict) -> bool:
+    """ignore.molecule = "Intra" / "Self": no pair inside one bond-connected
+    molecule (ReadTOMLForceFieldGenerator.cpp:963-985)."""
+    return ff.get("ignore", {}).get("molecule", "Nothing") in ("Intra", "Self")
+
+
 def _ignore_within(ff: dict, what: str) -> tuple[int, int]:
     ign = ff.get("ignore", {})
     mol = ign.get("molecule", "Nothing")
-    if mol in ("Intra", "Self"):
-        raise ValueError(f"{what}: molecule-based ignore lists are not supported")
     if mol in ("Others", "Inter"):
         raise ValueError('[error] ignore molecule do not support "Others" or "Inter".')
     within = ign.get("particles_within", {})
@@ -335,6 +339,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
             continue
         ratio = float(glob.get("cutoff", _PAIR_DEFAULT_RATIO[pot]))
         ign_groups = _ignore_groups(glob) or None
+        ign_mol = _ignore_molecule(glob)
         if ign_groups:
             spec.group_names = list(group_vec)
         if "table" in glob:  # uniform WCA / uniform attractive LJ between two named particle sets
@@ -344,7 +349,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                 unsupported(str(e))
                 continue
             t = PairTerm(ratio=ratio, p0=np.full(n, eps), p1=np.full(n, sig), kind="uniform", side=side,
-                         ign_bond=ign_bond, ign_contact=ign_contact, ignore_groups=ign_groups)
+                         ign_bond=ign_bond, ign_contact=ign_contact, ignore_groups=ign_groups, ign_molecule=ign_mol)
             if pot == "WCA":
                 spec.ljr = t
             else:
@@ -354,14 +359,14 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
             (radius,) = _per_particle(glob, n, ("radius",), "read_toml_excluded_volume_ff_generator")
             spec.exv = PairTerm(ratio=ratio, p0=radius * NM_PER_ANGSTROM,
                                 eps=float(glob["epsilon"]) * KJ_PER_KCAL, ign_bond=ign_bond,
-                                ign_contact=ign_contact, ignore_groups=ign_groups)
+                                ign_contact=ign_contact, ignore_groups=ign_groups, ign_molecule=ign_mol)
         elif pot == "DebyeHuckel":
             (q,) = _per_particle(glob, n, ("charge",), "read_toml_debye_huckel_ff_generator")
             if "ionic_strength" not in attr:
                 raise ValueError("[error] attributes table must contains ionic_strength for DebyeHuckel potential.")
             spec.dh = PairTerm(ratio=ratio, p0=q, ionic_strength=float(attr["ionic_strength"]),
                                temperature=temperature, ign_bond=ign_bond, ign_contact=ign_contact,
-                               ignore_groups=ign_groups)
+                               ignore_groups=ign_groups, ign_molecule=ign_mol)
         elif pot == "WCA":
             sig, eps = np.full(n, np.nan), np.full(n, np.nan)
             for p in glob["parameters"]:
@@ -370,12 +375,12 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                 sig[i] = float(_either(p, "sigma", "σ"))
                 eps[i] = float(_either(p, "epsilon", "ε"))
             spec.ljr = PairTerm(ratio=0.0, p0=eps * KJ_PER_KCAL, p1=sig * NM_PER_ANGSTROM, kind="wca",
-                                ign_bond=ign_bond, ign_contact=ign_contact, ignore_groups=ign_groups)
+                                ign_bond=ign_bond, ign_contact=ign_contact, ignore_groups=ign_groups, ign_molecule=ign_mol)
         else:
             eps, sig = _per_particle(glob, n, ("epsilon", "sigma"),
                                      "read_toml_lennard_jones_ff_generator")
             t = PairTerm(ratio=ratio, p0=eps * KJ_PER_KCAL, p1=sig * NM_PER_ANGSTROM, ign_bond=ign_bond,
-                         ign_contact=ign_contact, ignore_groups=ign_groups)
+                         ign_contact=ign_contact, ignore_groups=ign_groups, ign_molecule=ign_mol)
             if pot == "LennardJonesRepulsive":
                 spec.ljr = t
             else:

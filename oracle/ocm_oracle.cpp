@@ -34,6 +34,7 @@
 #include <cstring>
 #include <limits>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "oracle_tables.h"
@@ -395,6 +396,9 @@ typedef struct OracleSystem {
     const int32_t* grp;
     int64_t n_igp[4];
     const int32_t* igp[4];
+    // molecule-based ignores per pair term: no pair inside one molecule (the
+    // connected components of the bond edges, Topology.cpp:7-73)
+    int ign_molecule[4];
 } OracleSystem;
 
 // Energy slots: EXV, DH, LJR, LJA, HB, GO, FLA, FLD, GB, GD, capped Go.
@@ -740,6 +744,19 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
     auto sides = [](const int8_t* side, int64_t i, int64_t j) {
         return !side || ((side[i] & 1) && (side[j] & 2)) || ((side[i] & 2) && (side[j] & 1));
     };
+    // molecule of every bead (union-find over the bond edges), if any term asks
+    std::vector<int64_t> mol;
+    if (s->ign_molecule[0] || s->ign_molecule[1] || s->ign_molecule[2] || s->ign_molecule[3]) {
+        mol.resize(n);
+        for (int64_t i = 0; i < n; ++i) mol[i] = i;
+        std::function<int64_t(int64_t)> root = [&](int64_t a) { return mol[a] == a ? a : (mol[a] = root(mol[a])); };
+        for (auto& e : bond_edges) {
+            const int64_t a = root(e.first), b = root(e.second);
+            if (a != b) mol[std::max(a, b)] = std::min(a, b);
+        }
+        for (int64_t i = 0; i < n; ++i) mol[i] = root(i);
+    }
+    auto other_molecule = [&](int t, int64_t i, int64_t j) { return !s->ign_molecule[t] || mol[i] != mol[j]; };
     // true unless term t ignores the pair's (group, group) combination
     auto groups_ok = [&](int t, int64_t i, int64_t j) {
         if (!s->grp || s->n_igp[t] == 0) return true;
@@ -773,21 +790,21 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
                 };
                 const uint8_t eb = excl_bits(i, j);
                 double sc = 0;  // F_i = sc (x_i - x_j)
-                if (s->exv_on && !(eb & 1) && groups_ok(0, i, j) && !std::isnan(s->exv_radius[i]) &&
+                if (s->exv_on && !(eb & 1) && groups_ok(0, i, j) && other_molecule(0, i, j) && !std::isnan(s->exv_radius[i]) &&
                     !std::isnan(s->exv_radius[j]) && inside(0)) {
                     const double S = s->exv_radius[i] + s->exv_radius[j];
                     const double S12 = std::pow(S, 12);
                     E[0] += s->exv_eps * S12 * (std::pow(1.0 / r, 12) - exv_corr);
                     sc += 12.0 * s->exv_eps * S12 / std::pow(r, 14);
                 }
-                if (s->dh_on && !(eb & 2) && groups_ok(1, i, j) && !std::isnan(s->dh_q[i]) && !std::isnan(s->dh_q[j]) &&
+                if (s->dh_on && !(eb & 2) && groups_ok(1, i, j) && other_molecule(1, i, j) && !std::isnan(s->dh_q[i]) && !std::isnan(s->dh_q[j]) &&
                     inside(1)) {
                     const double qq = s->dh_q[i] * s->dh_q[j] * dh.k_e;
                     const double ex = std::exp(-r / dh.debye);
                     E[1] += qq * (ex / r - dh.corr);
                     sc += qq * ex * (1.0 / dh.debye + 1.0 / r) / r2;
                 }
-                if (s->ljr_on && !(eb & 4) && groups_ok(2, i, j) && !std::isnan(s->ljr_sigma[i]) &&
+                if (s->ljr_on && !(eb & 4) && groups_ok(2, i, j) && other_molecule(2, i, j) && !std::isnan(s->ljr_sigma[i]) &&
                     !std::isnan(s->ljr_sigma[j]) && sides(s->ljr_side, i, j) && inside(2)) {
                     const double sig = (s->ljr_sigma[i] + s->ljr_sigma[j]) * 0.5;
                     const double eps = s->ljr_geometric ? std::sqrt(s->ljr_eps[i] * s->ljr_eps[j])
@@ -798,7 +815,7 @@ int oracle_evaluate(const OracleSystem* s, double* forces, double* energies) {
                         sc += 24 * eps * (2 * s12 - s6) / r2;
                     }
                 }
-                if (s->lja_on && !(eb & 8) && groups_ok(3, i, j) && !std::isnan(s->lja_sigma[i]) &&
+                if (s->lja_on && !(eb & 8) && groups_ok(3, i, j) && other_molecule(3, i, j) && !std::isnan(s->lja_sigma[i]) &&
                     !std::isnan(s->lja_sigma[j]) && sides(s->lja_side, i, j) && inside(3)) {
                     const double sig = (s->lja_sigma[i] + s->lja_sigma[j]) * 0.5;
                     const double eps = (s->lja_eps[i] + s->lja_eps[j]) * 0.5;

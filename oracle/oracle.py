@@ -43,7 +43,7 @@ class OracleSystem(C.Structure):
         ("ljr_geometric", C.c_int), ("ljr_side", _I8), ("lja_side", _I8),
         ("n_cgo", C.c_int64), ("cgo_idx", _I64), ("cgo_k", _D), ("cgo_r0", _D), ("cgo_cap", _D),
         ("cgo_periodic", C.c_int), ("cgo_contact_edges", C.c_int),
-        ("grp", _I32), ("n_igp", C.c_int64 * 4), ("igp", _I32 * 4),
+        ("grp", _I32), ("n_igp", C.c_int64 * 4), ("igp", _I32 * 4), ("ign_molecule", C.c_int * 4),
     ]
 
 
@@ -177,6 +177,8 @@ def make_system(spec, fp32_cutoff: bool = True, pos=None, cells: int = -1):
     s.cgo_contact_edges = int(getattr(spec, "cgo_topology", "none") == "contact")
     names = getattr(spec, "group_names", None)
     terms = (spec.exv, spec.dh, spec.ljr, spec.lja)
+    for q, t in enumerate(terms):
+        s.ign_molecule[q] = int(t is not None and getattr(t, "ign_molecule", False))
     if names is not None and any(t is not None and getattr(t, "ignore_groups", None) for t in terms):
         ids = {nm: q for q, nm in enumerate(sorted({g for g in names if g is not None}))}
         s.grp = k.i32([ids[g] if g is not None else -1 for g in names])

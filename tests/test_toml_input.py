@@ -282,3 +282,43 @@ parameters = [
                              for i, j in [(0, 3), (0, 4), (1, 3), (1, 4)]
                              if np.linalg.norm(x[i] - x[j]) < rc)
     assert e["ExcludedVolume"] == pytest.approx(want, rel=1e-12, abs=1e-12)
+
+
+def test_molecule_based_ignores():
+    """ignore.molecule = "Intra": no pair inside a bond-connected molecule;
+    pairs between molecules interact (ReadTOMLForceFieldGenerator.cpp:963-985,
+    molecules from the bond edges, ReadTOMLInput.cpp:405)."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    # two chains: 0-1-2 and 3-4 (drop the 2-3 bond of BASE)
+    text = BASE.replace("  {indices = [2, 3], v0 = 3.8, k = 110.0},\n", "") + """
+[[forcefields.global]]
+interaction = "Pair"
+potential = "ExcludedVolume"
+epsilon = 0.6
+ignore.molecule = "Intra"
+parameters = [
+  {index = 0, radius = 2.5}, {index = 1, radius = 2.5}, {index = 2, radius = 2.5},
+  {index = 3, radius = 2.5}, {index = 4, radius = 2.5},
+]
+"""
+    s = _read(text).spec
+    assert s.exv.ign_molecule
+    names = [f["name"] for f in synth.build_system(s).describe()["forces"]]
+    assert "ExcludedVolume" in names
+    _, e = oracle.evaluate(s, fp32_cutoff=False)
+    x = s.pos
+    rc = 2.0 * 0.5
+    want = 0.6 * 4.184 * sum(0.5 ** 12 * (np.linalg.norm(x[i] - x[j]) ** -12 - rc ** -12)
+                             for i in (0, 1, 2) for j in (3, 4) if np.linalg.norm(x[i] - x[j]) < rc)
+    assert want != 0.0
+    assert e["ExcludedVolume"] == pytest.approx(want, rel=1e-12)
+
+
+def test_molecule_ignore_list_from_topology():
+    """The host builds the molecule ignore list from the bond edges."""
+    from opencafemol_gb300 import synth
+    topo = synth.Topology(5)
+    topo.add_edges(np.array([[0, 1], [1, 2], [3, 4]]), "bond")
+    pairs = synth._ignore(topo, -1, -1, True)
+    assert sorted(map(tuple, pairs.tolist())) == [(0, 1), (0, 2), (1, 2), (3, 4)]

@@ -178,3 +178,18 @@ def test_group_based_ignores_both_engines(gpu):
     ctx.setPositions(spec.pos)
     fp, _ = ctx.getState()
     _check(system, fp, ctx.getGroupEnergies(), f_ref, e_ref)
+
+
+def test_molecule_based_ignores_both_engines(gpu):
+    """ignore.molecule = "Intra": Debye-Hueckel acts only between chains."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    spec = synth.hps_slab(4, 50, (12.0, 12.0, 30.0), slab_width=10.0, seed=17)
+    spec.dh.ign_molecule = True
+    spec.dh.ign_bond = -1
+    system = synth.build_system(spec)
+    f_ref, e_ref = oracle.evaluate(spec)
+    ctx = gpu.Context(system, gpu.LangevinIntegrator(300.0, 0.1, 0.01, 1))
+    ctx.setPositions(spec.pos)
+    fp, _ = ctx.getState()
+    _check(system, fp, ctx.getGroupEnergies(), f_ref, e_ref)
