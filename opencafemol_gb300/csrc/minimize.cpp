@@ -9,7 +9,9 @@
 // evaluation; the search stops once the root-mean-square of all force
 // components is at most the tolerance.  A backtracking line search
 // (sufficient decrease, c1 = 1e-4) whose first trial moves no bead further
-// than 0.1 nm keeps the steps safe from overlapping configurations.
+// than 0.1 nm keeps the steps safe from overlapping configurations.  The
+// search also ends when no step lowers the energy any more (the FP32 force
+// noise floor), so a tolerance below that floor cannot loop forever.
 #include <algorithm>
 #include <cmath>
 #include <deque>
@@ -51,7 +53,7 @@ int64_t PlainContext::minimize(double tolerance, int64_t max_iterations) {
     const std::size_t memory = 10;
     std::vector<double> p(m3), xn(m3), gn(m3), q(m3);
     int64_t it = 0;
-    int failures = 0;
+    int failures = 0, stalled = 0;
     while (std::isfinite(e) && rms(g) > tolerance && (max_iterations == 0 || it < max_iterations)) {
         // two-loop recursion: p = -H g
         q = g;
@@ -119,9 +121,14 @@ int64_t PlainContext::minimize(double tolerance, int64_t max_iterations) {
                 R.pop_front();
             }
         }
+        // FP32 forces put a floor under the reachable RMS force: stop once
+        // 20 accepted steps in a row change the energy by less than 1e-12
+        // relative, whatever the tolerance asked for
+        stalled = std::fabs(en - e) <= 1e-12 * std::max(1.0, std::fabs(e)) ? stalled + 1 : 0;
         x.swap(xn);
         g.swap(gn);
         e = en;
+        if (stalled >= 20) break;
     }
     set_positions_internal(x.data());
     return it;
