@@ -75,6 +75,36 @@ def _aa_index(name: str) -> int:
         raise ValueError(f"unknown residue name {name!r}") from None
 
 
+class _Params(dict):
+    """One parameter table with the block's `env` table: a value written as
+    a string names an entry of `env` (Utility.hpp find_parameter, :33-139).
+    The table-name keys (y, d2y, coef, name) are plain strings."""
+
+    _NAMES = ("y", "d2y", "coef", "name")
+
+    def __init__(self, p: dict, env: dict | None):
+        super().__init__(p)
+        self.env = env or {}
+
+    def __getitem__(self, key):
+        v = super().__getitem__(key)
+        if isinstance(v, str) and key not in self._NAMES:
+            if not self.env:
+                raise ValueError(f'named variable "{v}" used but no env is defined')
+            if v not in self.env:
+                raise ValueError(f'named variable "{v}" used but not defined in env')
+            v = self.env[v]
+        return v
+
+    def get(self, key, default=None):
+        return self[key] if key in self else default
+
+
+def _params(block: dict):
+    env = block.get("env")
+    return [_Params(p, env) for p in block["parameters"]]
+
+
 def _index(p: dict) -> int:
     return int(p["index"]) + int(p.get("offset", 0))
 
@@ -119,7 +149,7 @@ def _ignore_within(ff: dict, what: str) -> tuple[int, int]:
 
 def _per_particle(ff: dict, n: int, keys: tuple[str, ...], what: str) -> list[np.ndarray]:
     out = [np.full(n, np.nan) for _ in keys]
-    for p in ff["parameters"]:
+    for p in _params(ff):
         i = _index(p)
         _check_range(i, n, what)
         for arr, k in zip(out, keys):
@@ -139,7 +169,7 @@ def _uniform_table(glob: dict, n: int, what: str):
     skipped, as in the reference; more than one remaining pair type would
     need one pair slot each and is reported as not covered."""
     names = {}
-    for p in glob["parameters"]:
+    for p in _params(glob):
         i = _index(p)
         _check_range(i, n, "read_toml_uniform_ff_generator")
         names.setdefault(str(p["name"]), []).append(i)
@@ -232,7 +262,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
         inter, pot = loc["interaction"], loc["potential"]
         what = f"{inter}/{pot}"
         if inter == "BondLength" and pot == "Harmonic":
-            for p in loc["parameters"]:
+            for p in _params(loc):
                 ij = _indices(p)
                 _check_range(ij, n, "read_toml_harmonic_bond_ff_generator")
                 bonds.append(ij)
@@ -241,7 +271,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
             if loc.get("topology") != "bond":
                 unsupported(f"{what}: only topology = \"bond\" is covered")
         elif inter == "BondLength" and pot == "GoContact":
-            for p in loc["parameters"]:
+            for p in _params(loc):
                 ij = _indices(p)
                 _check_range(ij, n, "read_toml_go_contact_ff_generator")
                 contacts.append(ij)
@@ -251,7 +281,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                 unsupported(f"{what}: only topology = \"contact\" is covered")
         elif inter == "BondLength" and pot == "CappedGoContact":
             cap = float(loc.get("capping_ratio", 0.75))  # ReadTOMLForceFieldGenerator.cpp:237
-            for p in loc["parameters"]:
+            for p in _params(loc):
                 ij = _indices(p)
                 _check_range(ij, n, "read_toml_capped_go_contact_ff_generator")
                 cgo_idx.append(ij)
@@ -263,7 +293,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                 unsupported(f"{what}: only one topology (\"none\" or \"contact\") for all blocks is covered")
             cgo_topology = topo
         elif inter == "BondLength" and pot == "Gaussian":
-            for p in loc["parameters"]:
+            for p in _params(loc):
                 ij = _indices(p)
                 _check_range(ij, n, "read_toml_gaussian_bond_ff_generator")
                 gb_idx.append(ij)
@@ -273,7 +303,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
             if loc.get("topology", "none") != "none":
                 unsupported(f"{what}: only topology = \"none\" is covered")
         elif inter == "DihedralAngle" and pot == "Gaussian":
-            for p in loc["parameters"]:
+            for p in _params(loc):
                 ijkl = _indices(p)
                 _check_range(ijkl, n, "read_toml_gaussian_dihedral_ff_generator")
                 gd_idx.append(ijkl)
@@ -283,14 +313,14 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
             if loc.get("topology", "none") != "none":
                 unsupported(f"{what}: only topology = \"none\" is covered")
         elif inter == "BondAngle" and pot == "FlexibleLocalAngle":
-            for p in loc["parameters"]:
+            for p in _params(loc):
                 ijk = _indices(p)
                 _check_range(ijk, n, "read_toml_flexible_local_angle_ff_generator")
                 fla_idx.append(ijk)
                 fla_k.append(float(p["k"]) * KJ_PER_KCAL)
                 fla_aa.append(_aa_index(str(p["y"])[3:6]))
         elif inter == "DihedralAngle" and pot == "FlexibleLocalDihedral":
-            for p in loc["parameters"]:
+            for p in _params(loc):
                 ijkl = _indices(p)
                 _check_range(ijkl, n, "read_toml_flexible_local_dihedral_ff_generator")
                 coef = str(p["coef"])
@@ -369,7 +399,7 @@ def read_toml(source, strict: bool = True, fp32_positions: bool = True) -> TomlS
                                ignore_groups=ign_groups, ign_molecule=ign_mol)
         elif pot == "WCA":
             sig, eps = np.full(n, np.nan), np.full(n, np.nan)
-            for p in glob["parameters"]:
+            for p in _params(glob):
                 i = _index(p)
                 _check_range(i, n, "read_toml_weeks_chandler_andersen_ff_generator")
                 sig[i] = float(_either(p, "sigma", "σ"))

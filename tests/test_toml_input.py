@@ -322,3 +322,26 @@ def test_molecule_ignore_list_from_topology():
     topo.add_edges(np.array([[0, 1], [1, 2], [3, 4]]), "bond")
     pairs = synth._ignore(topo, -1, -1, True)
     assert sorted(map(tuple, pairs.tolist())) == [(0, 1), (0, 2), (1, 2), (3, 4)]
+
+
+def test_env_named_parameters():
+    """A parameter written as a string names an entry of the block's env
+    table (Utility.hpp:33-139); table names (y, coef) stay strings."""
+    text = BASE + """
+[[forcefields.global]]
+interaction = "Pair"
+potential = "ExcludedVolume"
+epsilon = 0.6
+env.R = 2.0
+env.OFF = 1
+ignore.particles_within.bond = 1
+parameters = [
+  {index = 0, radius = "R"}, {index = 0, offset = "OFF", radius = 1.5}, {index = 2, radius = "R"},
+  {index = 3, radius = 2.0}, {index = 4, radius = "R"},
+]
+"""
+    s = _read(text).spec
+    assert np.allclose(s.exv.p0, [0.2, 0.15, 0.2, 0.2, 0.2])
+    bad = text.replace('env.R = 2.0\n', '')
+    with pytest.raises(ValueError, match='named variable "R"'):
+        _read(bad)
