@@ -1,6 +1,5 @@
 """CPU tests of the C ABI and the host-side mirror of the reference's
 generators, topology and system assembly (no GPU needed)."""
-import math
 import re
 from pathlib import Path
 

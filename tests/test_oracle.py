@@ -181,11 +181,8 @@ def test_net_force_zero_and_invariance():
 
 
 def test_philox_known_answers():
-    """Philox4x32-10 against the published known-answer vectors."""
-    import ctypes as C
-    L = oracle.lib()
-    # gaussian3 consumes the raw words; check the generator through the
-    # uniforms it implies: re-derive words from a direct call.
+    """Philox4x32-10 (the round function the engine and the oracle share)
+    against the published known-answer vectors."""
     out = []
     for ctr, key, ref in (
         ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
