@@ -9,7 +9,8 @@ bench "step" is one persistent launch that advances every replica by
 Printed JSON keys: value (device-timed,
 state resident in HBM), e2e (through the public API with host buffers and
 H2D/D2H copies inside the timed region), roofline of the dominant kernel,
-cpu_baseline (the FP64 CPU oracle on a bounded sample), clocks sampled
+cpu_baseline (the FP32 Verlet-list CPU restatement, OpenMP, on the whole
+ensemble for a bounded number of steps), clocks sampled
 during the timed region, and the plain single-system path on the same mix.
 """
 from __future__ import annotations
@@ -152,7 +153,7 @@ def measured_hbm_gbs():
         return 6800.0, "fallback 6.8 TB/s"
 
 
-def batched_roofline(specs, K, launch_s, sm_max_mhz, traffic):
+def batched_roofline(specs, K, launch_s, sm_max_mhz, traffic, sms=None):
     """Roofline object of one k_batch launch advancing every replica K steps.
 
     HBM view: compulsory bytes per MD step of a design that streams the
@@ -175,7 +176,7 @@ def batched_roofline(specs, K, launch_s, sm_max_mhz, traffic):
     hbm_peak, hbm_src = measured_hbm_gbs()
     achieved_gbs = bytes_step * K / launch_s / 1e9
     achieved_tf = flops_step * K / launch_s / 1e12
-    fp32_peak = fp32_peak_tflops(sm_max_mhz)
+    fp32_peak, sms = fp32_peak_tflops(sm_max_mhz, sms)
     return {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": hbm_src,
             "kernel": "k_batch (persistent, shared-memory resident)",
@@ -184,7 +185,8 @@ def batched_roofline(specs, K, launch_s, sm_max_mhz, traffic):
             "pairs_within_cutoff_per_bead": pairs / beads,
             "fp32": {"achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tf / fp32_peak, "flops_per_launch": flops_step * K,
-                     "peak_source": "nominal 152 SMs x 128 FP32 lanes x 2 flop x max SM clock"}}
+                     "peak_source": f"{sms} SMs (read from the device) x 128 FP32 lanes x 2 flop x "
+                                    f"max SM clock"}}
 
 
 def run_ours(args, rank, world):
@@ -242,7 +244,7 @@ def run_ours(args, rank, world):
     roof = batched_roofline(specs, K, dev_time / args.steps, clk.summary().get("sm_max_mhz"),
                             args.traffic_bytes if args.traffic_bytes > 0 else None)
 
-    cpu = run_cpu_baseline(specs, sample_systems=args.cpu_sample, md_steps=args.cpu_steps) if rank == 0 else None
+    cpu = run_cpu_baseline(specs, md_steps=args.cpu_steps) if rank == 0 else None
     if cpu:
         cpu.pop("seconds", None)
 
@@ -399,33 +401,35 @@ def run_plain_configs(ocm, args):
     return out
 
 
-def run_cpu_baseline(specs, sample_systems=48, md_steps=20):
-    from concurrent.futures import ThreadPoolExecutor
-
+def run_cpu_baseline(specs, md_steps=500, warm_steps=20, threads=0):
+    """The CPU baseline: every replica of the workload advanced ``md_steps``
+    steps by the FP32 Verlet-list restatement (oracle/cpu_baseline.cpp),
+    OpenMP over replicas on all host cores.  Set-up and ``warm_steps``
+    steps (the first list builds) are outside the timed region."""
     from oracle import oracle
-    idx = np.linspace(0, len(specs) - 1, sample_systems).round().astype(int)
-    cores = os.cpu_count() or 1
-    oracle.lib()
-
-    def one(k):
-        s = specs[k]
-        x = s.pos.copy()
-        v = np.zeros_like(x)
-        oracle.simulate(s, x, v, md_steps, seed=3)
-        return s.n * md_steps
-
+    ens = oracle.CpuEnsemble(specs)
+    cores = threads or oracle.CpuEnsemble.max_threads()
+    ens.run(warm_steps, threads)
     t0 = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=cores) as ex:
-        bs = sum(ex.map(one, idx))
+    ens.run(md_steps, threads)
     t = time.perf_counter() - t0
-    return {"value": bs / t, "unit": "bead-steps/s", "cores": min(cores, len(idx)), "kind": "port",
-            "sample": f"{len(idx)} of the {len(specs)} replicas x {md_steps} steps, FP64 oracle "
-                      f"(all-pairs), one thread per replica", "seconds": t}
+    beads = int(sum(s.n for s in specs))
+    ens.close()
+    return {"value": beads * md_steps / t, "unit": "bead-steps/s", "cores": int(cores), "kind": "port",
+            "sample": f"all {len(specs)} replicas ({beads} beads) x {md_steps} MD steps; CPU restatement, "
+                      f"not the reference: FP32 pair/bonded arithmetic, Verlet half list (0.3 nm skin, "
+                      f"cell-grid build), OpenMP over replicas on {cores} threads", "seconds": t}
 
 
-def fp32_peak_tflops(sm_max_mhz):
+def fp32_peak_tflops(sm_max_mhz, sms=None):
+    """FP32 FMA peak of the device: its SM count (read from the device
+    unless given) x 128 FP32 lanes per SM (4 sub-partitions x 32 on this
+    architecture) x 2 flops x the maximum SM clock sampled during the run."""
+    if sms is None:
+        import torch
+        sms = torch.cuda.get_device_properties(local_device()).multi_processor_count
     mhz = sm_max_mhz or 2070.0
-    return 152 * 128 * 2 * mhz * 1e6 / 1e12
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, sms
 
 
 def dist_barrier(world):
@@ -454,29 +458,46 @@ def aggregate(beads, md_steps, steps, dev_time_local, world):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's arithmetic lives in OpenMM, which
+    is not installed on either machine, so the CPU restatement of the same
+    force field stands in (oracle/cpu_baseline.cpp, all host threads).
+    Each step advances the same workload as one step of this benchmark's own
+    arm: every replica of the ensemble by ``--md-steps`` MD steps.  This
+    process never loads the engine library."""
     if rank != 0:
         return None
+    from oracle import oracle
     specs = ensemble_specs()
-    steps_cpu = []
-    K = max(1, args.ref_md_steps)  # a bounded sample per reference step
+    beads = int(sum(s.n for s in specs))
+    K = args.md_steps
+    ens = oracle.CpuEnsemble(specs)
+    cores = oracle.CpuEnsemble.max_threads()
     for _ in range(args.warmup):
-        run_cpu_baseline(specs, sample_systems=8, md_steps=2)
+        ens.run(K)
+    times = []
     for _ in range(args.steps):
-        r = run_cpu_baseline(specs, sample_systems=args.cpu_sample, md_steps=K)
-        steps_cpu.append(r)
-    value = float(np.median([r["value"] for r in steps_cpu]))
-    ms_per_step = float(np.median([r["seconds"] for r in steps_cpu])) * 1e3
-    cpu = dict(steps_cpu[-1])
-    cpu.pop("seconds", None)
-    cpu["value"] = value
+        t0 = time.perf_counter()
+        ens.run(K)
+        times.append(time.perf_counter() - t0)
+    ens.close()
+    engine_loaded = "libocm_gb300" in Path("/proc/self/maps").read_text()
+    total = float(np.sum(times))
+    value = beads * K * args.steps / total
+    cpu = {"value": value, "unit": "bead-steps/s", "cores": int(cores), "kind": "port",
+           "sample": f"the whole workload: all {len(specs)} replicas ({beads} beads) x {K} MD steps per "
+                     f"step; CPU restatement, not the reference (FP32, Verlet half list, OpenMP over "
+                     f"replicas on {cores} threads)"}
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "bead-steps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Go-model proteins)",
             "config": {"workload": f"batched ensemble: {len(specs)} Go proteins, N log-uniform "
                                    f"[{SIZE_LO},{SIZE_HI}], T~U[280,360] K, dt=10 fs",
-                       "note": "OpenMM (the reference's arithmetic) is not installed; the FP64 "
-                               "CPU restatement of the reference's force field stands in"},
+                       "replicas": len(specs), "beads": beads, "md_steps_per_step": K,
+                       "note": "OpenMM (the reference's arithmetic) is not installed on either machine "
+                               "(probed); the FP32 CPU restatement of the reference's force field "
+                               "stands in"},
+            "engine_library_loaded": engine_loaded,
             "cpu_baseline": cpu,
             "e2e": {"value": value, "unit": "bead-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -491,9 +512,7 @@ def main():
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--plain-sample", type=int, default=24)
     ap.add_argument("--plain-chunks", type=int, default=2)
-    ap.add_argument("--cpu-sample", type=int, default=48)
-    ap.add_argument("--cpu-steps", type=int, default=600)  # ~5 s of the 16-core host
-    ap.add_argument("--ref-md-steps", type=int, default=20)  # MD steps per reference-arm step
+    ap.add_argument("--cpu-steps", type=int, default=500)  # MD steps of the whole ensemble, ~2 s
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--serve-requests", type=int, default=96)
     ap.add_argument("--traffic-bytes", type=float, default=K_BATCH_DRAM_BYTES,

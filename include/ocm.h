@@ -38,7 +38,8 @@ enum ocm_status {
     OCM_ERR_STATE = 5,              /* call made in the wrong state (e.g. no positions set) */
     OCM_ERR_UNSUPPORTED = 6,        /* a valid reference input this engine does not handle */
     OCM_ERR_NONFINITE = 7,          /* NaN/Inf found in forces or positions */
-    OCM_ERR_TIMEOUT = 8             /* a bounded device wait gave up */
+    OCM_ERR_TIMEOUT = 8             /* reserved, never returned: no kernel of this library waits on a
+                                       flag or on another block, so there is no bounded wait to give up */
 };
 
 /* Force-group limit; OpenMM allows 32 groups (Force::setForceGroup). */

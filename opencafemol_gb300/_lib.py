@@ -1,8 +1,10 @@
 """ctypes binding of ``libocm_gb300.so`` (the C ABI declared in include/ocm.h).
 
-The library is built in-tree by ``opencafemol_gb300.build.build()``.  There
-is no fallback: if the library is missing or does not load, importing the
-package raises.
+The library is built in-tree by ``opencafemol_gb300.build.build()``.  It is
+mapped on the first call into it (so that the numpy-only parts of the
+package, e.g. the seeded system generators, can be used by processes that
+must not load the engine).  There is no fallback: if the library is missing
+or does not load, that first call raises ImportError.
 """
 from __future__ import annotations
 
@@ -141,7 +143,25 @@ def _load() -> C.CDLL:
     return lib
 
 
-lib = _load()
+class _LazyLib:
+    """The ctypes library, loaded on first attribute access."""
+
+    __slots__ = ("_cdll",)
+
+    def __init__(self):
+        self._cdll = None
+
+    def loaded(self) -> bool:
+        return self._cdll is not None
+
+    def __getattr__(self, name):
+        cdll = self._cdll
+        if cdll is None:
+            cdll = self._cdll = _load()
+        return getattr(cdll, name)
+
+
+lib = _LazyLib()
 
 
 def check(code: int) -> None:

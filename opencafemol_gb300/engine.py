@@ -189,11 +189,21 @@ class Batch:
         v = None if velocities is None else as_f64(velocities)
         check(lib.ocm_batch_set_positions_many(self._h, len(sl), i64ptr(sl), dptr(x), dptr(v)))
 
+    @staticmethod
+    def _out_buffer(out, total: int) -> np.ndarray:
+        """The caller's output array, or a new one; the C call writes
+        total x 3 doubles into it, so anything else is refused."""
+        if out is None:
+            return np.zeros((total, 3))
+        if (not isinstance(out, np.ndarray) or out.dtype != np.float64 or out.shape != (total, 3)
+                or not out.flags.c_contiguous or not out.flags.writeable):
+            raise ValueError(f"out must be a writeable C-contiguous float64 array of shape ({total}, 3)")
+        return out
+
     def get_positions_many(self, slots, out=None) -> np.ndarray:
         sl = np.ascontiguousarray(slots, np.int64)
         total = sum(self._n[int(k)] for k in sl)
-        if out is None:
-            out = np.zeros((total, 3))
+        out = self._out_buffer(out, total)
         check(lib.ocm_batch_get_positions_many(self._h, len(sl), i64ptr(sl), dptr(out)))
         return out
 
@@ -202,8 +212,7 @@ class Batch:
         allocation; at most 131072 beads and 2048 slots per call)."""
         sl = np.ascontiguousarray(slots, np.int64)
         total = sum(self._n[int(k)] for k in sl)
-        if out is None:
-            out = np.zeros((total, 3))
+        out = self._out_buffer(out, total)
         check(lib.ocm_batch_get_positions_many_noalloc(self._h, len(sl), i64ptr(sl), dptr(out)))
         return out
 

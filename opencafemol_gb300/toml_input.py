@@ -99,18 +99,35 @@ class _Params(dict):
     def get(self, key, default=None):
         return self[key] if key in self else default
 
+    def get_or(self, key, default):
+        """Lenient lookup of an optional key (Utility.hpp find_parameter_or,
+        :140-155): a missing key, or a name that env does not define, gives
+        the default instead of an error."""
+        if key not in self:
+            return default
+        v = super().__getitem__(key)
+        if isinstance(v, str):
+            return self.env.get(v, default)
+        return v
+
 
 def _params(block: dict):
     env = block.get("env")
     return [_Params(p, env) for p in block["parameters"]]
 
 
+def _offset(p: dict) -> int:
+    """The optional index offset, read as the reference reads it
+    (find_parameter_or(params, env, "offset", 0))."""
+    return int(p.get_or("offset", 0) if isinstance(p, _Params) else p.get("offset", 0))
+
+
 def _index(p: dict) -> int:
-    return int(p["index"]) + int(p.get("offset", 0))
+    return int(p["index"]) + _offset(p)
 
 
 def _indices(p: dict) -> list[int]:
-    off = int(p.get("offset", 0))
+    off = _offset(p)
     return [int(v) + off for v in p["indices"]]
 
 

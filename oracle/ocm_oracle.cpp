@@ -37,6 +37,7 @@
 #include <functional>
 #include <vector>
 
+#include "oracle_system.h"
 #include "oracle_tables.h"
 
 namespace oracle {
@@ -309,97 +310,6 @@ static bool cell_pairs(int64_t n, const V3* x, bool periodic, const double L[3],
 
 extern "C" {
 
-// Flat description of one system in the units the generators receive.
-typedef struct OracleSystem {
-    int64_t n;
-    const double* pos;  // 3n
-    int periodic;
-    double box[3];
-    // harmonic bonds: k is the OpenMM 1/2 k (r - r0)^2 constant
-    int64_t n_bonds;
-    const int64_t* bond_idx;
-    const double* bond_v0;
-    const double* bond_k;
-    int bond_periodic;
-    // Go contacts
-    int64_t n_go;
-    const int64_t* go_idx;
-    const double* go_k;
-    const double* go_r0;
-    int go_periodic;
-    // flexible-local angles: centre-residue table index (0..19)
-    int64_t n_fla;
-    const int64_t* fla_idx;
-    const double* fla_k;
-    const int32_t* fla_aa;
-    // flexible-local dihedrals: the two residue indices of the "AAA-BBB" coef
-    int64_t n_fld;
-    const int64_t* fld_idx;
-    const double* fld_k;
-    const int32_t* fld_aa1;
-    const int32_t* fld_aa2;
-    // pair terms; *_ign_bond / *_ign_contact: exclusion distance along
-    // "bond" / "contact" edges (-1: none)
-    int exv_on;
-    double exv_eps, exv_ratio;
-    const double* exv_radius;
-    int exv_ign_bond, exv_ign_contact;
-    int dh_on;
-    double dh_I, dh_T, dh_ratio;
-    const double* dh_q;
-    int dh_ign_bond, dh_ign_contact;
-    int ljr_on;
-    double ljr_ratio;
-    const double* ljr_eps;
-    const double* ljr_sigma;
-    int ljr_ign_bond, ljr_ign_contact;
-    int lja_on;
-    double lja_ratio;
-    const double* lja_eps;
-    const double* lja_sigma;
-    int lja_ign_bond, lja_ign_contact;
-    int fp32_cutoff;  // decide r < rc on the engine's FP32 r^2
-    // pair enumeration: 0 all pairs, 1 cell grid, -1 cell grid above 4096 beads
-    int pair_cells;
-    // AICG2+ Gaussian bonds k exp(-(r - v0)^2 / (2 sigma^2)) and dihedrals
-    // k exp(-dphi^2 / (2 sigma^2)) (theta0, sigma in radians)
-    int64_t n_gb;
-    const int64_t* gb_idx;
-    const double* gb_k;
-    const double* gb_v0;
-    const double* gb_sigma;
-    int gb_periodic;
-    int64_t n_gd;
-    const int64_t* gd_idx;
-    const double* gd_k;
-    const double* gd_theta0;
-    const double* gd_sigma;
-    int gd_periodic;
-    // WeeksChandlerAndersen in the repulsive LJ slot: geometric epsilon mean
-    // (WeeksChandlerAndersenForceFieldGenerator.cpp:38-45)
-    int ljr_geometric;
-    // uniform generators: per-particle side bits (1 former, 2 latter); a
-    // pair interacts if one is former and the other latter; null = all
-    const int8_t* ljr_side;
-    const int8_t* lja_side;
-    // capped Go contacts (CappedGoContactForceFieldGenerator.cpp:5-31)
-    int64_t n_cgo;
-    const int64_t* cgo_idx;
-    const double* cgo_k;
-    const double* cgo_r0;
-    const double* cgo_cap;   // capping ratio per contact
-    int cgo_periodic;
-    int cgo_contact_edges;   // the contacts are "contact" edges of the topology
-    // group-based ignores (InteractionGroup.hpp:19-99): per-particle group
-    // id (-1 none) and, per pair term (EXV, DH, LJR, LJA), the ignored
-    // (group, group) pairs, symmetric
-    const int32_t* grp;
-    int64_t n_igp[4];
-    const int32_t* igp[4];
-    // molecule-based ignores per pair term: no pair inside one molecule (the
-    // connected components of the bond edges, Topology.cpp:7-73)
-    int ign_molecule[4];
-} OracleSystem;
 
 // Energy slots: EXV, DH, LJR, LJA, HB, GO, FLA, FLD, GB, GD, capped Go.
 
@@ -412,8 +322,14 @@ int oracle_dh_params(double I, double T, double ratio, double* out5) {
     out5[4] = p.eps_r;
     return 0;
 }
-double oracle_fla_min_energy(int aa) { return fla_min_energy(aa); }
-double oracle_fld_min_energy(int cls) { return fld_min_energy(kFld[cls].c); }
+double oracle_fla_min_energy(int aa) { return fla_min_energy_cached(aa); }
+// Largest and second largest present value (strict comparison for EXV).
+void oracle_top_two(const double* v, int64_t n, int strict, double* out2) {
+    const auto t = top_two(v, n, strict != 0);
+    out2[0] = t.first;
+    out2[1] = t.second;
+}
+double oracle_fld_min_energy(int cls) { return fld_min_energy_cached(cls); }
 int oracle_natural_spline(const double* y10, double h, double* M10) {
     natural_spline(y10, h, M10);
     return 0;

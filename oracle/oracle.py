@@ -73,6 +73,14 @@ def lib() -> C.CDLL:
                                       C.c_double, C.c_uint32, C.c_uint64, C.c_int64]
         L.oracle_gaussian3.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, _D]
         L.oracle_gaussian3.restype = None
+        L.cpu_prepare.argtypes = [C.POINTER(OracleSystem), _D, _D, C.c_double, C.c_double, C.c_double,
+                                  C.c_uint32, C.POINTER(C.c_void_p)]
+        L.cpu_run_many.argtypes = [C.POINTER(C.c_void_p), C.c_int64, C.c_int64, C.c_int]
+        L.cpu_evaluate.argtypes = [C.c_void_p, _D, _D]
+        L.cpu_get_positions.argtypes = [C.c_void_p, _D]
+        L.cpu_free.argtypes = [C.c_void_p]
+        L.cpu_free.restype = None
+        L.cpu_max_threads.restype = C.c_int
         _lib = L
     return _lib
 
@@ -284,3 +292,62 @@ def gaussian3(seed, stream, bead, step, purpose=0):
     g = np.zeros(3)
     lib().oracle_gaussian3(seed, stream, bead, step, purpose, g.ctypes.data_as(_D))
     return g
+
+
+class CpuEnsemble:
+    """The timed CPU baseline (cpu_baseline.cpp): an FP32, Verlet-list,
+    OpenMP restatement of the same force field and integrator, holding an
+    ensemble of systems.  Set-up happens here (untimed); ``run`` advances
+    every system by ``steps`` Langevin steps on ``threads`` host threads (0:
+    all).  Not the reference (OpenMM is not installed) and not the checker:
+    it exists to be timed."""
+
+    def __init__(self, specs, seeds=None, velocities=None):
+        L = lib()
+        self.n = [int(sp.n) for sp in specs]
+        self._h = (C.c_void_p * len(specs))()
+        for k, sp in enumerate(specs):
+            s, keep = make_system(sp, fp32_cutoff=False)
+            m = np.ascontiguousarray(sp.masses, np.float64)
+            v = None if velocities is None else np.ascontiguousarray(velocities[k], np.float64)
+            seed = 1000 + k if seeds is None else int(seeds[k])
+            h = C.c_void_p()
+            code = L.cpu_prepare(C.byref(s), None if v is None else v.ctypes.data_as(_D), m.ctypes.data_as(_D),
+                                 float(sp.temperature), float(sp.friction), float(sp.dt), seed, C.byref(h))
+            del keep
+            if code != 0:
+                self.close()
+                raise ValueError(f"system {k}: a feature the CPU restatement does not cover (code {code})")
+            self._h[k] = h
+
+    @staticmethod
+    def max_threads() -> int:
+        return int(lib().cpu_max_threads())
+
+    def run(self, steps: int, threads: int = 0) -> None:
+        lib().cpu_run_many(self._h, len(self.n), int(steps), int(threads))
+
+    def evaluate(self, k: int):
+        """FP32 forces (n, 3) and the EXV, DH, LJR, LJA, HB, GO, FLA, FLD energies."""
+        f = np.zeros((self.n[k], 3))
+        e = np.zeros(8)
+        lib().cpu_evaluate(self._h[k], f.ctypes.data_as(_D), e.ctypes.data_as(_D))
+        return f, e
+
+    def positions(self, k: int) -> np.ndarray:
+        x = np.zeros((self.n[k], 3))
+        lib().cpu_get_positions(self._h[k], x.ctypes.data_as(_D))
+        return x
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is None:
+            return
+        for k in range(len(h)):
+            if h[k]:
+                lib().cpu_free(h[k])
+                h[k] = None
+        self._h = None
+
+    def __del__(self):
+        self.close()

@@ -78,5 +78,6 @@ def make(sample_dir: Path) -> dict:
 
 
 if __name__ == "__main__":
-    src = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference/sample/toml_input")
-    print(json.dumps(make(src), indent=1))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference>/sample/toml_input")
+    print(json.dumps(make(Path(sys.argv[1])), indent=1))

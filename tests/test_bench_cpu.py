@@ -12,7 +12,7 @@ from conftest import ROOT
 def test_roofline_object_is_json():
     import bench
     specs = bench.ensemble_specs(count=6)
-    roof = bench.batched_roofline(specs, K=10, launch_s=1e-3, sm_max_mhz=2070.0, traffic=None)
+    roof = bench.batched_roofline(specs, K=10, launch_s=1e-3, sm_max_mhz=2070.0, traffic=None, sms=152)
     json.dumps(roof)
     assert roof["bound"] == "hbm" and roof["unit"] == "GB/s"
     beads = sum(s.n for s in specs)
@@ -24,7 +24,7 @@ def test_roofline_object_is_json():
 
 def test_reference_arm_line():
     out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1",
-                          "--warmup", "3", "--cpu-sample", "2", "--cpu-steps", "1"],
+                          "--warmup", "3", "--md-steps", "2"],
                          cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr
     line = json.loads(out.stdout.strip().splitlines()[-1])
@@ -34,3 +34,6 @@ def test_reference_arm_line():
         assert k in line, k
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
     assert line["value"] > 0
+    # the whole 512-replica workload, and the engine library never mapped
+    assert line["config"]["replicas"] == 512 and line["config"]["md_steps_per_step"] == 2
+    assert line["engine_library_loaded"] is False

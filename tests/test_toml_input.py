@@ -345,3 +345,8 @@ parameters = [
     bad = text.replace('env.R = 2.0\n', '')
     with pytest.raises(ValueError, match='named variable "R"'):
         _read(bad)
+    # offset is optional (find_parameter_or, Utility.hpp:140-155): a name
+    # that env does not define falls back to 0 instead of failing
+    lenient = text.replace('env.OFF = 1\n', '')
+    s = _read(lenient).spec
+    assert np.allclose(s.exv.p0, [0.15, np.nan, 0.2, 0.2, 0.2], equal_nan=True)

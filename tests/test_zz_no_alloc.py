@@ -61,8 +61,15 @@ def test_noalloc_limits(gpu):
                     40 * (MAX_SLOTS + 1))
     assert code == 1
     assert f"at most {MAX_SLOTS} slots" in lib.ocm_last_error().decode()
-    # the limits are exact: the largest allowed request succeeds
-    n_ok = MAX_BEADS // 800
-    code, x = _read(gpu, b, lib.ocm_batch_get_positions_many_noalloc, [slots[0]] * n_ok, 800 * n_ok)
+    # the limits are exact: 2048 reads of a 64-bead slot are exactly 131072
+    # beads in exactly 2048 slots and succeed; one more bead in the same
+    # number of slots (2047 reads of 64 + one of 65) is refused
+    b3, s3 = _batch(gpu, [64, 65], seed0=3400)
+    code, x = _read(gpu, b3, lib.ocm_batch_get_positions_many_noalloc, [s3[0]] * MAX_SLOTS, 64 * MAX_SLOTS)
+    assert 64 * MAX_SLOTS == MAX_BEADS
     assert code == 0
-    assert np.array_equal(x[:800], b.positions(slots[0])) and np.array_equal(x[-800:], x[:800])
+    assert np.array_equal(x[:64], b3.positions(s3[0])) and np.array_equal(x[-64:], x[:64])
+    over = [s3[0]] * (MAX_SLOTS - 1) + [s3[1]]
+    code, _ = _read(gpu, b3, lib.ocm_batch_get_positions_many_noalloc, over, MAX_BEADS + 1)
+    assert code == 1
+    assert f"at most {MAX_BEADS} beads" in lib.ocm_last_error().decode()
