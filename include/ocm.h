@@ -327,12 +327,33 @@ int64_t ocm_batch_footprint(const ocm_system* sys);
 int ocm_batch_admit(ocm_batch* batch, const ocm_system* sys, const double* positions,
                     const double* velocities, double temperature, double friction,
                     double step_size, int32_t seed, int64_t n_steps, int64_t* slot_out);
+/* ocm_batch_admit for a trajectory that already ran steps_done of its
+ * n_steps steps (preemption / resume): with the positions and velocities
+ * read back from the slot it left (ocm_batch_get_positions /
+ * ocm_batch_get_velocities) and the same seed, the Langevin noise stream
+ * continues at step steps_done and the trajectory is the one it would have
+ * followed without the interruption.  The reference restarts a run from the
+ * TOML pos / vel keys instead (src/input/ReadTOMLInput.cpp:908-962). */
+int ocm_batch_admit_resume(ocm_batch* batch, const ocm_system* sys, const double* positions,
+                           const double* velocities, double temperature, double friction,
+                           double step_size, int32_t seed, int64_t n_steps, int64_t steps_done,
+                           int64_t* slot_out);
 /* Advance every admitted, unfinished system by min(steps_per_launch,
  * remaining) steps with one persistent launch; asynchronous with respect
- * to the host unless sync != 0. */
+ * to the host unless sync != 0.  A system whose force, velocity or
+ * position becomes non-finite, or whose force exceeds 1e9 kJ/mol/nm in a
+ * component, stops at that step and is reported by ocm_batch_slot_status;
+ * the other systems of the launch are not affected. */
 int ocm_batch_run(ocm_batch* batch, int32_t steps_per_launch, int sync);
-/* Wait for the last launch and list the slots whose systems have finished. */
+/* Wait for the last launch and list the slots whose systems have finished:
+ * every step done, or stopped because the system blew up (see
+ * ocm_batch_slot_status). */
 int ocm_batch_finished(ocm_batch* batch, int64_t* slots, int64_t capacity, int64_t* n_out);
+/* Wait for the last launch; *status = OCM_OK, or OCM_ERR_NONFINITE if the
+ * slot's system blew up (it is no longer advanced; its state is the one of
+ * the failing step).  The reference terminates the whole run in that case
+ * (src/OpenAICG2Plus.cpp:84-93). */
+int ocm_batch_slot_status(ocm_batch* batch, int64_t slot, int32_t* status);
 int ocm_batch_get_positions(ocm_batch* batch, int64_t slot, double* xyz);
 int ocm_batch_get_velocities(ocm_batch* batch, int64_t slot, double* v);
 /* Replace the positions (and, if v is not NULL, velocities) of n slots in
@@ -367,7 +388,9 @@ int ocm_batch_get_positions_many_noalloc(ocm_batch* batch, int64_t n, const int6
                                          double* xyz);
 int ocm_batch_steps_done(ocm_batch* batch, int64_t slot, int64_t* steps);
 /* Forces (3*n) and per-group energies (OCM_MAX_GROUPS) of one slot at its
- * current positions, evaluated by the batched kernel. */
+ * current positions, evaluated by the batched kernel.  Returns
+ * OCM_ERR_NONFINITE (with the outputs filled) if a force is non-finite or
+ * exceeds 1e9 kJ/mol/nm in a component. */
 int ocm_batch_get_state(ocm_batch* batch, int64_t slot, uint32_t groups, double* forces,
                         double* energies);
 /* Free a slot (its beads' capacity is returned to the pool). */

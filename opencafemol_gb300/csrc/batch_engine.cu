@@ -3,17 +3,22 @@
 //
 // One CTA per SM (or more, by occupancy) pulls systems from a work queue
 // ordered by decreasing cost.  A claimed system is loaded into shared
-// memory (FP64 master positions, FP32 positions and parameters, velocities,
-// 64-bit fixed-point force accumulators) and advanced for the whole chunk
-// without touching global memory except for L2-resident static parameters:
-//   tiles:    every 32x32 cluster pair (I <= J) whose bounding boxes lie
-//             within the largest cutoff, recomputed every step - no
-//             neighbour list and no skin;
-//   bonded:   bonds, Go contacts, FLA, FLD;
-//   update:   Langevin step per bead, fused with zeroing the accumulators
-//             and recomputing each cluster's bounding box.
-// Two __syncthreads per step.  Results depend only on (system, seed, step):
-// a system gives the same trajectory alone or in any mix.
+// memory (float-float positions, parameters, velocities) and advanced for
+// the whole chunk without touching global memory except for its neighbour
+// list entries beyond the shared-memory share and L2-resident parameters.
+// Per MD step:
+//   list:     Verlet lists with a 0.3 nm skin, rebuilt when a bead has
+//             moved more than half the skin (one thread per bead, j order);
+//   forces:   pair units (a bead and a j-range of its list) write the
+//             bead's pair force; one lane per chain position evaluates the
+//             chain-local bonded terms starting there and the lanes combine
+//             them by shuffles; other bonded terms are gathered by each of
+//             their beads;
+//   update:   Langevin step per bead from the summed forces, bounding boxes,
+//             displacement and blow-up checks.
+// No atomics on forces: every bead's force is a sum in a fixed order, so a
+// system gives the same trajectory alone, in any mix, for any chunking and
+// for any threads per CTA.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,6 +47,10 @@ constexpr int kMaxClusters = 64;  // 2048 beads per system
 constexpr int kSplitUnits = 512;
 constexpr int kMaxUnits = kSplitUnits;
 constexpr int kMaxSplit = 8;
+// A force component beyond this (kJ/mol/nm) marks a blown-up system: far
+// above any physical coarse-grained force, and the bound of the plain
+// engine's fixed-point accumulators.
+constexpr float kForceLimit = 1.0e9f;
 
 __host__ __device__ __forceinline__ int pair_split(int n) {
     int S = 1;
@@ -60,7 +69,7 @@ struct BatchArgs {
     int k;
     int nmax;
     double* energy;              // [slot][kNumSlots]
-    unsigned long long* forces;  // eval output [3][nmax]
+    float* forces;               // eval output [3][nmax]
     uint16_t* lists;             // neighbour-list arena
     uint32_t slots_enabled;
     size_t smem_bytes;           // dynamic shared memory of the launch
@@ -70,40 +79,6 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
     return v;
-}
-
-// 64-bit fixed-point force accumulator in shared memory, kept as separate
-// low and high 32-bit words ([3][nmax] each).  An addition adds the low word
-// with a 32-bit atomic, takes the carry from the returned old value and adds
-// high + carry: the final 64-bit value is exact and independent of the order
-// of the additions, and two 32-bit shared atomics cost far less than one
-// 64-bit shared atomic.
-struct FixedAcc {
-    uint32_t* lo;
-    uint32_t* hi;
-};
-
-__device__ __forceinline__ void facc_add(const FixedAcc& F, int idx, float f) {
-    const unsigned long long v = to_fixed(f);
-    const uint32_t l = (uint32_t)v;
-    const uint32_t old = atomicAdd(&F.lo[idx], l);
-    const uint32_t h = (uint32_t)(v >> 32) + (old + l < old ? 1u : 0u);
-    if (h) atomicAdd(&F.hi[idx], h);
-}
-
-__device__ __forceinline__ long long facc_get(const FixedAcc& F, int idx) {
-    return (long long)(((unsigned long long)F.hi[idx] << 32) | F.lo[idx]);
-}
-
-__device__ __forceinline__ void facc_zero(const FixedAcc& F, int idx) {
-    F.lo[idx] = 0u;
-    F.hi[idx] = 0u;
-}
-
-__device__ __forceinline__ void sadd(const FixedAcc& F, int nmax, int b, float3 f) {
-    facc_add(F, b, f.x);
-    facc_add(F, nmax + b, f.y);
-    facc_add(F, 2 * nmax + b, f.z);
 }
 
 __device__ __forceinline__ float3 lo3(const float* sxl, int nmax, int i) {
@@ -127,85 +102,188 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
     hi = h;
 }
 
-template <int TERMS, bool LABELS, bool ENERGY>
-__device__ __forceinline__ void batch_tile(int I, int J, int mslot, const uint32_t* __restrict__ masks,
-                                           const float4* sx, const float4* sp0, const float4* sp1,
-                                           const uint32_t* slab, const FixedAcc& sF, int nmax,
-                                           const PairConsts& pc, uint32_t excl_all, int lane,
-                                           float* eacc) {
-    const int ki = I * 32 + lane, kj = J * 32 + lane;
-    const float4 xi = sx[ki];
-    const float4 p0i = sp0[ki];
-    const float4 p1i = (TERMS & kTermLJA) ? sp1[ki] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const uint32_t labi = LABELS ? slab[ki] : 0u;
-    float4 xj = sx[kj];
-    float4 p0j = sp0[kj];
-    float4 p1j = (TERMS & kTermLJA) ? sp1[kj] : make_float4(0.f, 0.f, 0.f, 0.f);
-    uint32_t labj = LABELS ? slab[kj] : 0u;
-    uint32_t mw[4] = {0u, 0u, 0u, 0u};
-    if (mslot >= 0) {
+__device__ __forceinline__ void add3(float3& a, float3 b) {
+    a.x += b.x;
+    a.y += b.y;
+    a.z += b.z;
+}
+__device__ __forceinline__ float3 neg3(float3 a) { return make_float3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float3 shfl_up3(float3 v, int d) {
+    return make_float3(__shfl_up_sync(kFull, v.x, d), __shfl_up_sync(kFull, v.y, d), __shfl_up_sync(kFull, v.z, d));
+}
+__device__ __forceinline__ float3 shfl3(float3 v, int src) {
+    return make_float3(__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src), __shfl_sync(kFull, v.z, src));
+}
+
+// Per-term energy accumulators: FP64 sums of the FP32 per-term energies.
+struct EnergyAcc {
+    double e[kNumSlots];
+    __device__ void zero() {
 #pragma unroll
-        for (int term = 0; term < 4; ++term)
-            if (TERMS & (1 << term)) mw[term] = masks[(size_t)mslot * 128 + term * 32 + lane];
+        for (int k = 0; k < kNumSlots; ++k) e[k] = 0.0;
     }
-    const bool diag = I == J;
-    float3 fi = make_float3(0.f, 0.f, 0.f), fj = make_float3(0.f, 0.f, 0.f);
-    PairEnergy e;
-    e.zero();
-    const float3 nobox = make_float3(0.f, 0.f, 0.f);
-    for (int r = 0; r < 32; ++r) {
-        const bool do_pair = !diag || (r > 0 && (r < 16 || (r == 16 && lane < 16)));
-        if (do_pair) {
-            const float3 d = separation<false>(xi, xj, nobox, nobox);
-            const float r2 = norm2(d);
-            if (r2 < pc.list_rc2) {
-                uint32_t ex = excl_all;
-#pragma unroll
-                for (int term = 0; term < 4; ++term)
-                    if (TERMS & (1 << term)) ex |= ((mw[term] >> r) & 1u) << term;
-                if (LABELS) {
-#pragma unroll
-                    for (int term = 0; term < 4; ++term)
-                        if ((TERMS & (1 << term)) && (pc.uses_labels & (1 << term)) &&
-                            !labels_allow(labi, labj, term, pc.allow[term]))
-                            ex |= 1u << term;
-                }
-                const float s = pair_scalar<TERMS, ENERGY>(r2, p0i, p0j, p1i, p1j, ex, pc, e);
-                fi.x -= s * d.x;
-                fi.y -= s * d.y;
-                fi.z -= s * d.z;
-                fj.x += s * d.x;
-                fj.y += s * d.y;
-                fj.z += s * d.z;
+};
+
+// ---------------------------------------------------------------------------
+// Bonded records as staged in shared memory.
+// ---------------------------------------------------------------------------
+struct Bonded {
+    const float4* bpar;     // bond (p0, p1, r0sq_hi, r0sq_lo)
+    const uint32_t* bij;    // i | j << 16 | kind << 30
+    const uint2* aij;       // (i | j << 16, k | table << 16)
+    const float* ak;
+    const uint4* drec;      // (i | j << 16 | gauss << 31, k | l << 16, table / gauss index, k bits)
+    const float2* gdp;      // Gaussian dihedral (theta0, 1 / (2 sigma^2))
+    const FlaTable* fla;
+    const FldTable* fld;
+    const uint16_t* cb;     // chain bonds starting at bead b: [cb[b], cb[b+1])
+    const uint16_t* ca;     // chain angles
+    const uint16_t* cd;     // chain dihedrals
+    const uint16_t* gs;     // gather entries of bead b: [gs[b], gs[b+1])
+    const uint32_t* gl;     // type << 30 | role << 28 | term index
+};
+
+// Bond b: force on its first bead (the second gets the negation), energy.
+__device__ __forceinline__ float3 bond_force(const Bonded& B, int b, const float4* sx, const float* sxl, int ns,
+                                             float& en, int& slot) {
+    const uint32_t ij = B.bij[b];
+    const int kind = (int)(ij >> 30);
+    slot = bond_slot(kind);
+    const int bi = ij & 0xFFFF, bj = (ij >> 16) & 0x3FFF;
+    const float4 bp = B.bpar[b];
+    float3 dh, dl;
+    ff_sep(sx[bi], lo3(sxl, ns, bi), sx[bj], lo3(sxl, ns, bj), dh, dl);
+    const float3 d = make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
+    const float delta = ff_bond_delta(dh, dl, bp.z, bp.w);
+    const float sc = bond_scalar(kind, norm2(d), delta, bp.x, bp.y, bp.z, en);
+    return make_float3(-sc * d.x, -sc * d.y, -sc * d.z);
+}
+
+// Angle a: forces on its first (f1) and last (f3) bead; the middle one
+// gets -(f1 + f3).
+__device__ __forceinline__ void angle_force(const Bonded& B, int a, const float4* sx, const float* sxl, int ns,
+                                            float3& f1, float3& f3, float& en) {
+    const uint2 g = B.aij[a];
+    const int gi = g.x & 0xFFFF, gj = g.x >> 16, gk = g.y & 0xFFFF;
+    const float3 u = ffsep(sx, sxl, ns, gj, gi);
+    const float3 v = ffsep(sx, sxl, ns, gj, gk);
+    fla_forces(u, v, B.ak[a], B.fla[g.y >> 16], f1, f3, en);
+}
+
+// Dihedral q: forces on its four beads, energy and slot.
+__device__ __forceinline__ void dihedral_force(const Bonded& B, int q, const float4* sx, const float* sxl, int ns,
+                                               float3& f1, float3& f2, float3& f3, float3& f4, float& en,
+                                               int& slot) {
+    const uint4 qd = B.drec[q];
+    const bool gauss = (qd.x >> 31) != 0;
+    slot = gauss ? kSlotGD : kSlotFLD;
+    const int qi = qd.x & 0xFFFF, qj = (qd.x >> 16) & 0x7FFF, qk = qd.y & 0xFFFF, ql = qd.y >> 16;
+    const float3 F = ffsep(sx, sxl, ns, qj, qi);
+    const float3 G = ffsep(sx, sxl, ns, qk, qj);
+    const float3 H = ffsep(sx, sxl, ns, qk, ql);
+    if (gauss) {
+        const float2 gp = B.gdp[qd.z];
+        gauss_dihedral_forces(F, G, H, __uint_as_float(qd.w), gp.x, gp.y, f1, f2, f3, f4, en);
+    } else {
+        fld_forces(F, G, H, __uint_as_float(qd.w), B.fld[qd.z], f1, f2, f3, f4, en);
+    }
+}
+
+__device__ __forceinline__ bool slot_on(uint32_t slots_en, int slot) { return (slots_en >> slot) & 1u; }
+
+// Bonded force on bead b = I * 32 + lane of cluster I (one warp).  The lane
+// evaluates every chain-local term starting at b (bonds b-b+1, angles
+// b..b+2, dihedrals b..b+3) once, keeping its contributions to b..b+3; the
+// lanes then add what lanes 1..3 below them send up, in a fixed order, and
+// the three contributions that cross into cluster I + 1 go to carry[I].
+// Terms that are not chain-local are evaluated by each of their beads
+// (gather entries) and only that bead's share is kept.
+template <bool ENERGY>
+__device__ __forceinline__ float3 bonded_cluster(const Bonded& B, int I, int n, int lane, const float4* sx,
+                                                 const float* sxl, int ns, uint32_t slots_en, float3* carry,
+                                                 EnergyAcc& ea) {
+    const int b = I * 32 + lane;
+    float3 o0 = make_float3(0.f, 0.f, 0.f), o1 = o0, o2 = o0, o3 = o0;
+    if (b < n) {
+        for (int t = B.cb[b]; t < B.cb[b + 1]; ++t) {
+            float en;
+            int sl;
+            const float3 f = bond_force(B, t, sx, sxl, ns, en, sl);
+            if (!slot_on(slots_en, sl)) continue;
+            add3(o0, f);
+            add3(o1, neg3(f));
+            if (ENERGY) ea.e[sl] += (double)en;
+        }
+        if (slot_on(slots_en, kSlotFLA))
+            for (int t = B.ca[b]; t < B.ca[b + 1]; ++t) {
+                float3 f1, f3;
+                float en;
+                angle_force(B, t, sx, sxl, ns, f1, f3, en);
+                add3(o0, f1);
+                add3(o2, f3);
+                add3(o1, make_float3(-f1.x - f3.x, -f1.y - f3.y, -f1.z - f3.z));
+                if (ENERGY) ea.e[kSlotFLA] += (double)en;
             }
+        for (int t = B.cd[b]; t < B.cd[b + 1]; ++t) {
+            float3 f1, f2, f3, f4;
+            float en;
+            int sl;
+            dihedral_force(B, t, sx, sxl, ns, f1, f2, f3, f4, en, sl);
+            if (!slot_on(slots_en, sl)) continue;
+            add3(o0, f1);
+            add3(o1, f2);
+            add3(o2, f3);
+            add3(o3, f4);
+            if (ENERGY) ea.e[sl] += (double)en;
         }
-        const int src = (lane + 1) & 31;
-        xj.x = __shfl_sync(kFull, xj.x, src);
-        xj.y = __shfl_sync(kFull, xj.y, src);
-        xj.z = __shfl_sync(kFull, xj.z, src);
-        if (TERMS & kTermEXV) p0j.x = __shfl_sync(kFull, p0j.x, src);
-        if (TERMS & kTermDH) p0j.y = __shfl_sync(kFull, p0j.y, src);
-        if (TERMS & kTermLJR) {
-            p0j.z = __shfl_sync(kFull, p0j.z, src);
-            p0j.w = __shfl_sync(kFull, p0j.w, src);
-        }
-        if (TERMS & kTermLJA) {
-            p1j.x = __shfl_sync(kFull, p1j.x, src);
-            p1j.y = __shfl_sync(kFull, p1j.y, src);
-        }
-        if (LABELS) labj = __shfl_sync(kFull, labj, src);
-        fj.x = __shfl_sync(kFull, fj.x, src);
-        fj.y = __shfl_sync(kFull, fj.y, src);
-        fj.z = __shfl_sync(kFull, fj.z, src);
     }
-    sadd(sF, nmax, ki, fi);
-    sadd(sF, nmax, kj, fj);
-    if (ENERGY) {
-        eacc[kSlotEXV] += e.exv;
-        eacc[kSlotDH] += e.dh;
-        eacc[kSlotLJR] += e.ljr;
-        eacc[kSlotLJA] += e.lja;
+    // contributions of the three chain positions below, in the order
+    // 1, 2, 3 positions back
+    const float3 u1 = shfl_up3(o1, 1), u2 = shfl_up3(o2, 2), u3 = shfl_up3(o3, 3);
+    float3 fb = o0;
+    if (lane >= 1) add3(fb, u1);
+    if (lane >= 2) add3(fb, u2);
+    if (lane >= 3) add3(fb, u3);
+    // what lanes 29..31 send into the next cluster's first three beads
+    const float3 a1 = shfl3(o1, 31), a2 = shfl3(o2, 30), a3 = shfl3(o3, 29);
+    const float3 b2 = shfl3(o2, 31), b3 = shfl3(o3, 30);
+    const float3 c3 = shfl3(o3, 31);
+    if (lane == 0) {
+        float3 c0 = a1;
+        add3(c0, a2);
+        add3(c0, a3);
+        float3 c1 = b2;
+        add3(c1, b3);
+        carry[3 * I] = c0;
+        carry[3 * I + 1] = c1;
+        carry[3 * I + 2] = c3;
     }
+    if (b < n) {
+        for (int g = B.gs[b]; g < B.gs[b + 1]; ++g) {
+            const uint32_t e = B.gl[g];
+            const int type = (int)(e >> 30), role = (int)((e >> 28) & 3u), t = (int)(e & 0x0FFFFFFFu);
+            float en;
+            float3 f;
+            int sl;
+            if (type == 0) {
+                f = bond_force(B, t, sx, sxl, ns, en, sl);
+                if (role == 1) f = neg3(f);
+            } else if (type == 1) {
+                sl = kSlotFLA;
+                float3 f1, f3;
+                angle_force(B, t, sx, sxl, ns, f1, f3, en);
+                f = role == 0 ? f1 : role == 2 ? f3 : make_float3(-f1.x - f3.x, -f1.y - f3.y, -f1.z - f3.z);
+            } else {
+                float3 f1, f2, f3, f4;
+                dihedral_force(B, t, sx, sxl, ns, f1, f2, f3, f4, en, sl);
+                f = role == 0 ? f1 : role == 1 ? f2 : role == 2 ? f3 : f4;
+            }
+            if (!slot_on(slots_en, sl)) continue;
+            add3(fb, f);
+            if (ENERGY && role == 0) ea.e[sl] += (double)en;
+        }
+    }
+    return fb;
 }
 
 // Bounding box of cluster I from the FP32 positions (warp-wide).
@@ -235,11 +313,26 @@ __device__ __forceinline__ void cluster_bbox(int I, int n, const float4* sx, flo
     }
 }
 
-__device__ __forceinline__ bool bbox_close(float4 ci, float4 hi, float4 cj, float4 hj, float cut2) {
-    const float gx = fmaxf(0.f, fabsf(cj.x - ci.x) - hi.x - hj.x);
-    const float gy = fmaxf(0.f, fabsf(cj.y - ci.y) - hi.y - hj.y);
-    const float gz = fmaxf(0.f, fabsf(cj.z - ci.z) - hi.z - hj.z);
-    return gx * gx + gy * gy + gz * gz < cut2;
+// Exclusion bits of (i, j) for the j of an increasing walk: ep / ej track
+// the position in bead i's exclusion row (j | bits << 24, j increasing).
+__device__ __forceinline__ uint32_t excl_walk(int j, int& ep, int& ej, int e1, const int32_t* __restrict__ ex) {
+    while (ej < j) {
+        ++ep;
+        ej = ep < e1 ? (ex[ep] & 0xFFFFFF) : 0x7FFFFFFF;
+    }
+    return ej == j ? ((uint32_t)ex[ep] >> 24) : 0u;
+}
+
+template <bool LABELS>
+__device__ __forceinline__ uint32_t label_bits(uint32_t labi, uint32_t labj, const PairConsts& pc) {
+    uint32_t bits = 0u;
+    if (LABELS) {
+#pragma unroll
+        for (int term = 0; term < 4; ++term)
+            if ((pc.uses_labels & (1 << term)) && !labels_allow(labi, labj, term, pc.allow[term]))
+                bits |= 1u << term;
+    }
+    return bits;
 }
 
 // Neighbour list of every bead of the claimed system, built by one thread
@@ -284,18 +377,8 @@ __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, i
                 if (j == i) continue;
                 const float r2 = norm2(separation<false>(xi, sx[j], nobox, nobox));
                 if (!(r2 < cut2)) continue;
-                while (ej < j) {
-                    ++ep;
-                    ej = ep < e1 ? (ex[ep] & 0xFFFFFF) : 0x7FFFFFFF;
-                }
-                uint32_t bits = ej == j ? ((uint32_t)ex[ep] >> 24) : 0u;
-                if (LABELS) {
-                    const uint32_t labj = slab[j];
-#pragma unroll
-                    for (int term = 0; term < 4; ++term)
-                        if ((pc.uses_labels & (1 << term)) && !labels_allow(labi, labj, term, pc.allow[term]))
-                            bits |= 1u << term;
-                }
+                uint32_t bits = excl_walk(j, ep, ej, e1, ex);
+                if (LABELS) bits |= label_bits<true>(labi, slab[j], pc);
                 if ((bits & present) == present) continue;
                 while (j >= jb) {
                     sseg[i * S + s_next] = (uint16_t)min(cnt, maxn);
@@ -320,49 +403,131 @@ __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, i
     }
 }
 
-// Pair forces on bead i from list entries [k0, cnt), four entries per
-// iteration so their loads and arithmetic overlap.  One accumulator, in list
-// (= increasing j) order: entries outside the cutoff contribute nothing, so
-// the FP32 sum does not depend on when the list was built.
 template <int TERMS, bool ENERGY>
-__device__ __forceinline__ float3 list_forces(int i, int k0, int cnt, int cap_s, int npad,
+__device__ __forceinline__ void pair_accumulate(int i, int j, float4 xi, float4 xj, float4 p0i, float4 p1i,
+                                                const float4* sp0, const float4* sp1, uint32_t bits,
+                                                const PairConsts& pc, float3& fa, EnergyAcc& ea) {
+    const float3 nobox = make_float3(0.f, 0.f, 0.f);
+    const float3 d = separation<false>(xi, xj, nobox, nobox);
+    const float r2 = norm2(d);
+    if (r2 < pc.list_rc2) {
+        const float4 p0j = sp0[j];
+        const float4 p1j = (TERMS & kTermLJA) ? sp1[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        PairEnergy e;
+        e.zero();
+        const float s = pair_scalar<TERMS, ENERGY>(r2, p0i, p0j, p1i, p1j, bits, pc, e);
+        fa.x -= s * d.x;
+        fa.y -= s * d.y;
+        fa.z -= s * d.z;
+        if (ENERGY) {
+            // every pair is met from both of its beads
+            ea.e[kSlotEXV] += 0.5 * (double)e.exv;
+            ea.e[kSlotDH] += 0.5 * (double)e.dh;
+            ea.e[kSlotLJR] += 0.5 * (double)e.ljr;
+            ea.e[kSlotLJA] += 0.5 * (double)e.lja;
+        }
+    }
+}
+
+// Pair forces of list entries [k0, k1) of bead i in one memory space,
+// four entries per iteration: the entries' loads are issued first, and the
+// cutoff test selects the result instead of branching, so the four pair
+// evaluations interleave.  One accumulator in list (= increasing j) order:
+// entries outside the cutoff contribute exactly zero.
+template <int TERMS, bool ENERGY>
+__device__ __forceinline__ void list_range(int i, int k0, int k1, int npad, const uint16_t* __restrict__ L,
+                                           float4 xi, float4 p0i, float4 p1i, const float4* sx,
+                                           const float4* sp0, const float4* sp1, uint32_t excl_all,
+                                           const PairConsts& pc, float3& fa, EnergyAcc& ea) {
+    const float3 nobox = make_float3(0.f, 0.f, 0.f);
+    for (int k = k0; k < k1; k += 4) {
+        uint32_t ent[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) ent[u] = k + u < k1 ? (uint32_t)L[(size_t)(k + u) * npad + i] : (uint32_t)i;
+        float4 xj[4], p0j[4], p1j[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = (int)(ent[u] & 2047u);
+            xj[u] = sx[j];
+            p0j[u] = sp0[j];
+            p1j[u] = (TERMS & kTermLJA) ? sp1[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float3 d = separation<false>(xi, xj[u], nobox, nobox);
+            const float r2 = norm2(d);
+            const bool in = k + u < k1 && r2 < pc.list_rc2;
+            PairEnergy e;
+            e.zero();
+            float sc = pair_scalar<TERMS, ENERGY>(in ? r2 : pc.list_rc2, p0i, p0j[u], p1i, p1j[u],
+                                                  (ent[u] >> 11) | excl_all, pc, e);
+            sc = in ? sc : 0.f;
+            fa.x -= sc * d.x;
+            fa.y -= sc * d.y;
+            fa.z -= sc * d.z;
+            if (ENERGY && in) {
+                // every pair is met from both of its beads
+                ea.e[kSlotEXV] += 0.5 * (double)e.exv;
+                ea.e[kSlotDH] += 0.5 * (double)e.dh;
+                ea.e[kSlotLJR] += 0.5 * (double)e.ljr;
+                ea.e[kSlotLJA] += 0.5 * (double)e.lja;
+            }
+        }
+    }
+}
+
+// Pair forces on bead i from list entries [k0, k1): the shared-memory part
+// (k < cap_s), then the part in global memory.
+template <int TERMS, bool ENERGY>
+__device__ __forceinline__ float3 list_forces(int i, int k0, int k1, int cap_s, int npad,
                                               const uint16_t* slist,
                                               const uint16_t* __restrict__ glist,
                                               const float4* sx, const float4* sp0,
                                               const float4* sp1, uint32_t excl_all,
-                                              const PairConsts& pc, PairEnergy& e) {
-    const float3 nobox = make_float3(0.f, 0.f, 0.f);
+                                              const PairConsts& pc, EnergyAcc& ea) {
     const float4 xi = sx[i];
     const float4 p0i = sp0[i];
     const float4 p1i = (TERMS & kTermLJA) ? sp1[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     float3 fa = make_float3(0.f, 0.f, 0.f);
-    for (int k = k0; k < cnt; k += 4) {
-        uint32_t ent[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int kk = k + u;
-            ent[u] = kk < cnt ? (kk < cap_s ? (uint32_t)slist[kk * npad + i]
-                                            : (uint32_t)glist[(size_t)kk * npad + i])
-                              : 0xFFFFFFFFu;
-        }
-        float4 xj[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) xj[u] = sx[ent[u] != 0xFFFFFFFFu ? (int)(ent[u] & 2047u) : i];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (ent[u] == 0xFFFFFFFFu) continue;
-            const int j = (int)(ent[u] & 2047u);
-            const float3 d = separation<false>(xi, xj[u], nobox, nobox);
-            const float r2 = norm2(d);
-            if (r2 < pc.list_rc2) {
-                const float4 p0j = sp0[j];
-                const float4 p1j = (TERMS & kTermLJA) ? sp1[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-                const float s = pair_scalar<TERMS, ENERGY>(r2, p0i, p0j, p1i, p1j,
-                                                           (ent[u] >> 11) | excl_all, pc, e);
-                fa.x -= s * d.x;
-                fa.y -= s * d.y;
-                fa.z -= s * d.z;
-            }
+    const int ks = min(k1, cap_s);
+    if (k0 < ks) list_range<TERMS, ENERGY>(i, k0, ks, npad, slist, xi, p0i, p1i, sx, sp0, sp1, excl_all, pc, fa, ea);
+    const int kg = max(k0, cap_s);
+    if (kg < k1) list_range<TERMS, ENERGY>(i, kg, k1, npad, glist, xi, p0i, p1i, sx, sp0, sp1, excl_all, pc, fa, ea);
+    return fa;
+}
+
+// The same sum without a list, for a system whose list overflowed: every
+// j in [j0, j1) in increasing order, the clusters culled by their bounding
+// boxes at the cutoff.  The nonzero contributions and their order are those
+// of the list walk, so the force is bit-identical to it.
+template <int TERMS, bool LABELS, bool ENERGY>
+__device__ __forceinline__ float3 scan_forces(int i, int j0, int j1, int nt, const float4* sx, const float4* sp0,
+                                              const float4* sp1, const uint32_t* slab, const float4* bc,
+                                              const float4* bh, float cull2, const int32_t* __restrict__ ex_start,
+                                              const int32_t* __restrict__ ex, uint32_t excl_all,
+                                              const PairConsts& pc, EnergyAcc& ea) {
+    const float4 xi = sx[i];
+    const float4 p0i = sp0[i];
+    const float4 p1i = (TERMS & kTermLJA) ? sp1[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const uint32_t labi = LABELS ? slab[i] : 0u;
+    const uint32_t present = (uint32_t)pc.terms;
+    int ep = ex_start[i];
+    const int e1 = ex_start[i + 1];
+    int ej = ep < e1 ? (ex[ep] & 0xFFFFFF) : 0x7FFFFFFF;
+    float3 fa = make_float3(0.f, 0.f, 0.f);
+    for (int J = j0 >> 5; J < nt && J * 32 < j1; ++J) {
+        const float4 c = bc[J], h = bh[J];
+        const float gx = fmaxf(0.f, fabsf(xi.x - c.x) - h.x);
+        const float gy = fmaxf(0.f, fabsf(xi.y - c.y) - h.y);
+        const float gz = fmaxf(0.f, fabsf(xi.z - c.z) - h.z);
+        if (gx * gx + gy * gy + gz * gz >= cull2) continue;
+        const int ja = max(j0, J * 32), jz = min(j1, J * 32 + 32);
+        for (int j = ja; j < jz; ++j) {
+            if (j == i) continue;
+            uint32_t bits = excl_walk(j, ep, ej, e1, ex);
+            if (LABELS) bits |= label_bits<true>(labi, slab[j], pc);
+            if ((bits & present) == present) continue;
+            pair_accumulate<TERMS, ENERGY>(i, j, xi, sx[j], p0i, p1i, sp0, sp1, bits | excl_all, pc, fa, ea);
         }
     }
     return fa;
@@ -379,6 +544,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
     __shared__ int s_claim;
     __shared__ int s_move[2];
     __shared__ int s_overflow;
+    __shared__ int s_bad;
     __shared__ double s_energy[kNumSlots];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -390,6 +556,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
             s_move[0] = 0;
             s_move[1] = 0;
             s_overflow = 0;
+            s_bad = 0;
         }
         if (ENERGY && tid < kNumSlots) s_energy[tid] = 0.0;
         __syncthreads();
@@ -397,6 +564,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         if (q >= a.n_order) break;
         const int slot = a.order[q];
         const BatchSys& R = a.sys[slot];
+        if (INTEGRATE && R.status != 0) {  // blew up earlier: not advanced again
+            __syncthreads();  // every thread has read s_claim before it is rewritten
+            continue;
+        }
         const int n = R.n, nt = R.nt, npad = nt * 32;
         const PairConsts pc = R.pc;
         const LangevinConsts lc = R.lc;
@@ -408,9 +579,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         const float* ginvm = reinterpret_cast<const float*>(blob + R.off_invm);
         // ---- shared-memory layout of this system, arrays of stride ns ----
         // Positions are float-float: hi parts in sx (pair arithmetic), lo
-        // parts in sxl; x = hi + lo carries ~48 significant bits.
+        // parts in sxl; x = hi + lo carries ~48 significant bits.  fp / fb:
+        // each bead's pair and bonded force of the current step.
         const int ns = npad;
-        const FixedAcc sF{reinterpret_cast<uint32_t*>(smem), reinterpret_cast<uint32_t*>(smem) + 3 * ns};
+        float* fp = reinterpret_cast<float*>(smem);
+        float* fb = reinterpret_cast<float*>(smem + 12 * (size_t)ns);
         float4* sx = reinterpret_cast<float4*>(smem + 24 * (size_t)ns);
         float4* sp0 = reinterpret_cast<float4*>(smem + 40 * (size_t)ns);
         float* sxl = reinterpret_cast<float*>(smem + 56 * (size_t)ns);
@@ -429,6 +602,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         float4* bc = reinterpret_cast<float4*>(smem + off);
         float4* bh = bc + nt;
         off += 32 * (size_t)nt;
+        float3* carry = reinterpret_cast<float3*>(smem + off);
+        off += 36 * (size_t)nt;
+        off = (off + 15) & ~(size_t)15;
         uint16_t* sseg = reinterpret_cast<uint16_t*>(smem + off);
         off += 2 * kMaxUnits;
         // bonded records and tables: staged in shared memory when they fit,
@@ -438,25 +614,28 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         unsigned char* sbonded = smem + off;
         if (bonded_smem) off += (size_t)R.bonded_bytes;
         const unsigned char* bsrc = bonded_smem ? sbonded : gbonded;
-        const float4* bpar = reinterpret_cast<const float4*>(bsrc + R.rb_p);
-        const uint32_t* bij = reinterpret_cast<const uint32_t*>(bsrc + R.rb_ij);
-        const uint2* aij = reinterpret_cast<const uint2*>(bsrc + R.ra_ij);
-        const float* ak = reinterpret_cast<const float*>(bsrc + R.ra_k);
-        const uint4* drec = reinterpret_cast<const uint4*>(bsrc + R.rd);
-        const float2* gdp = reinterpret_cast<const float2*>(bsrc + R.rgd);
-        const FlaTable* fla = reinterpret_cast<const FlaTable*>(bsrc + R.rfla);
-        const FldTable* fld = reinterpret_cast<const FldTable*>(bsrc + R.rfld);
+        Bonded B;
+        B.bpar = reinterpret_cast<const float4*>(bsrc + R.rb_p);
+        B.bij = reinterpret_cast<const uint32_t*>(bsrc + R.rb_ij);
+        B.aij = reinterpret_cast<const uint2*>(bsrc + R.ra_ij);
+        B.ak = reinterpret_cast<const float*>(bsrc + R.ra_k);
+        B.drec = reinterpret_cast<const uint4*>(bsrc + R.rd);
+        B.gdp = reinterpret_cast<const float2*>(bsrc + R.rgd);
+        B.fla = reinterpret_cast<const FlaTable*>(bsrc + R.rfla);
+        B.fld = reinterpret_cast<const FldTable*>(bsrc + R.rfld);
+        B.cb = reinterpret_cast<const uint16_t*>(bsrc + R.rcb);
+        B.ca = reinterpret_cast<const uint16_t*>(bsrc + R.rca);
+        B.cd = reinterpret_cast<const uint16_t*>(bsrc + R.rcd);
+        B.gs = reinterpret_cast<const uint16_t*>(bsrc + R.rgs);
+        B.gl = reinterpret_cast<const uint32_t*>(bsrc + R.rgl);
         uint16_t* slist = reinterpret_cast<uint16_t*>(smem + off);
         const size_t list_bytes = a.smem_bytes > off ? a.smem_bytes - off : 0;
-        const int32_t* tmask = reinterpret_cast<const int32_t*>(blob + R.off_tmask);
-        const uint32_t* masks = reinterpret_cast<const uint32_t*>(blob + R.off_masks);
         const int32_t* ex_start = reinterpret_cast<const int32_t*>(blob + R.off_ex_start);
         const int32_t* exl = reinterpret_cast<const int32_t*>(blob + R.off_ex);
         uint16_t* glist = a.lists + R.list_off;
         const int maxn = R.maxn;
         // entries per bead kept in shared memory (multiple of 4)
         const int cap_s = min(maxn, (int)(list_bytes / (2 * (size_t)npad)) & ~3);
-        const int n_bonds = R.n_bonds, n_angles = R.n_angles, n_dih = R.n_dih;
         const int S = pair_split(n);
         const unsigned long long step0 = R.steps_done;
         int K = 1;
@@ -474,9 +653,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
 
         // ---- load ----
         for (int b = tid; b < npad; b += THREADS) {
-            facc_zero(sF, b);
-            facc_zero(sF, ns + b);
-            facc_zero(sF, 2 * ns + b);
             if (b < n) {
                 const double px = a.x[boff + b], py = a.y[boff + b], pz = a.z[boff + b];
                 const float hx = __double2float_rn(px), hy = __double2float_rn(py),
@@ -513,185 +689,104 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         for (int I = warp; I < nt; I += NW) cluster_bbox(I, n, sx, bc, bh, lane);
         __syncthreads();
 
-        // list cutoff = largest pair cutoff + skin; tiles use the cutoff alone
+        // list cutoff = largest pair cutoff + skin; the scan culls at the
+        // cutoff (with a margin for the FP32 box arithmetic)
         const float rc = sqrtf(pc.list_rc2);
         const float lcut = (rc + R.skin) * 1.0001f;
         const float lcut2 = lcut * lcut;
         const float tcut = rc * 1.0001f + 1e-4f;
         const float tcut2 = tcut * tcut;
         const float half_skin2 = 0.25f * R.skin * R.skin;
-        bool use_tiles = false;
+        bool use_scan = false;
         bool need_build = pairs_on;
         int builds = 0;
-        float eacc[kNumSlots];
-#pragma unroll
-        for (int k = 0; k < kNumSlots; ++k) eacc[k] = 0.f;
+        int st_done = 0;
+        EnergyAcc ea;
+        if (ENERGY) ea.zero();
 
         for (int st = 0; st < K; ++st) {
-            if (need_build && !use_tiles) {
+            if (need_build && !use_scan) {
                 build_lists<LABELS>(n, nt, npad, maxn, cap_s, lcut2, sx, slab, bc, bh, ex_start, exl,
                                     pc, slist, glist, scnt, sref, ns, tid, THREADS, S, sseg,
                                     &s_overflow);
                 ++builds;
                 __syncthreads();
-                use_tiles = s_overflow != 0;
+                use_scan = s_overflow != 0;
             }
             const unsigned long long step = step0 + (unsigned long long)st;
-            // Langevin noise for this thread's beads, drawn before the force
-            // work so its latency overlaps the pair loop.
-            float3 noise[BPT];
-            if (INTEGRATE) {
-#pragma unroll
-                for (int c = 0; c < BPT; ++c) {
-                    const int b = tid + c * THREADS;
-                    noise[c] = b < n ? gaussian3(lc.seed, lc.stream, (uint32_t)b, step, kPurposeLangevin)
-                                     : make_float3(0.f, 0.f, 0.f);
-                }
-            }
-            // ---- pair terms ----
-            if (pairs_on && !use_tiles && S > 1) {
-                // (bead, j-range) units u = i * S + s, 32 per warp; the S
-                // partial sums of a bead meet in a fixed butterfly
+            // ---- pair terms: (bead, j-range) units u = i * S + s, 32 per
+            // warp; the S partial sums of a bead meet in a fixed butterfly
+            // and its first sub-lane stores the bead's pair force ----
+            if (pairs_on) {
                 for (int base = warp * 32; base < n * S; base += THREADS) {
                     const int u = base + lane;
                     const int i = u / S, sr = u & (S - 1);
                     float3 fi = make_float3(0.f, 0.f, 0.f);
-                    PairEnergy e;
-                    e.zero();
                     if (i < n) {
-                        const int k0 = sseg[u];
-                        const int k1 = sr == S - 1 ? (int)scnt[i] : (int)sseg[u + 1];
-                        fi = list_forces<TERMS, ENERGY>(i, k0, k1, cap_s, npad, slist, glist, sx, sp0,
-                                                        sp1, excl_all, pc, e);
+                        if (!use_scan) {
+                            const int k0 = S > 1 ? (int)sseg[u] : 0;
+                            const int k1 = sr == S - 1 ? (int)scnt[i] : (int)sseg[u + 1];
+                            fi = list_forces<TERMS, ENERGY>(i, k0, k1, cap_s, npad, slist, glist, sx, sp0, sp1,
+                                                            excl_all, pc, ea);
+                        } else {
+                            const int j0 = (sr * n) / S, j1 = sr == S - 1 ? n : ((sr + 1) * n) / S;
+                            fi = scan_forces<TERMS, LABELS, ENERGY>(i, j0, j1, nt, sx, sp0, sp1, slab, bc, bh,
+                                                                    tcut2, ex_start, exl, excl_all, pc, ea);
+                        }
                     }
                     for (int o = 1; o < S; o <<= 1) {
                         fi.x += __shfl_xor_sync(kFull, fi.x, o);
                         fi.y += __shfl_xor_sync(kFull, fi.y, o);
                         fi.z += __shfl_xor_sync(kFull, fi.z, o);
                     }
-                    if (i < n && sr == 0) sadd(sF, ns, i, fi);
-                    if (ENERGY) {
-                        eacc[kSlotEXV] += 0.5f * e.exv;
-                        eacc[kSlotDH] += 0.5f * e.dh;
-                        eacc[kSlotLJR] += 0.5f * e.ljr;
-                        eacc[kSlotLJA] += 0.5f * e.lja;
+                    if (i < n && sr == 0) {
+                        fp[i] = fi.x;
+                        fp[ns + i] = fi.y;
+                        fp[2 * ns + i] = fi.z;
                     }
-                }
-            } else if (pairs_on && !use_tiles) {
-#pragma unroll
-                for (int c = 0; c < BPT; ++c) {
-                    const int i = tid + c * THREADS;
-                    if (i >= n) break;
-                    PairEnergy e;
-                    e.zero();
-                    const float3 fi = list_forces<TERMS, ENERGY>(i, 0, scnt[i], cap_s, npad, slist, glist,
-                                                                 sx, sp0, sp1, excl_all, pc, e);
-                    sadd(sF, ns, i, fi);
-                    if (ENERGY) {
-                        // every pair appears in both lists
-                        eacc[kSlotEXV] += 0.5f * e.exv;
-                        eacc[kSlotDH] += 0.5f * e.dh;
-                        eacc[kSlotLJR] += 0.5f * e.ljr;
-                        eacc[kSlotLJA] += 0.5f * e.lja;
-                    }
-                }
-            } else if (pairs_on) {
-                for (int t = warp; t < R.n_tiles; t += NW) {
-                    int J = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
-                    while ((J + 1) * (J + 2) / 2 <= t) ++J;
-                    while (J * (J + 1) / 2 > t) --J;
-                    const int I = t - J * (J + 1) / 2;
-                    if (!bbox_close(bc[I], bh[I], bc[J], bh[J], tcut2)) continue;
-                    batch_tile<TERMS, LABELS, ENERGY>(I, J, tmask[t], masks, sx, sp0, sp1, slab, sF,
-                                                      ns, pc, excl_all, lane, eacc);
                 }
             }
-            // ---- bonded: one flattened loop over dihedrals | angles |
-            // bonds, so the costliest terms spread over all threads ----
-            {
-                const int n_ad = n_dih + n_angles, n_all = n_ad + n_bonds;
-                const bool fld_on = (slots_en & (1u << kSlotFLD)) != 0;
-                const bool fla_on = (slots_en & (1u << kSlotFLA)) != 0;
-                const bool gd_on = (slots_en & (1u << kSlotGD)) != 0;
-                for (int t = tid; t < n_all; t += THREADS) {
-                    if (t < n_dih) {
-                        const uint4 qd = drec[t];
-                        const bool gauss = (qd.x >> 31) != 0;
-                        if (!(gauss ? gd_on : fld_on)) continue;
-                        const int qi = qd.x & 0xFFFF, qj = (qd.x >> 16) & 0x7FFF, qk = qd.y & 0xFFFF,
-                                  ql = qd.y >> 16;
-                        const float3 F = ffsep(sx, sxl, ns, qj, qi);
-                        const float3 G = ffsep(sx, sxl, ns, qk, qj);
-                        const float3 H = ffsep(sx, sxl, ns, qk, ql);
-                        float3 f1, f2, f3, f4;
-                        float en;
-                        if (gauss) {
-                            const float2 gp = gdp[qd.z];
-                            gauss_dihedral_forces(F, G, H, __uint_as_float(qd.w), gp.x, gp.y, f1, f2, f3, f4,
-                                                  en);
-                        } else {
-                            fld_forces(F, G, H, __uint_as_float(qd.w), fld[qd.z], f1, f2, f3, f4, en);
-                        }
-                        sadd(sF, ns, qi, f1);
-                        sadd(sF, ns, qj, f2);
-                        sadd(sF, ns, qk, f3);
-                        sadd(sF, ns, ql, f4);
-                        if (ENERGY) eacc[gauss ? kSlotGD : kSlotFLD] += en;
-                    } else if (t < n_ad) {
-                        if (!fla_on) continue;
-                        const int b = t - n_dih;
-                        const uint2 g = aij[b];
-                        const int gi = g.x & 0xFFFF, gj = g.x >> 16, gk = g.y & 0xFFFF;
-                        const float3 u = ffsep(sx, sxl, ns, gj, gi);
-                        const float3 v = ffsep(sx, sxl, ns, gj, gk);
-                        float3 f1, f3;
-                        float en;
-                        fla_forces(u, v, ak[b], fla[g.y >> 16], f1, f3, en);
-                        sadd(sF, ns, gi, f1);
-                        sadd(sF, ns, gk, f3);
-                        sadd(sF, ns, gj, make_float3(-f1.x - f3.x, -f1.y - f3.y, -f1.z - f3.z));
-                        if (ENERGY) eacc[kSlotFLA] += en;
-                    } else {
-                        const int b = t - n_ad;
-                        const uint32_t ij = bij[b];
-                        const int kind = (int)(ij >> 30);
-                        const int sl = bond_slot(kind);
-                        if (!(slots_en & (1u << sl))) continue;
-                        const int bi = ij & 0xFFFF, bj = (ij >> 16) & 0x3FFF;
-                        const float4 bp = bpar[b];
-                        float3 dh, dl;
-                        ff_sep(sx[bi], lo3(sxl, ns, bi), sx[bj], lo3(sxl, ns, bj), dh, dl);
-                        const float3 d = make_float3(dh.x + dl.x, dh.y + dl.y, dh.z + dl.z);
-                        const float delta = ff_bond_delta(dh, dl, bp.z, bp.w);
-                        float en;
-                        const float sc = bond_scalar(kind, norm2(d), delta, bp.x, bp.y, bp.z, en);
-                        sadd(sF, ns, bi, make_float3(-sc * d.x, -sc * d.y, -sc * d.z));
-                        sadd(sF, ns, bj, make_float3(sc * d.x, sc * d.y, sc * d.z));
-                        if (ENERGY) eacc[sl] += en;
-                    }
+            // ---- bonded: one warp per cluster of 32 chain positions,
+            // started from the far end of the warp range so warps that ran
+            // few pair units take the bonded work ----
+            for (int I = NW - 1 - warp; I < nt; I += NW) {
+                const float3 f = bonded_cluster<ENERGY>(B, I, n, lane, sx, sxl, ns, slots_en, carry, ea);
+                const int b = I * 32 + lane;
+                if (b < n) {
+                    fb[b] = f.x;
+                    fb[ns + b] = f.y;
+                    fb[2 * ns + b] = f.z;
                 }
             }
             __syncthreads();
             if (!INTEGRATE) break;
-            // ---- Langevin update, bounding boxes, displacement check ----
-            // Bead b = tid + c * THREADS is cluster b / 32 handled by this warp.
+            // ---- Langevin update, bounding boxes, displacement and
+            // blow-up checks; bead b = I * 32 + lane of cluster I = warp +
+            // c * NW ----
             const int mv = st & 1;
 #pragma unroll
             for (int c = 0; c < BPT; ++c) {
                 const int I = warp + c * NW;
                 if (I >= nt) break;
                 const int b = I * 32 + lane;
-                bool moved = false;
+                bool moved = false, bad = false;
                 if (b < n) {
-                    const float fx = fixed_to_float(facc_get(sF, b));
-                    const float fy = fixed_to_float(facc_get(sF, ns + b));
-                    const float fz = fixed_to_float(facc_get(sF, 2 * ns + b));
-                    facc_zero(sF, b);
-                    facc_zero(sF, ns + b);
-                    facc_zero(sF, 2 * ns + b);
+                    float fx = fb[b], fy = fb[ns + b], fz = fb[2 * ns + b];
+                    if (pairs_on) {
+                        fx = fp[b] + fx;
+                        fy = fp[ns + b] + fy;
+                        fz = fp[2 * ns + b] + fz;
+                    }
+                    if (lane < 3 && I > 0) {
+                        const float3 cin = carry[3 * (I - 1) + lane];
+                        fx += cin.x;
+                        fy += cin.y;
+                        fz += cin.z;
+                    }
+                    bad = !(fabsf(fx) <= kForceLimit && fabsf(fy) <= kForceLimit && fabsf(fz) <= kForceLimit);
                     const float im = sim[b];
                     if (im > 0.f) {
-                        const float3 g = noise[c];
+                        const float3 g = gaussian3(lc.seed, lc.stream, (uint32_t)b, step, kPurposeLangevin);
                         const float sq = sqrtf(im) * lc.noise;
                         const float fs = lc.fscale * im;
                         const float vx = lc.vscale * sv[b] + fs * fx + sq * g.x;
@@ -705,15 +800,19 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                         ff_add(h.y, sxl[ns + b], vy * lc.dt);
                         ff_add(h.z, sxl[2 * ns + b], vz * lc.dt);
                         sx[b] = h;
+                        bad = bad || !(isfinite(h.x) && isfinite(h.y) && isfinite(h.z));
                         const float dx = h.x - sref[b], dy = h.y - sref[ns + b], dz = h.z - sref[2 * ns + b];
                         moved = dx * dx + dy * dy + dz * dz > half_skin2;
                     }
                 }
                 if (__any_sync(kFull, moved) && lane == 0) atomicOr(&s_move[mv], 1);
+                if (__any_sync(kFull, bad) && lane == 0) atomicOr(&s_bad, 1);
                 __syncwarp();
                 cluster_bbox(I, n, sx, bc, bh, lane);
             }
             __syncthreads();
+            st_done = st + 1;
+            if (s_bad) break;  // the system blew up this step: stop advancing it
             need_build = s_move[mv] != 0;
             if (tid == 0) s_move[mv ^ 1] = 0;
         }
@@ -730,22 +829,43 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
                 a.vz[boff + b] = sv[2 * ns + b];
             }
             if (tid == 0) {
-                a.sys[slot].steps_done = step0 + (unsigned long long)K;
+                a.sys[slot].steps_done = step0 + (unsigned long long)st_done;
                 a.sys[slot].builds = builds;
                 if (s_overflow) a.sys[slot].overflow = 1;
+                if (s_bad) a.sys[slot].status = kBatchStatusBlownUp;
             }
         } else {
+            bool bad = false;
             for (int b = tid; b < n; b += THREADS) {
-                a.forces[b] = (unsigned long long)facc_get(sF, b);
-                a.forces[nmax + b] = (unsigned long long)facc_get(sF, ns + b);
-                a.forces[2 * nmax + b] = (unsigned long long)facc_get(sF, 2 * ns + b);
+                float fx = fb[b], fy = fb[ns + b], fz = fb[2 * ns + b];
+                if (pairs_on) {
+                    fx = fp[b] + fx;
+                    fy = fp[ns + b] + fy;
+                    fz = fp[2 * ns + b] + fz;
+                }
+                const int I = b >> 5, l = b & 31;
+                if (l < 3 && I > 0) {
+                    const float3 cin = carry[3 * (I - 1) + l];
+                    fx += cin.x;
+                    fy += cin.y;
+                    fz += cin.z;
+                }
+                bad = bad || !(fabsf(fx) <= kForceLimit && fabsf(fy) <= kForceLimit && fabsf(fz) <= kForceLimit);
+                a.forces[b] = fx;
+                a.forces[nmax + b] = fy;
+                a.forces[2 * nmax + b] = fz;
             }
-            if (tid == 0 && s_overflow) a.sys[slot].overflow = 1;
+            if (bad) atomicOr(&s_bad, 1);
+            __syncthreads();
+            if (tid == 0) {
+                if (s_overflow) a.sys[slot].overflow = 1;
+                a.sys[slot].eval_status = s_bad ? kBatchStatusBlownUp : 0;
+            }
         }
         if (ENERGY) {
 #pragma unroll
             for (int k = 0; k < kNumSlots; ++k) {
-                const double v = warp_sum_d((double)eacc[k]);
+                const double v = warp_sum_d(ea.e[k]);
                 if (lane == 0 && v != 0.0) atomicAdd(&s_energy[k], v);
             }
             __syncthreads();
@@ -820,19 +940,111 @@ void launch_batch_threads(int threads, const BatchArgs& a, int grid, size_t smem
 
 int64_t align_up(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 
-struct BlobLayout {
-    int64_t size = 0;
-    int off_p0, off_p1, off_lab, off_invm, off_tmask, off_masks, off_ex_start, off_ex;
-    int off_bonded, bonded_bytes, rb_p, rb_ij, ra_ij, ra_k, rd, rgd, rfla, rfld;
-    int n_tiles, n_masks;
+// The bonded terms of one system in kernel order.  A term is chain-local
+// when its beads are consecutive chain positions (bond b, b+1; angle b..b+2;
+// dihedral b..b+3, either direction; angles and dihedrals are reversed to
+// increasing order, which leaves the angle and the torsion unchanged).
+// Chain-local terms come first, sorted by their first bead (stable, so
+// terms on the same beads keep their order), with per-bead start indices;
+// every other term is listed in the gather entries of each of its beads
+// (type << 30 | role << 28 | term index).
+struct BondedPlan {
+    std::vector<BondTerm> bonds;
+    std::vector<AngleTerm> angles;
+    std::vector<DihedralTerm> dihedrals;
+    std::vector<uint16_t> cb, ca, cd, gs;  // n + 1 each
+    std::vector<uint32_t> gl;
 };
 
-BlobLayout blob_layout(const CompiledSystem& c, int n_masks) {
+BondedPlan plan_bonded(const CompiledSystem& c) {
+    const int64_t n = c.n;
+    BondedPlan P;
+    std::vector<BondTerm> ob;
+    std::vector<AngleTerm> oa;
+    std::vector<DihedralTerm> od;
+    std::vector<std::pair<int64_t, BondTerm>> chb;
+    std::vector<std::pair<int64_t, AngleTerm>> cha;
+    std::vector<std::pair<int64_t, DihedralTerm>> chd;
+    for (BondTerm t : c.bonds) {
+        if (t.i > t.j) std::swap(t.i, t.j);
+        if (t.j == t.i + 1) chb.emplace_back(t.i, t);
+        else ob.push_back(t);
+    }
+    for (AngleTerm t : c.angles) {
+        if (t.i > t.k) std::swap(t.i, t.k);
+        if (t.j == t.i + 1 && t.k == t.i + 2) cha.emplace_back(t.i, t);
+        else oa.push_back(t);
+    }
+    for (DihedralTerm t : c.dihedrals) {
+        if (t.i == t.j + 1 && t.j == t.k + 1 && t.k == t.l + 1) {
+            std::swap(t.i, t.l);
+            std::swap(t.j, t.k);
+        }
+        if (t.j == t.i + 1 && t.k == t.i + 2 && t.l == t.i + 3) chd.emplace_back(t.i, t);
+        else od.push_back(t);
+    }
+    auto by_start = [](const auto& a, const auto& b) { return a.first < b.first; };
+    std::stable_sort(chb.begin(), chb.end(), by_start);
+    std::stable_sort(cha.begin(), cha.end(), by_start);
+    std::stable_sort(chd.begin(), chd.end(), by_start);
+    auto starts = [n](const auto& v) {
+        std::vector<uint16_t> s(n + 1, 0);
+        std::vector<int64_t> cnt(n + 1, 0);
+        for (const auto& e : v) ++cnt[e.first + 1];
+        for (int64_t b = 0; b < n; ++b) cnt[b + 1] += cnt[b];
+        for (int64_t b = 0; b <= n; ++b) s[b] = (uint16_t)cnt[b];
+        return s;
+    };
+    P.cb = starts(chb);
+    P.ca = starts(cha);
+    P.cd = starts(chd);
+    for (auto& e : chb) P.bonds.push_back(e.second);
+    for (auto& e : cha) P.angles.push_back(e.second);
+    for (auto& e : chd) P.dihedrals.push_back(e.second);
+    std::vector<std::vector<uint32_t>> g(n);
+    auto entry = [](uint32_t type, uint32_t role, size_t idx) { return type << 30 | role << 28 | (uint32_t)idx; };
+    for (const BondTerm& t : ob) {
+        const size_t k = P.bonds.size();
+        P.bonds.push_back(t);
+        g[t.i].push_back(entry(0, 0, k));
+        g[t.j].push_back(entry(0, 1, k));
+    }
+    for (const AngleTerm& t : oa) {
+        const size_t k = P.angles.size();
+        P.angles.push_back(t);
+        g[t.i].push_back(entry(1, 0, k));
+        g[t.j].push_back(entry(1, 1, k));
+        g[t.k].push_back(entry(1, 2, k));
+    }
+    for (const DihedralTerm& t : od) {
+        const size_t k = P.dihedrals.size();
+        P.dihedrals.push_back(t);
+        g[t.i].push_back(entry(2, 0, k));
+        g[t.j].push_back(entry(2, 1, k));
+        g[t.k].push_back(entry(2, 2, k));
+        g[t.l].push_back(entry(2, 3, k));
+    }
+    P.gs.assign(n + 1, 0);
+    for (int64_t b = 0; b < n; ++b) {
+        P.gl.insert(P.gl.end(), g[b].begin(), g[b].end());
+        if (P.gl.size() > 0xFFFF) throw Error(6, "[error] too many bonded terms per system for the batched path");
+        P.gs[b + 1] = (uint16_t)P.gl.size();
+    }
+    if (P.bonds.size() > 0xFFFF || P.angles.size() > 0xFFFF || P.dihedrals.size() > 0xFFFF)
+        throw Error(6, "[error] too many bonded terms per system for the batched path");
+    return P;
+}
+
+struct BlobLayout {
+    int64_t size = 0;
+    int off_p0, off_p1, off_lab, off_invm, off_ex_start, off_ex;
+    int off_bonded, bonded_bytes, rb_p, rb_ij, ra_ij, ra_k, rd, rgd, rfla, rfld;
+    int rcb, rca, rcd, rgs, rgl;
+};
+
+BlobLayout blob_layout(const CompiledSystem& c, const BondedPlan& P) {
     BlobLayout L{};
     const int64_t n = c.n;
-    const int nt = (int)((n + 31) / 32);
-    L.n_tiles = nt * (nt + 1) / 2;
-    L.n_masks = n_masks;
     int64_t o = 0;
     auto take = [&](int64_t bytes) {
         const int64_t at = o;
@@ -844,53 +1056,32 @@ BlobLayout blob_layout(const CompiledSystem& c, int n_masks) {
     L.off_lab = take(4 * n);
     L.off_invm = take(4 * n);
     // bonded region: bond params (float4) | bond indices (u32) | angle
-    // indices (uint2) | angle k (f32) | dihedral records (uint4) | FLA | FLD
+    // indices (uint2) | angle k (f32) | dihedral records (uint4) | Gaussian
+    // dihedral parameters | FLA | FLD | chain starts (3 x u16) | gather
+    // starts (u16) | gather entries (u32)
     L.off_bonded = (int)o;
-    const int64_t nb = (int64_t)c.bonds.size(), na = (int64_t)c.angles.size(),
-                  nd = (int64_t)c.dihedrals.size();
+    const int64_t nb = (int64_t)P.bonds.size(), na = (int64_t)P.angles.size(),
+                  nd = (int64_t)P.dihedrals.size();
     L.rb_p = take(16 * nb) - L.off_bonded;
     L.rb_ij = take(4 * nb) - L.off_bonded;
     L.ra_ij = take(8 * na) - L.off_bonded;
     L.ra_k = take(4 * na) - L.off_bonded;
     L.rd = take(16 * nd) - L.off_bonded;
     int64_t ngd = 0;
-    for (const auto& t : c.dihedrals) ngd += t.kind == kDihGauss ? 1 : 0;
+    for (const auto& t : P.dihedrals) ngd += t.kind == kDihGauss ? 1 : 0;
     L.rgd = take(8 * ngd) - L.off_bonded;
     L.rfla = take((int64_t)sizeof(FlaTable) * c.fla.size()) - L.off_bonded;
     L.rfld = take((int64_t)sizeof(FldTable) * c.fld.size()) - L.off_bonded;
+    L.rcb = take(2 * (n + 1)) - L.off_bonded;
+    L.rca = take(2 * (n + 1)) - L.off_bonded;
+    L.rcd = take(2 * (n + 1)) - L.off_bonded;
+    L.rgs = take(2 * (n + 1)) - L.off_bonded;
+    L.rgl = take(4 * (int64_t)P.gl.size()) - L.off_bonded;
     L.bonded_bytes = (int)(o - L.off_bonded);
-    L.off_tmask = take(4 * (int64_t)L.n_tiles);
-    L.off_masks = take(4 * 128 * (int64_t)n_masks);
     L.off_ex_start = take(4 * (n + 1));
     L.off_ex = take(4 * (int64_t)c.ex_j.size());
     L.size = align_up(o, 256);
     return L;
-}
-
-// Exclusion masks in chain order: tile index t = J(J+1)/2 + I (I <= J).
-void build_masks(const CompiledSystem& c, std::vector<int32_t>& tmask, std::vector<uint32_t>& masks) {
-    const int nt = (int)((c.n + 31) / 32);
-    tmask.assign(nt * (nt + 1) / 2, -1);
-    masks.clear();
-    for (int64_t i = 0; i < c.n; ++i) {
-        for (int32_t e = c.ex_start[i]; e < c.ex_start[i + 1]; ++e) {
-            const int64_t j = c.ex_j[e];
-            if (j <= i) continue;
-            const int I = (int)(i >> 5), J = (int)(j >> 5);
-            const int t = J * (J + 1) / 2 + I;
-            if (tmask[t] < 0) {
-                tmask[t] = (int32_t)(masks.size() / 128);
-                masks.resize(masks.size() + 128, 0u);
-            }
-            uint32_t* w = &masks[(size_t)tmask[t] * 128];
-            const int li = (int)(i & 31), lj = (int)(j & 31);
-            for (int term = 0; term < kNumPairTerms; ++term) {
-                if (!(c.ex_bits[e] & (1 << term))) continue;
-                w[term * 32 + li] |= 1u << ((lj - li) & 31);
-                if (I == J) w[term * 32 + lj] |= 1u << ((li - lj) & 31);
-            }
-        }
-    }
 }
 
 constexpr float kBatchSkin = 0.3f;  // nm
@@ -1000,6 +1191,8 @@ BatchEngine::BatchEngine(int device, int64_t max_systems, int64_t max_beads, int
     lists_.alloc(list_cap);
     OCM_CK(cudaMallocHost(&h_overflow_, sizeof(int) * max_systems));
     std::memset(h_overflow_, 0, sizeof(int) * max_systems);
+    OCM_CK(cudaMallocHost(&h_status_, sizeof(int) * max_systems));
+    std::memset(h_status_, 0, sizeof(int) * max_systems);
     sys_.alloc(max_systems);
     OCM_CK(cudaMemset(sys_.p, 0, sizeof(BatchSys) * max_systems));
     order_.alloc(max_systems);
@@ -1016,20 +1209,21 @@ BatchEngine::~BatchEngine() {
     if (ev1_) cudaEventDestroy(ev1_);
     if (ev_copy_) cudaEventDestroy(ev_copy_);
     if (h_overflow_) cudaFreeHost(h_overflow_);
+    if (h_status_) cudaFreeHost(h_status_);
     if (stream_) cudaStreamDestroy(stream_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
 }
 
+// Shared memory of the per-system state: 98 B per bead (118 with the
+// general pair terms), cluster boxes and carries, the pair-split offsets.
 size_t BatchEngine::smem_bytes(int nmax, bool general) const {
-    return (size_t)nmax * (general ? 118 : 98) + 2 * kMaxClusters * sizeof(float4) + 2 * kMaxUnits;
+    return (size_t)nmax * (general ? 118 : 98) + (32 + 36) * (size_t)kMaxClusters + 16 + 2 * kMaxUnits;
 }
 
 int64_t BatchEngine::footprint(const SystemDesc& d) {
     CompiledSystem c = compile_system(d);
-    std::vector<int32_t> tm;
-    std::vector<uint32_t> mk;
-    build_masks(c, tm, mk);
-    const BlobLayout L = blob_layout(c, (int)(mk.size() / 128));
+    const BondedPlan P = plan_bonded(c);
+    const BlobLayout L = blob_layout(c, P);
     return L.size + c.n * (3 * 8 + 3 * 4) + (int64_t)sizeof(BatchSys);
 }
 
@@ -1045,9 +1239,11 @@ void BatchEngine::set_threads(int threads) {
 }
 
 int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double* vel, double T,
-                           double friction, double dt, int32_t seed, int64_t n_steps) {
+                           double friction, double dt, int32_t seed, int64_t n_steps, int64_t steps_done) {
     OCM_CK(cudaSetDevice(device_));
     if (n_steps < 0) throw Error(1, "[error] negative step count");
+    if (steps_done < 0 || steps_done > n_steps)
+        throw Error(1, "[error] steps already done must lie in [0, step count]");
     if (!(dt > 0) || !(friction >= 0) || !(T >= 0)) throw Error(1, "[error] invalid integrator parameters");
     CompiledSystem c = compile_system(d);
     check_batchable(c, nmax_);
@@ -1061,10 +1257,8 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
             break;
         }
     if (slot < 0) throw Error(3, "[error] no free slot in the batch");
-    std::vector<int32_t> tmask;
-    std::vector<uint32_t> masks;
-    build_masks(c, tmask, masks);
-    const BlobLayout L = blob_layout(c, (int)(masks.size() / 128));
+    const BondedPlan P = plan_bonded(c);
+    const BlobLayout L = blob_layout(c, P);
     const int npad = (int)align_up(n, 32);
     const int maxn = initial_list_capacity(c, pos);
     const int64_t boff = beads_.alloc(n, 1);
@@ -1092,26 +1286,26 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     put(L.off_invm, c.inv_mass.data(), 4 * n);
     {
         // compact bonded records (bead indices < 2048 fit 16 bits)
-        std::vector<float4> bp(c.bonds.size());
-        std::vector<uint32_t> bij(c.bonds.size());
-        for (size_t b = 0; b < c.bonds.size(); ++b) {
-            const BondTerm& t = c.bonds[b];
+        std::vector<float4> bp(P.bonds.size());
+        std::vector<uint32_t> bij(P.bonds.size());
+        for (size_t b = 0; b < P.bonds.size(); ++b) {
+            const BondTerm& t = P.bonds[b];
             bp[b] = make_float4(t.p0, t.p1, t.r0sq_hi, t.r0sq_lo);
             bij[b] = (uint32_t)t.i | ((uint32_t)t.j << 16) | ((uint32_t)t.kind << 30);
         }
-        std::vector<uint2> aij(c.angles.size());
-        std::vector<float> ak(c.angles.size());
-        for (size_t b = 0; b < c.angles.size(); ++b) {
-            const AngleTerm& t = c.angles[b];
+        std::vector<uint2> aij(P.angles.size());
+        std::vector<float> ak(P.angles.size());
+        for (size_t b = 0; b < P.angles.size(); ++b) {
+            const AngleTerm& t = P.angles[b];
             aij[b] = make_uint2((uint32_t)t.i | ((uint32_t)t.j << 16), (uint32_t)t.k | ((uint32_t)t.table << 16));
             ak[b] = t.kk;
         }
         // dihedral record: FLD table index, or (bit 31 of .x set) the index
         // of the Gaussian dihedral's (theta0, 1 / (2 sigma^2))
-        std::vector<uint4> dr(c.dihedrals.size());
+        std::vector<uint4> dr(P.dihedrals.size());
         std::vector<float2> gd;
-        for (size_t b = 0; b < c.dihedrals.size(); ++b) {
-            const DihedralTerm& t = c.dihedrals[b];
+        for (size_t b = 0; b < P.dihedrals.size(); ++b) {
+            const DihedralTerm& t = P.dihedrals[b];
             uint32_t kb;
             std::memcpy(&kb, &t.kk, 4);
             const bool gauss = t.kind == kDihGauss;
@@ -1132,9 +1326,12 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
         put(ob + L.rgd, gd.data(), 8 * gd.size());
         put(ob + L.rfla, c.fla.data(), sizeof(FlaTable) * c.fla.size());
         put(ob + L.rfld, c.fld.data(), sizeof(FldTable) * c.fld.size());
+        put(ob + L.rcb, P.cb.data(), 2 * P.cb.size());
+        put(ob + L.rca, P.ca.data(), 2 * P.ca.size());
+        put(ob + L.rcd, P.cd.data(), 2 * P.cd.size());
+        put(ob + L.rgs, P.gs.data(), 2 * P.gs.size());
+        put(ob + L.rgl, P.gl.data(), 4 * P.gl.size());
     }
-    put(L.off_tmask, tmask.data(), 4 * tmask.size());
-    put(L.off_masks, masks.data(), 4 * masks.size());
     {
         std::vector<int32_t> ex(c.ex_j.size());
         for (size_t e = 0; e < ex.size(); ++e) ex[e] = c.ex_j[e] | ((int32_t)c.ex_bits[e] << 24);
@@ -1147,16 +1344,14 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     R.blob_off = blob_off;
     R.n = (int)n;
     R.nt = (int)((n + 31) / 32);
-    R.n_tiles = L.n_tiles;
-    R.n_bonds = (int)c.bonds.size();
-    R.n_angles = (int)c.angles.size();
-    R.n_dih = (int)c.dihedrals.size();
-    R.n_masks = L.n_masks;
+    R.n_bonds = (int)P.bonds.size();
+    R.n_angles = (int)P.angles.size();
+    R.n_dih = (int)P.dihedrals.size();
     R.off_p0 = L.off_p0; R.off_p1 = L.off_p1; R.off_lab = L.off_lab; R.off_invm = L.off_invm;
     R.off_bonded = L.off_bonded; R.bonded_bytes = L.bonded_bytes;
     R.rb_p = L.rb_p; R.rb_ij = L.rb_ij; R.ra_ij = L.ra_ij; R.ra_k = L.ra_k; R.rd = L.rd; R.rgd = L.rgd;
     R.rfla = L.rfla; R.rfld = L.rfld;
-    R.off_tmask = L.off_tmask; R.off_masks = L.off_masks;
+    R.rcb = L.rcb; R.rca = L.rca; R.rcd = L.rcd; R.rgs = L.rgs; R.rgl = L.rgl;
     R.off_ex_start = L.off_ex_start; R.off_ex = L.off_ex;
     R.skin = kBatchSkin;
     R.maxn = maxn;
@@ -1172,7 +1367,7 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     R.lc.dt = (float)dt;
     R.lc.seed = (uint32_t)seed;
     R.lc.stream = 0u;
-    R.steps_done = 0;
+    R.steps_done = (unsigned long long)steps_done;
     R.steps_target = (unsigned long long)n_steps;
 
     std::vector<double> px(n), py(n), pz(n);
@@ -1215,7 +1410,7 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
     S.blob_off = blob_off;
     S.blob_size = L.size;
     S.steps_target = (uint64_t)n_steps;
-    S.steps_done = 0;
+    S.steps_done = (uint64_t)steps_done;
     S.list_off = list_off;
     S.list_size = list_size;
     S.maxn = maxn;
@@ -1274,17 +1469,21 @@ void BatchEngine::launch(bool integrate, bool energy, int k, const std::vector<i
 void BatchEngine::run(int32_t k, bool sync) {
     OCM_CK(cudaSetDevice(device_));
     if (k <= 0) throw Error(1, "[error] steps per launch must be positive");
+    // settle the previous launch first: list growth and systems that blew up
+    grow_lists();
     std::vector<int32_t> order;
     for (int64_t s = 0; s < max_systems_; ++s)
-        if (slots_[s].used && slots_[s].steps_done < slots_[s].steps_target) order.push_back((int32_t)s);
+        if (slots_[s].used && !slots_[s].failed && slots_[s].steps_done < slots_[s].steps_target)
+            order.push_back((int32_t)s);
     std::stable_sort(order.begin(), order.end(),
                      [&](int32_t a, int32_t b) { return slots_[a].cost > slots_[b].cost; });
-    grow_lists();
     OCM_CK(cudaStreamWaitEvent(stream_, ev_copy_, 0));
     OCM_CK(cudaEventRecord(ev0_, stream_));
     if (!order.empty()) launch(true, false, k, order, stream_);
     OCM_CK(cudaEventRecord(ev1_, stream_));
     OCM_CK(cudaMemcpy2DAsync(h_overflow_, sizeof(int), &sys_.p[0].overflow, sizeof(BatchSys),
+                             sizeof(int), max_systems_, cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaMemcpy2DAsync(h_status_, sizeof(int), &sys_.p[0].status, sizeof(BatchSys),
                              sizeof(int), max_systems_, cudaMemcpyDeviceToHost, stream_));
     ran_ = true;
     for (int32_t q : order)
@@ -1301,13 +1500,33 @@ double BatchEngine::last_run_ms() {
     return ms;
 }
 
-void BatchEngine::sync_steps() { OCM_CK(cudaStreamSynchronize(stream_)); }
+// Waits for the last launch and takes note of systems that blew up in it:
+// they stopped at the failing step, so their step counters come from the
+// device, and they are not launched again.
+void BatchEngine::sync_steps() {
+    OCM_CK(cudaStreamSynchronize(stream_));
+    if (!ran_) return;
+    for (int64_t s = 0; s < max_systems_; ++s) {
+        if (!slots_[s].used || slots_[s].failed || h_status_[s] == 0) continue;
+        slots_[s].failed = true;
+        unsigned long long done = 0;
+        OCM_CK(cudaMemcpy(&done, &sys_.p[s].steps_done, sizeof(done), cudaMemcpyDeviceToHost));
+        slots_[s].steps_done = done;
+    }
+}
+
+int32_t BatchEngine::slot_status(int64_t slot) {
+    OCM_CK(cudaSetDevice(device_));
+    if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
+    sync_steps();
+    return slots_[slot].failed ? 7 : 0;
+}
 
 // A list that overflowed made its system fall back to the tile sweep for
 // the rest of that chunk (same results, more work); give it more room now.
 void BatchEngine::grow_lists() {
     if (!ran_) return;
-    OCM_CK(cudaStreamSynchronize(stream_));
+    sync_steps();
     for (int64_t s = 0; s < max_systems_; ++s) {
         if (!h_overflow_[s] || !slots_[s].used) continue;
         h_overflow_[s] = 0;
@@ -1343,7 +1562,7 @@ void BatchEngine::finished(int64_t* out, int64_t cap, int64_t* n_out) {
     sync_steps();
     int64_t c = 0;
     for (int64_t s = 0; s < max_systems_; ++s) {
-        if (!slots_[s].used || slots_[s].steps_done < slots_[s].steps_target) continue;
+        if (!slots_[s].used || (!slots_[s].failed && slots_[s].steps_done < slots_[s].steps_target)) continue;
         if (out && c < cap) out[c] = s;
         ++c;
     }
@@ -1417,21 +1636,23 @@ void BatchEngine::get_state(int64_t slot, uint32_t groups, double* forces, doubl
         else launch_batch_threads<kTermEXV | kTermDH, false>(threads_, a, 1, smem, stream_, false, true, num_sms_,
                                                               want);
     }
-    std::vector<unsigned long long> f(3 * nmax_);
+    std::vector<float> f(3 * nmax_);
     double e[kNumSlots];
-    OCM_CK(cudaMemcpyAsync(f.data(), forces_.p, 3 * nmax_ * sizeof(unsigned long long),
-                           cudaMemcpyDeviceToHost, stream_));
+    int bad = 0;
+    OCM_CK(cudaMemcpyAsync(f.data(), forces_.p, 3 * nmax_ * sizeof(float), cudaMemcpyDeviceToHost, stream_));
     OCM_CK(cudaMemcpyAsync(e, energy_.p + slot * kNumSlots, sizeof(e), cudaMemcpyDeviceToHost, stream_));
+    OCM_CK(cudaMemcpyAsync(&bad, &sys_.p[slot].eval_status, sizeof(int), cudaMemcpyDeviceToHost, stream_));
     OCM_CK(cudaStreamSynchronize(stream_));
     if (forces)
         for (int64_t i = 0; i < S.n; ++i)
-            for (int c = 0; c < 3; ++c)
-                forces[3 * i + c] = (double)(long long)f[(size_t)c * nmax_ + i] * kFixedInv;
+            for (int c = 0; c < 3; ++c) forces[3 * i + c] = (double)f[(size_t)c * nmax_ + i];
     if (energies) {
         for (int g = 0; g < 32; ++g) energies[g] = 0.0;
         for (int k = 0; k < kNumSlots; ++k)
             if (S.slot_group[k] >= 0) energies[S.slot_group[k]] += e[k];
     }
+    if (bad) throw Error(7, "[error] non-finite or out-of-range force (above 1e9 kJ/mol/nm) in slot " +
+                                std::to_string(slot));
 }
 
 void BatchEngine::retire(int64_t slot) {
@@ -1439,6 +1660,8 @@ void BatchEngine::retire(int64_t slot) {
     if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
     sync_steps();
     Slot& S = slots_[slot];
+    h_overflow_[slot] = 0;
+    h_status_[slot] = 0;
     beads_.release(S.bead_off, S.n);
     blob_.release(S.blob_off, S.blob_size);
     list_alloc_.release(S.list_off, S.list_size);

@@ -16,24 +16,30 @@
 namespace ocm {
 
 // Device record of one admitted system.
+// Status of a system in the batch (BatchSys::status).
+constexpr int kBatchStatusBlownUp = 1;  // non-finite or out-of-range force, velocity or position
+
 struct BatchSys {
     long long bead_off;    // offset into the bead arena
     long long blob_off;    // byte offset of the static blob
     long long list_off;    // offset (entries) of the neighbour-list region
-    int n, nt, n_tiles;    // beads, 32-bead clusters, cluster pairs
-    int n_bonds, n_angles, n_dih, n_masks;
+    int n, nt;             // beads, 32-bead clusters
+    int n_bonds, n_angles, n_dih;
     int off_p0, off_p1, off_lab, off_invm;   // byte offsets inside the blob
-    // Compact bonded records and the FLA/FLD tables, one contiguous region
-    // [off_bonded, off_bonded + bonded_bytes) that the kernel stages into
-    // shared memory when it fits; section offsets are relative to it.
+    // Compact bonded records, the FLA/FLD tables and the chain / gather
+    // indices, one contiguous region [off_bonded, off_bonded + bonded_bytes)
+    // that the kernel stages into shared memory when it fits; section
+    // offsets are relative to it.
     int off_bonded, bonded_bytes;
     int rb_p, rb_ij, ra_ij, ra_k, rd, rgd, rfla, rfld;
-    int off_tmask, off_masks;
+    int rcb, rca, rcd, rgs, rgl;
     int off_ex_start, off_ex;                // exclusion CSR (j | bits << 24)
     int maxn;              // neighbour-list entries per bead
     int active;
     int overflow;          // set by the kernel when a list did not fit
     int builds;            // list builds in the last chunk
+    int status;            // kBatchStatus*: set by the kernel, the system stops advancing
+    int eval_status;       // the same check on the last single evaluation
     float skin;
     PairConsts pc;
     LangevinConsts lc;
@@ -62,8 +68,11 @@ class BatchEngine {
     BatchEngine(int device, int64_t max_systems, int64_t max_beads, int32_t max_beads_per_system);
     ~BatchEngine();
     static int64_t footprint(const SystemDesc& d);
+    // steps_done > 0 resumes a trajectory: the step counter (and with it
+    // the Langevin noise stream) continues from there.
     int64_t admit(const SystemDesc& d, const double* pos, const double* vel, double T,
-                  double friction, double dt, int32_t seed, int64_t n_steps);
+                  double friction, double dt, int32_t seed, int64_t n_steps, int64_t steps_done = 0);
+    int32_t slot_status(int64_t slot);
     void run(int32_t steps_per_launch, bool sync);
     void finished(int64_t* slots, int64_t cap, int64_t* n_out);
     void get_positions(int64_t slot, double* xyz);
@@ -94,6 +103,7 @@ class BatchEngine {
         int slot_group[kNumSlots];
         int64_t list_off = 0, list_size = 0;
         int maxn = 0;
+        bool failed = false;  // blew up: no longer advanced
     };
     void grow_lists();
     void sync_steps();
@@ -117,10 +127,11 @@ class BatchEngine {
     DevBuf<unsigned char> blob_dev_;
     DevBuf<uint16_t> lists_;
     int* h_overflow_ = nullptr;  // pinned copy of the records' overflow flags
+    int* h_status_ = nullptr;    // pinned copy of the records' status words
     DevBuf<BatchSys> sys_;
     DevBuf<int32_t> order_, head_;
     DevBuf<double> energy_;
-    DevBuf<unsigned long long> forces_;
+    DevBuf<float> forces_;
     // staging of the many-slot state copies (grown on demand)
     DevBuf<long long> seg_bead_, seg_off_;
     DevBuf<int> seg_n_;

@@ -556,6 +556,15 @@ int ocm_batch_admit(ocm_batch* batch, const ocm_system* s, const double* pos, co
     BATCH_CALL(need(s, "system"); need(pos, "positions"); need(slot_out, "slot_out");
                *slot_out = batch->b->admit(s->g.desc(), pos, vel, T, friction, dt, seed, n_steps));
 }
+int ocm_batch_admit_resume(ocm_batch* batch, const ocm_system* s, const double* pos, const double* vel,
+                           double T, double friction, double dt, int32_t seed, int64_t n_steps,
+                           int64_t steps_done, int64_t* slot_out) {
+    BATCH_CALL(need(s, "system"); need(pos, "positions"); need(vel, "velocities"); need(slot_out, "slot_out");
+               *slot_out = batch->b->admit(s->g.desc(), pos, vel, T, friction, dt, seed, n_steps, steps_done));
+}
+int ocm_batch_slot_status(ocm_batch* batch, int64_t slot, int32_t* status) {
+    BATCH_CALL(need(status, "status"); *status = batch->b->slot_status(slot));
+}
 int ocm_batch_run(ocm_batch* batch, int32_t steps_per_launch, int sync) {
     BATCH_CALL(batch->b->run(steps_per_launch, sync != 0));
 }

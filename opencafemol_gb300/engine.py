@@ -151,19 +151,39 @@ class Batch:
         return system.footprint()
 
     def admit(self, system: System, positions, velocities=None, temperature: float = 300.0,
-              friction: float = 0.1, step_size: float = 0.01, seed: int = 0, n_steps: int = 0) -> int:
+              friction: float = 0.1, step_size: float = 0.01, seed: int = 0, n_steps: int = 0,
+              steps_done: int = 0) -> int:
+        """Admit a system into a free slot.  ``steps_done`` > 0 resumes a
+        trajectory that already ran that many of its ``n_steps`` steps
+        (velocities required): the Langevin noise continues from that step,
+        so the positions and velocities read back from the slot it left
+        give the uninterrupted trajectory."""
         pos = as_f64(positions).reshape(system.n, 3)
         vel = None if velocities is None else as_f64(velocities).reshape(system.n, 3)
         slot = C.c_int64()
-        check(lib.ocm_batch_admit(self._h, system.handle, dptr(pos), dptr(vel), float(temperature),
-                                  float(friction), float(step_size), int(seed), int(n_steps),
-                                  C.byref(slot)))
+        if steps_done:
+            if vel is None:
+                raise ValueError("resuming a trajectory needs its velocities")
+            check(lib.ocm_batch_admit_resume(self._h, system.handle, dptr(pos), dptr(vel), float(temperature),
+                                             float(friction), float(step_size), int(seed), int(n_steps),
+                                             int(steps_done), C.byref(slot)))
+        else:
+            check(lib.ocm_batch_admit(self._h, system.handle, dptr(pos), dptr(vel), float(temperature),
+                                      float(friction), float(step_size), int(seed), int(n_steps),
+                                      C.byref(slot)))
         self._n[slot.value] = system.n
         self._systems[slot.value] = system
         return slot.value
 
     def run(self, steps_per_launch: int, sync: bool = False) -> None:
         check(lib.ocm_batch_run(self._h, int(steps_per_launch), int(sync)))
+
+    def status(self, slot: int) -> int:
+        """0, or 7 (OCMError code NONFINITE) if the slot's system blew up and
+        stopped advancing."""
+        st = C.c_int32()
+        check(lib.ocm_batch_slot_status(self._h, int(slot), C.byref(st)))
+        return st.value
 
     def finished(self) -> list[int]:
         n = C.c_int64()
