@@ -189,11 +189,24 @@ def batched_roofline(specs, K, launch_s, sm_max_mhz, traffic, sms=None):
                                     f"max SM clock"}}
 
 
+def rank_share(rank, world):
+    """This rank's systems: one seeded ensemble of N_SYSTEMS x world Go
+    proteins (the first N_SYSTEMS are the one-GPU workload), partitioned into
+    whole systems by opencafemol_gb300.partition (largest first onto the
+    least-loaded rank), about N_SYSTEMS per rank."""
+    from opencafemol_gb300 import partition
+    specs = ensemble_specs(count=N_SYSTEMS * world)
+    if world == 1:
+        return specs, specs
+    sh = partition.shard([s.n for s in specs], rank, world)
+    return [specs[k] for k in sorted(sh.indices)], specs
+
+
 def run_ours(args, rank, world):
     import opencafemol_gb300 as ocm
     from opencafemol_gb300 import synth
 
-    specs = ensemble_specs()
+    specs, all_specs = rank_share(rank, world)
     systems = [synth.build_system(s) for s in specs]
     beads = int(sum(s.n for s in specs))
     K = args.md_steps
@@ -201,6 +214,7 @@ def run_ours(args, rank, world):
 
     batch = ocm.Batch(max_systems=len(specs), max_total_beads=beads + 1024,
                       max_beads_per_system=SIZE_HI, device=local_device())
+    total_beads = int(sum(s.n for s in all_specs))
     slots = [batch.admit(sysobj, s.pos, temperature=s.temperature, friction=s.friction,
                          step_size=s.dt, seed=1000 + k, n_steps=10 ** 12)
              for k, (sysobj, s) in enumerate(zip(systems, specs))]
@@ -253,10 +267,12 @@ def run_ours(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Go-model proteins)",
-        "config": {"workload": f"batched ensemble: {len(specs)} Go proteins, N log-uniform "
+        "config": {"workload": f"batched ensemble: {len(all_specs)} Go proteins, N log-uniform "
                                f"[{SIZE_LO},{SIZE_HI}], T~U[280,360] K, dt=10 fs",
-                   "replicas": len(specs), "beads": beads, "md_steps_per_launch": K,
-                   "parallelism": f"replicas x{world} (independent ensembles)",
+                   "replicas": len(all_specs), "beads": total_beads, "md_steps_per_launch": K,
+                   "parallelism": (f"whole systems partitioned over {world} GPUs ({len(specs)} on rank 0, "
+                                   f"largest first onto the least-loaded rank; no collective)"
+                                   if world > 1 else "one GPU"),
                    "launch_shape": {"threads_per_cta": batch.threads(), "autotuned": tuned is not None,
                                     "trials_ms": [t["ms"] for t in tuned["trials"]] if tuned else None},
                    "l2": "flushed (256 MiB write) between timed launches"},
@@ -301,7 +317,7 @@ def run_e2e(ocm, synth, specs, systems, args, world):
         batch.run(K, sync=True)
         batch.get_positions_many(slots, pout)
     t = dist_max(time.perf_counter() - t0, world)
-    return {"value": beads * K * args.steps * world / t, "unit": "bead-steps/s",
+    return {"value": dist_sum(float(beads), world) * K * args.steps / t, "unit": "bead-steps/s",
             "h2d_bytes_per_step": int(pin.nbytes + vin.nbytes), "d2h_bytes_per_step": int(pout.nbytes),
             "what": "positions+velocities H2D (pinned) -> K MD steps -> positions D2H, per step"}
 
@@ -438,23 +454,32 @@ def dist_barrier(world):
         dist.barrier()
 
 
-def dist_max(v, world):
-    """Max of a host value over ranks (NCCL on the GPUs, gloo on the host)."""
+def _dist_reduce(v, world, op_name):
+    """A host value reduced over ranks (NCCL on the GPUs, gloo on the host)."""
     if world <= 1:
         return v
     import torch
     import torch.distributed as dist
     dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
     t = torch.tensor([v], dtype=torch.float64, device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=getattr(dist.ReduceOp, op_name))
     return float(t.item())
 
 
+def dist_max(v, world):
+    return _dist_reduce(v, world, "MAX")
+
+
+def dist_sum(v, world):
+    return _dist_reduce(v, world, "SUM")
+
+
 def aggregate(beads, md_steps, steps, dev_time_local, world):
-    """Whole-job bead-steps/s: every rank advances its own replica set by the
-    same work; the job's time is the slowest rank's (weak scaling)."""
+    """Whole-job bead-steps/s: each rank advances its own share of the
+    ensemble (``beads`` on this rank) by the same number of steps; the job's
+    time is the slowest rank's."""
     t = dist_max(dev_time_local, world)
-    return beads * md_steps * steps * world / t, t
+    return dist_sum(float(beads), world) * md_steps * steps / t, t
 
 
 def run_reference(args, rank, world):

@@ -277,6 +277,15 @@ int ocm_context_step(ocm_context* ctx, int64_t steps);
  * iterations_out may be NULL. */
 int ocm_context_minimize(ocm_context* ctx, double tolerance, int64_t max_iterations,
                          int64_t* iterations_out);
+/* Why the last ocm_context_minimize stopped and the RMS force it reached
+ * (kJ/mol/nm, may be NULL).  *reason: 0 the RMS force reached the
+ * tolerance; 1 the iteration limit; 2 the energy stopped changing (twenty
+ * accepted steps in a row below 1e-12 relative: the FP32 force noise floor,
+ * so a tolerance under that floor is not reached); 3 no step along the
+ * search direction lowered the energy.  OpenMM's LocalEnergyMinimizer
+ * reports none of this (the reference calls it and goes on,
+ * src/Simulator.cpp:41-46).  OCM_ERR_STATE before any minimisation. */
+int ocm_context_minimize_report(ocm_context* ctx, int32_t* reason, double* rms_force);
 
 typedef struct ocm_context_stats {
     int64_t steps_done;

@@ -91,6 +91,7 @@ SIGNATURES = {
                                                            C.c_int64, _I32P, _I32P, _I32P]),
     "ocm_add_capped_go_contact": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP, C.c_double, C.c_int, _I32P]),
     "ocm_context_minimize": (C.c_int, [_P, C.c_double, C.c_int64, _I64P]),
+    "ocm_context_minimize_report": (C.c_int, [_P, _I32P, _DP]),
     "ocm_context_create": (C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int,
                                      C.POINTER(_P)]),
     "ocm_context_destroy": (None, [_P]),

@@ -503,6 +503,11 @@ int ocm_context_minimize(ocm_context* ctx, double tolerance, int64_t max_iterati
     CTX_CALL(const int64_t it = ctx->c->minimize(tolerance, max_iterations);
              if (iterations_out) *iterations_out = it);
 }
+int ocm_context_minimize_report(ocm_context* ctx, int32_t* reason, double* rms_force) {
+    CTX_CALL(need(reason, "reason"); const auto& c = *ctx->c;
+             if (c.min_reason < 0) throw ocm::Error(5, "[error] no minimisation has run on this context");
+             *reason = c.min_reason; if (rms_force) *rms_force = c.min_rms);
+}
 int ocm_context_get_stats(ocm_context* ctx, ocm_context_stats* out) {
     CTX_CALL(need(out, "out"); const auto& c = *ctx->c; out->steps_done = c.steps_done;
              out->list_builds = c.list_builds; out->tiles = c.tiles_last;

@@ -54,7 +54,10 @@ struct BoxD {
 };
 
 struct ListFlags {
-    enum : int { kTileOverflow = 1, kMaskOverflow = 2, kSkinViolation = 4, kChargedOverflow = 8 };
+    // kBlownUp: a force contribution or a summed force of 1e9 kJ/mol/nm or
+    // more (the fixed-point accumulators hold about 2.1e9), a non-finite
+    // force, velocity or position
+    enum : int { kTileOverflow = 1, kMaskOverflow = 2, kSkinViolation = 4, kChargedOverflow = 8, kBlownUp = 16 };
 };
 
 // Device-resident single system, the part of an OpenMM Context + Langevin
@@ -78,6 +81,10 @@ class PlainContext {
     void cluster_order(int64_t* out, int64_t cap, int64_t* n_out);
     // L-BFGS local energy minimisation (minimize.cpp); returns the iterations
     int64_t minimize(double tolerance, int64_t max_iterations);
+    // Why the last minimisation stopped (kMin*) and its final RMS force.
+    enum { kMinConverged = 0, kMinIterationCap = 1, kMinStagnated = 2, kMinLineSearch = 3 };
+    int32_t min_reason = -1;
+    double min_rms = 0.0;
     bool charged_split() const { return charged_split_; }
     double tile_cutoff() const { return tile_cutoff_; }
     int64_t charged_pairs() const { return charged_last_; }
@@ -103,7 +110,7 @@ class PlainContext {
     BoxD box_d() const;
     float wrap_pad() const;
     void alloc_tile_arrays();
-    void eval(uint32_t groups, bool energy, double* forces, double* slot_energy);
+    bool eval(uint32_t groups, bool energy, double* forces, double* slot_energy);
     uint32_t slots_for_groups(uint32_t groups) const;
     void check_positions_set() const;
     // positions from the minimiser: no re-estimate of the cluster column width

@@ -11,10 +11,15 @@
 // (sufficient decrease, c1 = 1e-4) whose first trial moves no bead further
 // than 0.1 nm keeps the steps safe from overlapping configurations.  The
 // search also ends when no step lowers the energy any more (the FP32 force
-// noise floor), so a tolerance below that floor cannot loop forever.
+// noise floor), so a tolerance below that floor cannot loop forever; why
+// it stopped (converged, iteration cap, stagnation, failed line search) and
+// the final RMS force are kept for ocm_context_minimize_report.  A trial
+// position whose evaluation blows up (a force of 1e9 kJ/mol/nm or more)
+// counts as infinite energy, so the line search backs off from it.
 #include <algorithm>
 #include <cmath>
 #include <deque>
+#include <limits>
 #include <vector>
 
 #include "engine.hpp"
@@ -41,13 +46,24 @@ int64_t PlainContext::minimize(double tolerance, int64_t max_iterations) {
     auto evaluate = [&](const std::vector<double>& pos, std::vector<double>& grad) {
         set_positions_internal(pos.data());
         double e = 0;
-        get_state(0xffffffffu, f.data(), &e);
+        try {
+            get_state(0xffffffffu, f.data(), &e);
+        } catch (const Error& err) {
+            if (err.code != 7) throw;
+            e = std::numeric_limits<double>::infinity();
+        }
         for (std::size_t i = 0; i < m3; ++i) grad[i] = -f[i];
         return e;
     };
     auto rms = [&](const std::vector<double>& grad) { return std::sqrt(dot(grad, grad) / (double)m3); };
 
     double e = evaluate(x, g);
+    if (!std::isfinite(e)) {
+        set_positions_internal(x.data());
+        throw Error(7, "[error] the starting positions give a non-finite energy or a force of 1e9 kJ/mol/nm "
+                       "or more; minimisation cannot start");
+    }
+    min_reason = kMinIterationCap;
     std::deque<std::vector<double>> S, Y;
     std::deque<double> R;
     const std::size_t memory = 10;
@@ -98,7 +114,10 @@ int64_t PlainContext::minimize(double tolerance, int64_t max_iterations) {
             // no decrease along this direction: forget the curvature pairs
             // and try steepest descent once more, then give up
             set_positions_internal(x.data());
-            if (S.empty() || ++failures > 1) break;
+            if (S.empty() || ++failures > 1) {
+                min_reason = kMinLineSearch;
+                break;
+            }
             S.clear();
             Y.clear();
             R.clear();
@@ -128,9 +147,14 @@ int64_t PlainContext::minimize(double tolerance, int64_t max_iterations) {
         x.swap(xn);
         g.swap(gn);
         e = en;
-        if (stalled >= 20) break;
+        if (stalled >= 20) {
+            min_reason = kMinStagnated;
+            break;
+        }
     }
     set_positions_internal(x.data());
+    min_rms = rms(g);
+    if (min_rms <= tolerance) min_reason = kMinConverged;
     return it;
 }
 

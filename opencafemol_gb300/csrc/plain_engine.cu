@@ -685,12 +685,23 @@ struct ForceArgs {
     const float4 *xq, *xlo, *p0;
     const int32_t *chg_idx, *chg_rows, *chg_len;
     int n_chg, chg_row_cap;
+    int32_t* flags;
 };
 
-__device__ __forceinline__ void add_force(unsigned long long* F, int n, int i, float3 f) {
-    fixed_add(&F[i], f.x);
-    fixed_add(&F[n + i], f.y);
-    fixed_add(&F[2 * n + i], f.z);
+// A force of this size (kJ/mol/nm) or more, or a non-finite one, marks a
+// blown-up system: the 64-bit accumulators hold |F| < 2^31 at 2^32 units
+// per kJ/mol/nm, so sums of such contributions could wrap.
+constexpr float kForceLimit = 1.0e9f;
+
+__device__ __forceinline__ bool force_ok(float3 f) {
+    return fabsf(f.x) < kForceLimit && fabsf(f.y) < kForceLimit && fabsf(f.z) < kForceLimit;
+}
+
+__device__ __forceinline__ void add_force(const ForceArgs& a, int i, float3 f) {
+    if (!force_ok(f)) atomicOr(a.flags, ListFlags::kBlownUp);
+    fixed_add(&a.F[i], f.x);
+    fixed_add(&a.F[a.n + i], f.y);
+    fixed_add(&a.F[2 * a.n + i], f.z);
 }
 
 __device__ __forceinline__ float3 bonded_sep(const ForceArgs& a, int i, int j, int periodic) {
@@ -735,7 +746,7 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
             for (int t = c0; t < c1; ++t) {
                 while (t >= row_end) {
                     const int oi = a.perm[ki];
-                    if (oi >= 0) add_force(a.F, a.n, oi, fi);
+                    if (oi >= 0) add_force(a, oi, fi);
                     fi = make_float3(0.f, 0.f, 0.f);
                     ++I;
                     row_end = a.tile_start[I + 1];
@@ -812,7 +823,7 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                     fj.z = __shfl_sync(kFull, fj.z, src);
                 }
                 const int oj = a.perm[kj];
-                if (oj >= 0) add_force(a.F, a.n, oj, fj);
+                if (oj >= 0) add_force(a, oj, fj);
                 if (ENERGY) {
                     eacc[0] += e.exv;
                     eacc[1] += e.dh;
@@ -821,7 +832,7 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                 }
             }
             const int oi = a.perm[ki];
-            if (oi >= 0) add_force(a.F, a.n, oi, fi);
+            if (oi >= 0) add_force(a, oi, fi);
         }
         if (ENERGY) {
 #pragma unroll
@@ -853,8 +864,8 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                 const float3 d = make_float3((float)dx, (float)dy, (float)dz);
                 float en;
                 const float s = bond_scalar(b.kind, norm2(d), delta, b.p0, b.p1, b.r0sq_hi, en);
-                add_force(a.F, a.n, b.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
-                add_force(a.F, a.n, b.j, make_float3(s * d.x, s * d.y, s * d.z));
+                add_force(a, b.i, make_float3(-s * d.x, -s * d.y, -s * d.z));
+                add_force(a, b.j, make_float3(s * d.x, s * d.y, s * d.z));
                 if (b.kind == kBondHarmonic) eh = en;
                 else if (b.kind == kBondGo) eg = en;
                 else if (b.kind == kBondGauss) eb = en;
@@ -883,9 +894,9 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
             const float3 v = bonded_sep(a, g.j, g.k, g.periodic);  // x3 - x2
             float3 f1, f3;
             fla_forces(u, v, g.kk, a.fla[g.table], f1, f3, en);
-            add_force(a.F, a.n, g.i, f1);
-            add_force(a.F, a.n, g.k, f3);
-            add_force(a.F, a.n, g.j, make_float3(-f1.x - f3.x, -f1.y - f3.y, -f1.z - f3.z));
+            add_force(a, g.i, f1);
+            add_force(a, g.k, f3);
+            add_force(a, g.j, make_float3(-f1.x - f3.x, -f1.y - f3.y, -f1.z - f3.z));
         }
         if (ENERGY) {
             const double v = warp_sum((double)en);
@@ -913,10 +924,10 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                     gauss_dihedral_forces(F, G, H, q.kk, q.theta0, q.inv2s2, f1, f2, f3, f4, en);
                     egd = en;
                 }
-                add_force(a.F, a.n, q.i, f1);
-                add_force(a.F, a.n, q.j, f2);
-                add_force(a.F, a.n, q.k, f3);
-                add_force(a.F, a.n, q.l, f4);
+                add_force(a, q.i, f1);
+                add_force(a, q.j, f2);
+                add_force(a, q.k, f3);
+                add_force(a, q.l, f4);
             }
         }
         if (ENERGY) {
@@ -945,6 +956,7 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                 const int len = min(a.chg_len[t], a.chg_row_cap);
                 const int32_t* row = a.chg_rows + (size_t)t * a.chg_row_cap;
                 long long fx = 0, fy = 0, fz = 0;
+                bool bad = false;
                 for (int p = lane; p < len; p += 32) {
                     const int j = row[p];
                     const float3 d = ff_separation<PERIODIC>(xi, li, a.xq[j], a.xlo[j], a.box, a.inv_box);
@@ -953,6 +965,7 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                         PairEnergy e;
                         e.zero();
                         const float sc = pair_scalar<kTermDH, ENERGY>(r2, pi, a.p0[j], zero4, zero4, 0u, a.pc, e);
+                        bad = bad || !force_ok(make_float3(sc * d.x, sc * d.y, sc * d.z));
                         fx += (long long)to_fixed(-sc * d.x);
                         fy += (long long)to_fixed(-sc * d.y);
                         fz += (long long)to_fixed(-sc * d.z);
@@ -965,6 +978,7 @@ __global__ void __launch_bounds__(kForceThreads) k_forces(ForceArgs a) {
                     fy += __shfl_xor_sync(0xffffffffu, fy, o);
                     fz += __shfl_xor_sync(0xffffffffu, fz, o);
                 }
+                if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(a.flags, ListFlags::kBlownUp);
                 if (lane == 0) {
                     if (fx) atomicAdd(&a.F[i], (unsigned long long)fx);
                     if (fy) atomicAdd(&a.F[a.n + i], (unsigned long long)fy);
@@ -1011,6 +1025,7 @@ __global__ void k_integrate(IntegrateArgs a) {
     const float fx = fixed_to_float((long long)a.F[i]);
     const float fy = fixed_to_float((long long)a.F[a.n + i]);
     const float fz = fixed_to_float((long long)a.F[2 * a.n + i]);
+    bool bad = !(fabsf(fx) < kForceLimit && fabsf(fy) < kForceLimit && fabsf(fz) < kForceLimit);
     a.F[i] = 0ull;
     a.F[a.n + i] = 0ull;
     a.F[2 * a.n + i] = 0ull;
@@ -1032,7 +1047,9 @@ __global__ void k_integrate(IntegrateArgs a) {
         a.x[i] = x;
         a.y[i] = y;
         a.z[i] = z;
+        bad = bad || !(isfinite(x) && isfinite(y) && isfinite(z));
     }
+    if (bad) atomicOr(a.flags, ListFlags::kBlownUp);
     double w[3] = {x, y, z};
     if (a.periodic)
         for (int c = 0; c < 3; ++c) w[c] = wrap_coord(w[c], a.box[c], a.inv_box[c]);
@@ -1564,6 +1581,7 @@ void PlainContext::launch_forces(cudaStream_t s, bool energy, uint32_t slots_ena
     a.chg_len = chg_len_.p;
     a.n_chg = (int)n_charged_;
     a.chg_row_cap = (int)chg_row_cap_;
+    a.flags = flags_.p;
     a.blocks_chg = charged_split_ ? (int)std::max<int64_t>(1, div_up(n_charged_, kWarpsPerForceBlock)) : 0;
     a.energy = energy_.p;
     int blocks_tiles = a.blocks_tiles;
@@ -1677,13 +1695,18 @@ uint32_t PlainContext::slots_for_groups(uint32_t groups) const {
     return s;
 }
 
-void PlainContext::eval(uint32_t groups, bool energy, double* forces, double* slot_energy) {
+// Returns true when the evaluation flagged a blown-up system (the outputs
+// are filled all the same).
+bool PlainContext::eval(uint32_t groups, bool energy, double* forces, double* slot_energy) {
     OCM_CK(cudaSetDevice(device));
     check_positions_set();
     ensure_capacity();
     OCM_CK(cudaMemsetAsync(energy_.p, 0, kNumSlots * sizeof(double), stream_));
     OCM_CK(cudaMemsetAsync(F_.p, 0, 3 * n * sizeof(unsigned long long), stream_));
+    OCM_CK(cudaMemsetAsync(flags_.p, 0, sizeof(int32_t), stream_));
     launch_forces(stream_, energy, slots_for_groups(groups), 0);
+    int32_t flags = 0;
+    OCM_CK(cudaMemcpyAsync(&flags, flags_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
     std::vector<unsigned long long> f;
     if (forces) {
         f.resize(3 * n);
@@ -1700,25 +1723,32 @@ void PlainContext::eval(uint32_t groups, bool energy, double* forces, double* sl
                 forces[3 * i + c] = (double)(long long)f[c * n + i] * kFixedInv;
     if (slot_energy)
         for (int k = 0; k < kNumSlots; ++k) slot_energy[k] = e[k];
+    return (flags & ListFlags::kBlownUp) != 0;
+}
+
+static void throw_blown_up() {
+    throw Error(7, "[error] non-finite force, or a force of 1e9 kJ/mol/nm or more (outputs filled)");
 }
 
 void PlainContext::get_state(uint32_t groups, double* forces, double* energy) {
     double se[kNumSlots];
-    eval(groups, energy != nullptr, forces, se);
+    const bool blown = eval(groups, energy != nullptr, forces, se);
     if (energy) {
         double tot = 0;
         for (int k = 0; k < kNumSlots; ++k)
             if (cs.slot_group[k] >= 0 && ((groups >> cs.slot_group[k]) & 1u)) tot += se[k];
         *energy = tot;
     }
+    if (blown) throw_blown_up();
 }
 
 void PlainContext::group_energies(double* e32) {
     double se[kNumSlots];
-    eval(0xffffffffu, true, nullptr, se);
+    const bool blown = eval(0xffffffffu, true, nullptr, se);
     for (int g = 0; g < 32; ++g) e32[g] = 0.0;
     for (int k = 0; k < kNumSlots; ++k)
         if (cs.slot_group[k] >= 0) e32[cs.slot_group[k]] += se[k];
+    if (blown) throw_blown_up();
 }
 
 cudaGraphExec_t PlainContext::graph_for(int chunk) {
@@ -1794,6 +1824,9 @@ void PlainContext::step(int64_t nsteps) {
             cs.box[0] > 0 ? 1.0 / cs.box[0] : 0.0, cs.box[1] > 0 ? 1.0 / cs.box[1] : 0.0,
             cs.box[2] > 0 ? 1.0 / cs.box[2] : 0.0, xq_.p, xlo_.p);
         OCM_CK(cudaStreamSynchronize(s));
+        if (flags & ListFlags::kBlownUp)
+            throw Error(7, "[error] the system blew up (a non-finite force, velocity or position, or a force of "
+                           "1e9 kJ/mol/nm or more); the context keeps its state from before this step call");
         if (flags & ListFlags::kSkinViolation) {
             if (rebuild_interval == 1)
                 throw Error(7, "[error] particles moved more than half the skin in one step");

@@ -121,11 +121,21 @@ class LocalEnergyMinimizer:
     of all force components is at most ``tolerance`` kJ/mol/nm, or
     ``maxIterations`` iterations (0: no limit).  Returns the iterations."""
 
+    REASONS = ("converged", "iteration limit", "stagnated at the FP32 force floor", "line search failed")
+
     @staticmethod
     def minimize(context: Context, tolerance: float = 10.0, maxIterations: int = 0) -> int:
         it = C.c_int64()
         check(lib.ocm_context_minimize(context._h, float(tolerance), int(maxIterations), C.byref(it)))
         return it.value
+
+    @staticmethod
+    def report(context: Context) -> dict:
+        """Why the last minimisation of ``context`` stopped, and the RMS
+        force it reached (the tolerance may be below the FP32 force floor)."""
+        r, rms = C.c_int32(), C.c_double()
+        check(lib.ocm_context_minimize_report(context._h, C.byref(r), C.byref(rms)))
+        return {"reason": LocalEnergyMinimizer.REASONS[r.value], "code": r.value, "rms_force": rms.value}
 
 
 class Batch:
