@@ -250,7 +250,8 @@ def run_ours(args, rank, world):
 
     # ---- plain single-system path on a sample of the same mix ----
     plain = run_plain(ocm, specs, systems, args) if args.plain_sample > 0 else None
-    plain_cfgs = run_plain_configs(ocm, args) if (args.cfg0_steps > 0 or args.cfg1_steps > 0) else None
+    plain_cfgs = (run_plain_configs(ocm, args)
+                  if (args.cfg0_steps > 0 or args.cfg1_steps > 0 or args.cfg2_steps > 0) else None)
 
     # ---- served stream (continuous batching), p50/p99 completion latency ----
     serve = run_serving(ocm, args) if args.serve_requests > 0 and rank == 0 else None
@@ -373,11 +374,12 @@ def run_plain(ocm, specs, systems, args):
 
 
 def run_plain_configs(ocm, args):
-    """The plain single-system path on the two single-system shapes:
-    a 60-bead Go protein (10 fs steps, non-periodic) and a 20,000-bead HPS
-    condensate slab (100 chains x 200 beads, 15 x 15 x 150 nm periodic box,
-    HPS cutoff 2.0 nm, Debye-Hueckel 3.5 nm on 20% charged beads).  The slab
-    starts from a random packing, so it is relaxed first (untimed, strong
+    """The plain single-system path on the single-system shapes: a 60-bead
+    Go protein (10 fs steps, non-periodic), a 20,000-bead HPS condensate
+    slab (100 chains x 200 beads, 15 x 15 x 150 nm periodic box, HPS cutoff
+    2.0 nm, Debye-Hueckel 3.5 nm on 20% charged beads) and the 200,000-bead
+    slab of the same recipe (1000 chains, 30 x 30 x 300 nm).  The slabs
+    start from a random packing, so they are relaxed first (untimed, strong
     friction, 2 fs steps).  Wall-clock timing around synchronous steps."""
     from opencafemol_gb300 import synth
     out = {}
@@ -387,6 +389,9 @@ def run_plain_configs(ocm, args):
     if args.cfg1_steps > 0:
         cases.append(("hps_slab_20000", synth.hps_slab(100, 200, (15.0, 15.0, 150.0), slab_width=30.0, seed=7),
                       args.cfg1_relax, args.cfg1_steps))
+    if args.cfg2_steps > 0:
+        cases.append(("hps_slab_200000", synth.hps_slab(1000, 200, (30.0, 30.0, 300.0), slab_width=60.0, seed=7),
+                      args.cfg1_relax, args.cfg2_steps))
     for name, spec, relax, steps in cases:
         system = synth.build_system(spec)
         pos = spec.pos
@@ -545,6 +550,7 @@ def main():
     ap.add_argument("--cfg0-steps", type=int, default=10000)
     ap.add_argument("--cfg1-steps", type=int, default=2000)
     ap.add_argument("--cfg1-relax", type=int, default=3000)
+    ap.add_argument("--cfg2-steps", type=int, default=1000)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-step-scale", type=int, default=50)
     ap.add_argument("--serve-chunk", type=int, default=100)

@@ -237,6 +237,148 @@ def add_aicg_gaussians(spec: CGSpec, seed: int, gb_sigma: float = 0.015,
     return spec
 
 
+def _pack_chains(n_chains: int, chain_len: int, L: np.ndarray, zlo: float, zhi: float, min_dist: float,
+                 rng: np.random.Generator, bond: float = 0.38, theta=(1.75, 2.6)) -> np.ndarray:
+    """Random-walk chains packed into the slab zlo <= z <= zhi of a periodic
+    box, every bead at least ``min_dist`` from every other bead except its
+    bonded predecessor.  All chains grow at once, one bead per chain per
+    round: a chain proposes one candidate (eight after a failure), drawn
+    with numpy (bond angle in ``theta`` after the second bead, a free
+    direction after 400 failed tries); candidates are checked against the
+    placed beads through a dense cell grid and against each other with a
+    periodic k-d tree.  A chain stuck for 800 tries steps back eight beads;
+    after 200 step-backs it starts over."""
+    from scipy.spatial import cKDTree
+    n = n_chains * chain_len
+    nc = np.maximum(1, np.floor(L / min_dist).astype(np.int64))
+    cw = L / nc
+    cap = 4  # a cell is min_dist wide: at most three beads fit (one bonded pair closer)
+    grid = np.full((int(np.prod(nc)), cap), -1, np.int64)
+    gcnt = np.zeros(int(np.prod(nc)), np.int64)
+    pos = np.full((n, 3), np.nan)
+    wpos = np.full((n + 1, 3), np.nan, np.float32)  # wrapped into the box; row n: an empty slot
+    length = np.zeros(n_chains, np.int64)
+    prev_dir = np.zeros((n_chains, 3))
+    tries = np.zeros(n_chains, np.int64)
+    backs = np.zeros(n_chains, np.int64)
+    offs = np.array([(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)])
+    md2 = min_dist * min_dist
+
+    def wrap(p):
+        w = p - L * np.floor(p / L)
+        return np.where(w >= L, w - L, w)
+
+    def cells(p):
+        return np.minimum((wrap(p) / cw).astype(np.int64), nc - 1)
+
+    def lin(c):
+        return (c[..., 0] * nc[1] + c[..., 1]) * nc[2] + c[..., 2]
+
+    def insert(lc, gidx):
+        order = np.argsort(lc, kind="stable")
+        lcs, gs = lc[order], gidx[order]
+        uniq, first, counts = np.unique(lcs, return_index=True, return_counts=True)
+        rank = np.arange(len(lcs)) - np.repeat(first, counts)
+        slot = gcnt[lcs] + rank
+        if np.any(slot >= cap):
+            raise RuntimeError("slab packing: a grid cell overflowed")
+        grid[lcs, slot] = gs
+        gcnt[uniq] += counts
+
+    def drop_beads(c, keep):
+        """Remove beads keep.. of chain c from the grid."""
+        for g in range(c * chain_len + keep, c * chain_len + int(length[c])):
+            cell = int(lin(cells(pos[g])))
+            row = grid[cell, : gcnt[cell]]
+            rest = row[row != g]
+            grid[cell, :] = -1
+            grid[cell, : len(rest)] = rest
+            gcnt[cell] = len(rest)
+            pos[g] = np.nan
+            wpos[g] = np.nan
+        length[c] = keep
+        if keep >= 2:
+            b = pos[c * chain_len + keep - 1] - pos[c * chain_len + keep - 2]
+            b -= L * np.round(b / L)
+            prev_dir[c] = b / np.linalg.norm(b)
+
+    while True:
+        act = np.nonzero(length < chain_len)[0]
+        if act.size == 0:
+            break
+        ncand = np.where(tries[act] == 0, 1, 8)
+        row = np.repeat(np.arange(act.size), ncand)      # candidate -> active chain
+        ch = act[row]
+        k = length[ch]
+        m = row.size
+        cand = np.empty((m, 3))
+        dirs = np.zeros((m, 3))
+        first = k == 0
+        if first.any():
+            f = int(first.sum())
+            cand[first] = np.stack([rng.uniform(0, L[0], f), rng.uniform(0, L[1], f), rng.uniform(zlo, zhi, f)], 1)
+        rest = np.nonzero(~first)[0]
+        if rest.size:
+            d = rng.normal(size=(rest.size, 3))
+            d /= np.linalg.norm(d, axis=1, keepdims=True)
+            con = (k[rest] >= 2) & (tries[ch[rest]] < 400)
+            if con.any():
+                b = prev_dir[ch[rest[con]]]
+                t = np.where(np.abs(b[:, :1]) < 0.9, np.array([1.0, 0.0, 0.0]), np.array([0.0, 1.0, 0.0]))
+                u = np.cross(b, t)
+                u /= np.linalg.norm(u, axis=1, keepdims=True)
+                w = np.cross(b, u)
+                th = rng.uniform(theta[0], theta[1], len(b))[:, None]
+                ph = rng.uniform(-math.pi, math.pi, len(b))[:, None]
+                d[con] = -np.cos(th) * b + np.sin(th) * (np.cos(ph) * u + np.sin(ph) * w)
+            dirs[rest] = d
+            cand[rest] = pos[ch[rest] * chain_len + k[rest] - 1] + bond * d
+        ok = (cand[:, 2] >= zlo) & (cand[:, 2] <= zhi)
+        wc = wrap(cand)
+        cc = np.minimum((wc / cw).astype(np.int64), nc - 1)
+        raw = cc[:, None, :] + offs[None, :, :]                                # (m, 27, 3)
+        shift = (np.floor_divide(raw, nc) * L).astype(np.float32)              # image of each cell
+        idx = grid[lin(raw % nc)]                                              # (m, 27, cap)
+        own_prev = np.where(k > 0, ch * chain_len + k - 1, -2)
+        idx = np.where(idx == own_prev[:, None, None], -1, idx)
+        dd = wpos[np.where(idx >= 0, idx, n)] + (shift - wc[:, None, :].astype(np.float32))[:, :, None, :]
+        d2 = np.einsum("mcsk,mcsk->mcs", dd, dd)
+        ok &= ~np.any(d2 < np.float32(md2), axis=(1, 2))  # empty slots hold NaN: never close
+        # each chain keeps its first valid candidate
+        good = np.nonzero(ok)[0]
+        _, firsts = np.unique(row[good], return_index=True)
+        pick = good[firsts]
+        if pick.size > 1:
+            w = cand[pick] - L * np.floor(cand[pick] / L)
+            w = np.where(w >= L, w - L, w)
+            pairs = cKDTree(w, boxsize=L).query_pairs(min_dist, output_type="ndarray")
+            if len(pairs):
+                pick = np.delete(pick, np.unique(pairs.max(axis=1)))
+        placed = np.zeros(act.size, bool)
+        if pick.size:
+            ca = ch[pick]
+            gidx = ca * chain_len + k[pick]
+            pos[gidx] = cand[pick]
+            wpos[gidx] = wc[pick]
+            prev_dir[ca] = dirs[pick]
+            length[ca] += 1
+            tries[ca] = 0
+            insert(lin(cc[pick]), gidx)
+            placed[row[pick]] = True
+        fail = act[~placed]
+        tries[fail] += ncand[~placed]
+        for c in fail[tries[fail] > 800]:
+            c = int(c)
+            backs[c] += 1
+            if backs[c] > 200:
+                drop_beads(c, 0)
+                backs[c] = 0
+            else:
+                drop_beads(c, max(0, int(length[c]) - 8))
+            tries[c] = 0
+    return pos
+
+
 def hps_slab(n_chains: int, chain_len: int, box, slab_width: float, seed: int,
              hps_cutoff: float = 2.0, dh_cutoff: float = 3.5, charge_fraction: float = 0.2,
              ionic_strength: float = 0.15, temperature: float = 300.0,
@@ -247,90 +389,9 @@ def hps_slab(n_chains: int, chain_len: int, box, slab_width: float, seed: int,
     lam_t = rng.uniform(0.0, 1.0, 20)
     n = n_chains * chain_len
     types = rng.integers(0, 20, n).astype(np.int32)
-    pos = np.zeros((n, 3))
-    # hash grid of placed beads for the overlap test
-    cell = min_dist
-    grid: dict[tuple, list[int]] = {}
     L = np.array(box)
     zlo, zhi = 0.5 * box[2] - 0.5 * slab_width, 0.5 * box[2] + 0.5 * slab_width
-
-    def key(p):
-        w = p - L * np.floor(p / L)
-        return tuple((w // cell).astype(int))
-
-    def clash(p, skip=()):
-        k = key(p)
-        nc = np.maximum(1, (L // cell).astype(int))
-        for dx in (-1, 0, 1):
-            for dy in (-1, 0, 1):
-                for dz in (-1, 0, 1):
-                    kk = ((k[0] + dx) % nc[0], (k[1] + dy) % nc[1], (k[2] + dz) % nc[2])
-                    for j in grid.get(kk, ()):
-                        if j in skip:
-                            continue
-                        d = pos[j] - p
-                        d -= L * np.round(d / L)
-                        if d @ d < min_dist * min_dist:
-                            return True
-        return False
-
-    def put(i, p):
-        nc = np.maximum(1, (L // cell).astype(int))
-        k = key(p)
-        grid.setdefault((k[0] % nc[0], k[1] % nc[1], k[2] % nc[2]), []).append(i)
-        pos[i] = p
-
-    def unput(i):
-        nc = np.maximum(1, (L // cell).astype(int))
-        k = key(pos[i])
-        grid[(k[0] % nc[0], k[1] % nc[1], k[2] % nc[2])].remove(i)
-
-    i = 0
-    for _c in range(n_chains):
-        start = i
-        for _restart in range(50):
-            i = start
-            for _try in range(1000):
-                p0 = np.array([rng.uniform(0, box[0]), rng.uniform(0, box[1]), rng.uniform(zlo, zhi)])
-                if not clash(p0):
-                    break
-            put(i, p0)
-            i += 1
-            prev_b = None
-            ok = True
-            for _k in range(1, chain_len):
-                placed = False
-                # bond angle in [1.75, 2.6] rad first; free direction when stuck at a wall
-                for _try in range(800):
-                    if prev_b is None or _try >= 400:
-                        dvec = rng.normal(size=3)
-                        dvec /= np.linalg.norm(dvec)
-                    else:
-                        u, w = _orthonormal(prev_b)
-                        th = rng.uniform(1.75, 2.6)
-                        ph = rng.uniform(-math.pi, math.pi)
-                        dvec = -math.cos(th) * prev_b + math.sin(th) * (math.cos(ph) * u + math.sin(ph) * w)
-                    cand = pos[i - 1] + 0.38 * dvec
-                    if cand[2] < zlo or cand[2] > zhi:
-                        continue
-                    # only the bonded predecessor may be closer than min_dist (the
-                    # bond-angle range keeps i-2 at >= 0.58 nm; a free direction
-                    # must not fold back onto it)
-                    if not clash(cand, skip=(i - 1,)):
-                        placed = True
-                        break
-                if not placed:
-                    ok = False
-                    break
-                put(i, cand)
-                prev_b = dvec
-                i += 1
-            if ok:
-                break
-            for k in range(start, i):
-                unput(k)
-        else:
-            raise RuntimeError("could not place a chain in the slab")
+    pos = _pack_chains(n_chains, chain_len, L, zlo, zhi, min_dist, rng)
     pos = pos - L * np.floor(pos / L)
     pos = _f32(pos)
     pos = np.where(pos >= L, pos - L, pos)  # FP32 rounding may land exactly on L
