@@ -142,7 +142,7 @@ BYTES_INTEGRATE_PER_BEAD = 100
 # dram__bytes_read.sum + dram__bytes_write.sum of one timed k_batch launch of
 # the default workload (100 MD steps of the 512-replica mix), from a
 # `ncu --set full --clock-control none` capture of this script
-K_BATCH_DRAM_BYTES = 20386304 + 256
+K_BATCH_DRAM_BYTES = 21352192 + 0
 
 
 def measured_hbm_gbs():
