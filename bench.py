@@ -370,7 +370,8 @@ def run_plain(ocm, specs, systems, args):
         t += time.perf_counter() - t0
         bead_steps += s.n * K * args.plain_chunks
     return {"value": bead_steps / t, "unit": "bead-steps/s", "systems_sampled": int(len(idx)),
-            "what": "one Context per system, systems stepped sequentially"}
+            "what": "one Context per system, systems stepped sequentially (default engine: systems of "
+                    "at most 512 beads on the one-system batched kernel, larger ones on the tiles)"}
 
 
 def run_plain_configs(ocm, args):
@@ -418,6 +419,7 @@ def run_plain_configs(ocm, args):
                      "ns_per_day": steps / t * spec.dt * 86400 * 1e-3, "us_per_step": t / steps * 1e6,
                      "list_builds": int(st["list_builds"]), "tiles": int(st["tiles"]),
                      "charged_pairs": int(st["charged_pairs"]), "tile_cutoff_nm": round(st["tile_cutoff"], 4),
+                     "engine": "one-system batched kernel" if st["one_system"] else "cluster-pair tiles",
                      "untimed_relaxation_steps": int(relax)}
     return out
 

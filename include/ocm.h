@@ -277,6 +277,17 @@ int ocm_context_step(ocm_context* ctx, int64_t steps);
  * iterations_out may be NULL. */
 int ocm_context_minimize(ocm_context* ctx, double tolerance, int64_t max_iterations,
                          int64_t* iterations_out);
+/* Engine of ocm_context_step.  0 (default): a non-periodic system of at
+ * most 512 beads runs as a one-system persistent launch of the batched
+ * kernel (its whole chunk of steps in one SM's shared memory, no per-step
+ * launches; the state moves device-to-device between the context and the
+ * one-slot batch), every other system on the cluster-pair tiles; 1: always
+ * the tiles; 2: always the one-system kernel (non-periodic, at most 2048
+ * beads, else OCM_ERR_UNSUPPORTED).  Both engines evaluate the same force
+ * field with the same Langevin noise stream; trajectories differ by FP32
+ * rounding.  Evaluations (get_state, energies, minimisation) always use the
+ * tiles.  OpenMM has no counterpart: a Platform picks its kernels itself. */
+int ocm_context_set_engine(ocm_context* ctx, int32_t mode);
 /* Why the last ocm_context_minimize stopped and the RMS force it reached
  * (kJ/mol/nm, may be NULL).  *reason: 0 the RMS force reached the
  * tolerance; 1 the iteration limit; 2 the energy stopped changing (twenty
@@ -299,7 +310,7 @@ typedef struct ocm_context_stats {
     double  tile_cutoff;      /* nm: largest cutoff the cluster-pair tiles serve */
     int64_t charged_pairs;    /* entries of the charged-pair list (0 without one) */
     int32_t charged_split;    /* 1 if Debye-Hueckel runs on its own charged-pair list */
-    int32_t reserved_;
+    int32_t one_system;       /* 1 if the last step call ran on the one-system batched kernel */
 } ocm_context_stats;
 int ocm_context_get_stats(ocm_context* ctx, ocm_context_stats* out);
 /* Rebuild interval / skin overrides (0 keeps the current value). */

@@ -37,7 +37,7 @@ class ContextStats(C.Structure):
                 ("masked_tiles", C.c_int64), ("rebuild_interval", C.c_int32),
                 ("reordered", C.c_int32), ("skin", C.c_double), ("max_cutoff", C.c_double),
                 ("tile_cutoff", C.c_double), ("charged_pairs", C.c_int64), ("charged_split", C.c_int32),
-                ("reserved_", C.c_int32)]
+                ("one_system", C.c_int32)]
 
 
 _P = C.c_void_p
@@ -92,6 +92,7 @@ SIGNATURES = {
     "ocm_add_capped_go_contact": (C.c_int, [_P, C.c_int64, _I64P, _DP, _DP, C.c_double, C.c_int, _I32P]),
     "ocm_context_minimize": (C.c_int, [_P, C.c_double, C.c_int64, _I64P]),
     "ocm_context_minimize_report": (C.c_int, [_P, _I32P, _DP]),
+    "ocm_context_set_engine": (C.c_int, [_P, C.c_int32]),
     "ocm_context_create": (C.c_int, [_P, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int,
                                      C.POINTER(_P)]),
     "ocm_context_destroy": (None, [_P]),

@@ -1515,6 +1515,54 @@ void BatchEngine::sync_steps() {
     }
 }
 
+void BatchEngine::load_state_device(int64_t slot, const double* x, const double* y, const double* z,
+                                    const float* vx, const float* vy, const float* vz, uint64_t steps_done,
+                                    uint64_t steps_target) {
+    OCM_CK(cudaSetDevice(device_));
+    if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
+    if (steps_done > steps_target) throw Error(1, "[error] steps already done exceed the step target");
+    sync_steps();
+    Slot& S = slots_[slot];
+    const int64_t n = S.n, o = S.bead_off;
+    cudaStream_t s = stream_;
+    OCM_CK(cudaMemcpyAsync(x_.p + o, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(y_.p + o, y, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(z_.p + o, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(vx_.p + o, vx, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(vy_.p + o, vy, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(vz_.p + o, vz, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    BatchSys& R = sys_host_[slot];
+    R.steps_done = steps_done;
+    R.steps_target = steps_target;
+    R.status = 0;
+    BatchSys* dst = sys_.p + slot;
+    OCM_CK(cudaMemcpyAsync(&dst->steps_done, &R.steps_done, 2 * sizeof(unsigned long long),
+                           cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemcpyAsync(&dst->status, &R.status, sizeof(int), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaStreamSynchronize(s));
+    S.steps_done = steps_done;
+    S.steps_target = steps_target;
+    S.failed = false;
+    h_status_[slot] = 0;
+}
+
+void BatchEngine::store_state_device(int64_t slot, double* x, double* y, double* z, float* vx, float* vy,
+                                     float* vz) {
+    OCM_CK(cudaSetDevice(device_));
+    if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");
+    sync_steps();
+    const Slot& S = slots_[slot];
+    const int64_t n = S.n, o = S.bead_off;
+    cudaStream_t s = stream_;
+    OCM_CK(cudaMemcpyAsync(x, x_.p + o, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(y, y_.p + o, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(z, z_.p + o, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(vx, vx_.p + o, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(vy, vy_.p + o, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaMemcpyAsync(vz, vz_.p + o, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    OCM_CK(cudaStreamSynchronize(s));
+}
+
 int32_t BatchEngine::slot_status(int64_t slot) {
     OCM_CK(cudaSetDevice(device_));
     if (slot < 0 || slot >= max_systems_ || !slots_[slot].used) throw Error(1, "[error] invalid slot");

@@ -1,8 +1,8 @@
 // batch_engine.hpp - many independent systems advanced by one persistent
 // kernel per chunk of steps.  Each CTA claims a system from a work queue
 // (largest first), pulls its state into shared memory, runs the chunk
-// there (cluster-pair tiles with per-step bounding-box culling, bonded
-// terms, Langevin update) and writes the state back.
+// there (Verlet lists, pair units, chain-local and gathered bonded terms,
+// Langevin update) and writes the state back.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -15,9 +15,10 @@
 
 namespace ocm {
 
-// Device record of one admitted system.
 // Status of a system in the batch (BatchSys::status).
 constexpr int kBatchStatusBlownUp = 1;  // non-finite or out-of-range force, velocity or position
+
+// Device record of one admitted system.
 
 struct BatchSys {
     long long bead_off;    // offset into the bead arena
@@ -73,6 +74,13 @@ class BatchEngine {
     int64_t admit(const SystemDesc& d, const double* pos, const double* vel, double T,
                   double friction, double dt, int32_t seed, int64_t n_steps, int64_t steps_done = 0);
     int32_t slot_status(int64_t slot);
+    // Device-to-device state exchange of one slot with buffers of the same
+    // device (the plain context's one-system fast path): positions (FP64
+    // SoA), velocities (FP32 SoA), the step counter and the step target.
+    // Both wait for the batch's stream; the copies are complete on return.
+    void load_state_device(int64_t slot, const double* x, const double* y, const double* z, const float* vx,
+                           const float* vy, const float* vz, uint64_t steps_done, uint64_t steps_target);
+    void store_state_device(int64_t slot, double* x, double* y, double* z, float* vx, float* vy, float* vz);
     void run(int32_t steps_per_launch, bool sync);
     void finished(int64_t* slots, int64_t cap, int64_t* n_out);
     void get_positions(int64_t slot, double* xyz);

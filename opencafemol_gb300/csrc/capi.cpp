@@ -503,6 +503,7 @@ int ocm_context_minimize(ocm_context* ctx, double tolerance, int64_t max_iterati
     CTX_CALL(const int64_t it = ctx->c->minimize(tolerance, max_iterations);
              if (iterations_out) *iterations_out = it);
 }
+int ocm_context_set_engine(ocm_context* ctx, int32_t mode) { CTX_CALL(ctx->c->set_engine(mode)); }
 int ocm_context_minimize_report(ocm_context* ctx, int32_t* reason, double* rms_force) {
     CTX_CALL(need(reason, "reason"); const auto& c = *ctx->c;
              if (c.min_reason < 0) throw ocm::Error(5, "[error] no minimisation has run on this context");
@@ -515,7 +516,7 @@ int ocm_context_get_stats(ocm_context* ctx, ocm_context_stats* out) {
              out->reordered = c.reorder ? 1 : 0; out->skin = c.skin;
              out->max_cutoff = c.cs.max_cutoff; out->tile_cutoff = c.tile_cutoff();
              out->charged_pairs = c.charged_pairs(); out->charged_split = c.charged_split() ? 1 : 0;
-             out->reserved_ = 0);
+             out->one_system = c.last_step_one_system() ? 1 : 0);
 }
 int ocm_context_set_list_options(ocm_context* ctx, int32_t interval, double skin) {
     CTX_CALL(ctx->c->set_list_options(interval, skin));

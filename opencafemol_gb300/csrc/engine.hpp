@@ -60,6 +60,8 @@ struct ListFlags {
     enum : int { kTileOverflow = 1, kMaskOverflow = 2, kSkinViolation = 4, kChargedOverflow = 8, kBlownUp = 16 };
 };
 
+class BatchEngine;
+
 // Device-resident single system, the part of an OpenMM Context + Langevin
 // integrator that the reference drives through Simulator::run.
 class PlainContext {
@@ -76,6 +78,15 @@ class PlainContext {
     void group_energies(double* energies32);
     double kinetic_energy();
     void step(int64_t n);
+    // Engine of step(): kEngineAuto runs a non-periodic system of at most
+    // kOneSystemMaxBeads beads as a one-system persistent launch of the
+    // batched kernel (one SM: no per-step launches, no grid-wide list
+    // build) and every other system on the cluster-pair tiles;
+    // kEngineTiles / kEngineOneSystem force one or the other.
+    enum { kEngineAuto = 0, kEngineTiles = 1, kEngineOneSystem = 2 };
+    static constexpr int64_t kOneSystemMaxBeads = 512;
+    void set_engine(int32_t mode);
+    bool last_step_one_system() const { return last_step_one_system_; }
     void set_list_options(int32_t interval, double skin);
     void list_pairs(int64_t* out, int64_t cap, int64_t* n_out);
     void cluster_order(int64_t* out, int64_t cap, int64_t* n_out);
@@ -117,6 +128,17 @@ class PlainContext {
     void set_positions_internal(const double* xyz);
     void set_positions_impl(const double* xyz, bool retune);
 
+    bool one_system_eligible();
+    void step_one_system(int64_t nsteps);
+
+    SystemDesc desc_;  // kept for the one-system batch
+    int32_t engine_mode_ = kEngineAuto;
+    std::unique_ptr<BatchEngine> one_;
+    int64_t one_slot_ = -1;
+    bool one_refused_ = false;  // the batched kernel does not take this system
+    bool last_step_one_system_ = false;
+    int32_t one_seed_ = 0;
+    double one_T_ = 0, one_friction_ = 0, one_dt_ = 0;
     cudaStream_t stream_ = nullptr;
     std::map<int, cudaGraphExec_t> graphs_;
     bool positions_set_ = false;

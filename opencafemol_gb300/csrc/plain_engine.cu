@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "batch_engine.hpp"
 #include "device_math.cuh"
 #include "engine.hpp"
 
@@ -1090,7 +1091,7 @@ __global__ void k_positions_to_float(int n, const double* __restrict__ x,
                          __double2float_rn(__dsub_rn(w[2], (double)p.z)), 0.f);
 }
 
-__global__ void k_advance(unsigned long long* step_base, int k) { *step_base += (unsigned long long)k; }
+__global__ void k_advance(unsigned long long* step_base, unsigned long long k) { *step_base += k; }
 
 __global__ void k_velocity_init(int n, const float* __restrict__ invm, float kT, uint32_t seed,
                                 uint32_t stream, float* vx, float* vy, float* vz) {
@@ -1186,6 +1187,11 @@ PlainContext::PlainContext(const SystemDesc& d, double temperature, double frict
     if (!(friction >= 0)) throw Error(1, "[error] friction must be >= 0");
     if (!(temperature >= 0)) throw Error(1, "[error] temperature must be >= 0");
     cs = compile_system(d);
+    desc_ = d;
+    one_seed_ = seed;
+    one_T_ = temperature;
+    one_friction_ = friction;
+    one_dt_ = dt;
     n = cs.n;
     if (n <= 0) throw Error(1, "[error] system has no particles");
     if (n > (1 << 27)) throw Error(6, "[error] system too large");
@@ -1763,7 +1769,7 @@ cudaGraphExec_t PlainContext::graph_for(int chunk) {
             launch_forces(stream_, false, all, r);
             launch_integrate(stream_, r);
         }
-        k_advance<<<1, 1, 0, stream_>>>(step_base_.p, chunk);
+        k_advance<<<1, 1, 0, stream_>>>(step_base_.p, (unsigned long long)chunk);
     } catch (...) {
         cudaStreamEndCapture(stream_, &g);
         throw;
@@ -1776,11 +1782,81 @@ cudaGraphExec_t PlainContext::graph_for(int chunk) {
     return exec;
 }
 
+void PlainContext::set_engine(int32_t mode) {
+    if (mode != kEngineAuto && mode != kEngineTiles && mode != kEngineOneSystem)
+        throw Error(1, "[error] engine must be 0 (auto), 1 (tiles) or 2 (one-system batched kernel)");
+    if (mode == kEngineOneSystem && (cs.periodic || n > 2048))
+        throw Error(6, "[error] the one-system batched kernel runs non-periodic systems of at most 2048 beads");
+    engine_mode_ = mode;
+}
+
+bool PlainContext::one_system_eligible() {
+    if (engine_mode_ == kEngineTiles || one_refused_) return false;
+    if (cs.periodic) return false;
+    for (const auto& b : cs.bonds)
+        if (b.periodic) return false;
+    return engine_mode_ == kEngineOneSystem || n <= kOneSystemMaxBeads;
+}
+
+// step() on the batched kernel as a one-system persistent launch: the
+// context's positions, velocities and step counter go device-to-device into
+// a one-slot batch, which runs the steps in shared memory on one SM, and
+// come back.  The Langevin noise is the same counter-based stream (seed,
+// bead, step) as on the tiles, so the physics is the same and only FP32
+// rounding differs.  The first call builds the batch (a host copy of the
+// state for the admission); a system the batched kernel does not take goes
+// to the tiles from then on.
+void PlainContext::step_one_system(int64_t nsteps) {
+    OCM_CK(cudaStreamSynchronize(stream_));
+    if (!one_) {
+        std::vector<double> x(3 * n), v(3 * n);
+        get_positions(x.data());
+        get_velocities(v.data());
+        const int64_t fp = BatchEngine::footprint(desc_);
+        const int64_t arena = std::max<int64_t>(n, fp / 256 + 64);
+        auto b = std::make_unique<BatchEngine>(device, 1, arena, (int32_t)n);
+        one_slot_ = b->admit(desc_, x.data(), v.data(), one_T_, one_friction_, one_dt_, one_seed_, 0, 0);
+        one_ = std::move(b);
+    }
+    unsigned long long base = 0;
+    OCM_CK(cudaMemcpy(&base, step_base_.p, sizeof(base), cudaMemcpyDeviceToHost));
+    one_->load_state_device(one_slot_, x_.p, y_.p, z_.p, vx_.p, vy_.p, vz_.p, base, base + (uint64_t)nsteps);
+    for (int64_t left = nsteps; left > 0;) {
+        const int32_t chunk = (int32_t)std::min<int64_t>(left, 4096);
+        one_->run(chunk, false);
+        left -= chunk;
+    }
+    if (one_->slot_status(one_slot_) != 0)
+        throw Error(7, "[error] the system blew up (a non-finite force, velocity or position, or a force of "
+                       "1e9 kJ/mol/nm or more); the context keeps its state from before this step call");
+    one_->store_state_device(one_slot_, x_.p, y_.p, z_.p, vx_.p, vy_.p, vz_.p);
+    k_advance<<<1, 1, 0, stream_>>>(step_base_.p, (unsigned long long)nsteps);
+    OCM_CK(cudaGetLastError());
+    k_positions_to_float<<<div_up(n, 256), 256, 0, stream_>>>(
+        (int)n, x_.p, y_.p, z_.p, 0, cs.box[0], cs.box[1], cs.box[2], 0.0, 0.0, 0.0, xq_.p, xlo_.p);
+    OCM_CK(cudaGetLastError());
+    OCM_CK(cudaStreamSynchronize(stream_));
+    steps_done += nsteps;
+    last_step_one_system_ = true;
+}
+
 void PlainContext::step(int64_t nsteps) {
     OCM_CK(cudaSetDevice(device));
     check_positions_set();
     if (nsteps < 0) throw Error(1, "[error] negative step count");
     if (nsteps == 0) return;
+    if (one_system_eligible()) {
+        try {
+            step_one_system(nsteps);
+            return;
+        } catch (const Error& e) {
+            // a system the batched kernel does not take (shared memory,
+            // list capacity) runs on the tiles; other errors propagate
+            if (one_ || (e.code != 3 && e.code != 6) || engine_mode_ == kEngineOneSystem) throw;
+            one_refused_ = true;
+        }
+    }
+    last_step_one_system_ = false;
     if (graphs_.empty()) ensure_capacity();
     for (int attempt = 0; attempt < 12; ++attempt) {
         cudaStream_t s = stream_;

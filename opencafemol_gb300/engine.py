@@ -20,13 +20,26 @@ ALL_GROUPS = 0xFFFFFFFF
 
 
 class Context:
-    def __init__(self, system: System, integrator: LangevinIntegrator, device: int = 0):
+    """OpenMM's Context + LangevinIntegrator as the reference's Simulator
+    drives them.  ``engine`` picks the kernels of ``step``: "auto" (a
+    non-periodic system of at most 512 beads as a one-system persistent
+    launch of the batched kernel, anything else on the cluster-pair tiles),
+    "tiles" or "one_system"."""
+
+    ENGINES = {"auto": 0, "tiles": 1, "one_system": 2}
+
+    def __init__(self, system: System, integrator: LangevinIntegrator, device: int = 0, engine: str = "auto"):
         self.system = system  # keeps the system alive
         self.n = system.n
         h = C.c_void_p()
         check(lib.ocm_context_create(system.handle, integrator.temperature, integrator.friction,
                                      integrator.step_size, integrator.seed, int(device), C.byref(h)))
         self._h = h
+        if engine != "auto":
+            self.set_engine(engine)
+
+    def set_engine(self, engine: str) -> None:
+        check(lib.ocm_context_set_engine(self._h, Context.ENGINES[engine]))
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -100,7 +100,7 @@ def test_batch_matches_plain_after_one_step(gpu):
     b = gpu.Batch(max_systems=1, max_total_beads=512, max_beads_per_system=512)
     slot = b.admit(system, s.pos, velocities=v0, temperature=s.temperature, seed=77, n_steps=1)
     b.run(1)
-    ctx = gpu.Context(system, gpu.LangevinIntegrator(s.temperature, s.friction, s.dt, 77))
+    ctx = gpu.Context(system, gpu.LangevinIntegrator(s.temperature, s.friction, s.dt, 77), engine="tiles")
     ctx.setPositions(s.pos)
     ctx.setVelocities(v0)
     ctx.step(1)

@@ -32,10 +32,11 @@ def test_plain_get_state_reports_blow_up(gpu):
     assert np.all(np.isfinite(f)) and np.isfinite(e)
 
 
-def test_plain_step_reports_blow_up_and_keeps_state(gpu):
+@pytest.mark.parametrize("engine", ["tiles", "one_system"])
+def test_plain_step_reports_blow_up_and_keeps_state(gpu, engine):
     from opencafemol_gb300 import synth
     spec, x = _overlapping()
-    ctx = gpu.Context(synth.build_system(spec), gpu.LangevinIntegrator(300.0, 0.1, 0.01, 3))
+    ctx = gpu.Context(synth.build_system(spec), gpu.LangevinIntegrator(300.0, 0.1, 0.01, 3), engine=engine)
     ctx.setPositions(x)
     ctx.setVelocitiesToTemperature(300.0, 4)
     v0 = ctx.getVelocities()

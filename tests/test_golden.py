@@ -129,11 +129,13 @@ def test_trajectories_match_fixture(gpu):
     spec, d, _ = _load("sh3_aicg2")
     steps, seed = (int(v) for v in d["traj_meta"])
     system = synth.build_system(spec)
-    ctx = gpu.Context(system, gpu.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, seed))
-    ctx.setPositions(spec.pos)
-    ctx.setVelocities(np.zeros_like(spec.pos))
-    ctx.step(steps)
-    assert np.max(np.abs(ctx.getPositions() - d["traj_pos"])) <= 1e-5
+    for engine in ("tiles", "one_system"):
+        ctx = gpu.Context(system, gpu.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, seed),
+                          engine=engine)
+        ctx.setPositions(spec.pos)
+        ctx.setVelocities(np.zeros_like(spec.pos))
+        ctx.step(steps)
+        assert np.max(np.abs(ctx.getPositions() - d["traj_pos"])) <= 1e-5, engine
     b = gpu.Batch(max_systems=1, max_total_beads=128, max_beads_per_system=128)
     slot = b.admit(system, spec.pos, velocities=np.zeros_like(spec.pos), temperature=spec.temperature,
                    friction=spec.friction, step_size=spec.dt, seed=seed, n_steps=steps)

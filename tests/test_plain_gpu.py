@@ -15,10 +15,11 @@ FORCE_TOL = 1e-4
 ENERGY_TOL = 1e-5
 
 
-def _ctx(ocm, spec, seed=7):
+def _ctx(ocm, spec, seed=7, engine="tiles"):
     from opencafemol_gb300 import synth
     system = synth.build_system(spec)
-    ctx = ocm.Context(system, ocm.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, seed))
+    ctx = ocm.Context(system, ocm.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, seed),
+                      engine=engine)
     ctx.setPositions(spec.pos)
     return system, ctx
 
@@ -207,13 +208,15 @@ def test_cluster_order_deterministic(gpu):
     assert np.median(ext[:, 2]) < 4.0
 
 
-def test_langevin_one_step(gpu):
+@pytest.mark.parametrize("engine", ["tiles", "one_system"])
+def test_langevin_one_step(gpu, engine):
     """x(t+dt), v(t+dt/2) after one step against the oracle's Langevin
-    update fed with the oracle's forces and the same Philox stream."""
+    update fed with the oracle's forces and the same Philox stream (both
+    engines of step)."""
     from opencafemol_gb300 import synth
     from oracle import oracle
     spec = synth.go_protein(120, 11)
-    system, ctx = _ctx(gpu, spec, seed=1234)
+    system, ctx = _ctx(gpu, spec, seed=1234, engine=engine)
     rng = np.random.default_rng(0)
     v0 = rng.normal(scale=0.1, size=(spec.n, 3)).astype(np.float32).astype(np.float64)
     ctx.setVelocities(v0)
@@ -226,24 +229,26 @@ def test_langevin_one_step(gpu):
     assert np.max(np.abs(x1 - xr)) <= 1e-6
 
 
-def test_trajectory_deterministic(gpu):
+@pytest.mark.parametrize("engine", ["tiles", "one_system"])
+def test_trajectory_deterministic(gpu, engine):
     from opencafemol_gb300 import synth
     spec = synth.go_protein(150, 12)
     runs = []
     for _ in range(2):
-        _, ctx = _ctx(gpu, spec, seed=99)
+        _, ctx = _ctx(gpu, spec, seed=99, engine=engine)
         ctx.setVelocitiesToTemperature(spec.temperature, 5)
         ctx.step(200)
         runs.append(ctx.getPositions())
     assert np.array_equal(runs[0], runs[1])
 
 
-def test_temperature_equilibrates(gpu):
+@pytest.mark.parametrize("engine", ["tiles", "one_system"])
+def test_temperature_equilibrates(gpu, engine):
     """<KE> -> 3N/2 kT for Langevin dynamics at the bath temperature."""
     from opencafemol_gb300 import synth
     spec = synth.go_protein(200, 13)
     spec.friction = 1.0
-    _, ctx = _ctx(gpu, spec, seed=3)
+    _, ctx = _ctx(gpu, spec, seed=3, engine=engine)
     ctx.setVelocitiesToTemperature(spec.temperature, 4)
     ctx.step(2000)
     kes = []
@@ -315,3 +320,52 @@ def test_lj_same_sigma_path_bit_identical(gpu):
     assert far.sum() > 0.9 * spec.n
     assert np.array_equal(f_same[far], f_gen[far])
     assert not np.array_equal(f_same[k], f_gen[k])
+
+
+def test_one_system_engine_is_the_batched_kernel(gpu):
+    """A small non-periodic context steps on the batched kernel by default:
+    the trajectory equals a one-slot batch's bit for bit, does not depend
+    on how the steps are chunked into step calls, and evaluations between
+    step calls see the current state."""
+    from opencafemol_gb300 import synth
+    spec = synth.go_protein(180, 14)
+    system = synth.build_system(spec)
+    v0 = np.random.default_rng(3).normal(scale=0.2, size=(spec.n, 3)).astype(np.float32).astype(np.float64)
+    b = gpu.Batch(max_systems=1, max_total_beads=256, max_beads_per_system=256)
+    slot = b.admit(system, spec.pos, velocities=v0, temperature=spec.temperature, friction=spec.friction,
+                   step_size=spec.dt, seed=41, n_steps=300)
+    b.run(300)
+    runs = []
+    for chunks in ([300], [1, 99, 200]):
+        ctx = gpu.Context(system, gpu.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, 41))
+        ctx.setPositions(spec.pos)
+        ctx.setVelocities(v0)
+        for c in chunks:
+            ctx.step(c)
+            f, e = ctx.getState()
+            assert np.all(np.isfinite(f)) and np.isfinite(e)
+        st = ctx.stats()
+        assert st["one_system"] == 1 and st["steps_done"] == 300
+        runs.append((ctx.getPositions(), ctx.getVelocities()))
+    for x, v in runs:
+        assert np.array_equal(x, b.positions(slot)) and np.array_equal(v, b.velocities(slot))
+
+
+def test_engine_choice(gpu):
+    """Periodic systems and systems above 512 beads stay on the tiles by
+    default; the one-system kernel refuses periodic systems."""
+    from opencafemol_gb300 import synth
+    big = synth.go_protein(600, 15)
+    _, ctx = _ctx(gpu, big, engine="auto")
+    ctx.step(5)
+    assert ctx.stats()["one_system"] == 0
+    ctx.set_engine("one_system")
+    ctx.step(5)
+    assert ctx.stats()["one_system"] == 1 and ctx.stats()["steps_done"] == 10
+    slab = synth.hps_slab(4, 50, (12.0, 12.0, 30.0), slab_width=10.0, seed=17)
+    _, cp = _ctx(gpu, slab, engine="auto")
+    cp.step(3)
+    assert cp.stats()["one_system"] == 0
+    with pytest.raises(gpu.OCMError) as ei:
+        cp.set_engine("one_system")
+    assert ei.value.code == 6

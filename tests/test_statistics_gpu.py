@@ -67,7 +67,8 @@ def _plain_samples(gpu, spec):
     system = synth.build_system(spec)
     out = np.zeros((REPLICAS, SAMPLES, 3))
     for k in range(REPLICAS):
-        ctx = gpu.Context(system, gpu.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, 700 + k))
+        ctx = gpu.Context(system, gpu.LangevinIntegrator(spec.temperature, spec.friction, spec.dt, 700 + k),
+                          engine="tiles")
         ctx.setPositions(spec.pos)
         ctx.setVelocities(_mb_velocities(spec, 100 + k))
         ctx.step(EQUIL)
