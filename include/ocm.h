@@ -369,6 +369,14 @@ int ocm_batch_run(ocm_batch* batch, int32_t steps_per_launch, int sync);
  * every step done, or stopped because the system blew up (see
  * ocm_batch_slot_status). */
 int ocm_batch_finished(ocm_batch* batch, int64_t* slots, int64_t capacity, int64_t* n_out);
+/* Balanced launches (on != 0; off by default): in each ocm_batch_run the
+ * costliest unfinished system advances steps_per_launch steps and every
+ * other one proportionally more (by its bead count, up to 64x), so that a
+ * launch keeps every SM busy until its end instead of waiting for the
+ * largest system.  A system's trajectory does not depend on how its steps
+ * are split into launches.  Meant for a serving loop; the ensemble
+ * benchmark keeps every system in step. */
+int ocm_batch_set_balanced(ocm_batch* batch, int on);
 /* Wait for the last launch; *status = OCM_OK, or OCM_ERR_NONFINITE if the
  * slot's system blew up (it is no longer advanced; its state is the one of
  * the failing step).  The reference terminates the whole run in that case

@@ -61,6 +61,7 @@ __host__ __device__ __forceinline__ int pair_split(int n) {
 struct BatchArgs {
     BatchSys* sys;
     const int32_t* order;
+    const int32_t* order_k;      // steps of each claimed system this launch, or null: k for all
     int n_order;
     int* head;
     double *x, *y, *z;
@@ -641,7 +642,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
         int K = 1;
         if (INTEGRATE) {
             const unsigned long long left = R.steps_target > step0 ? R.steps_target - step0 : 0ull;
-            K = (int)min((unsigned long long)a.k, left);
+            K = (int)min((unsigned long long)(a.order_k ? a.order_k[q] : a.k), left);
         }
         const uint32_t slots_en = INTEGRATE ? 0xffffffffu : a.slots_enabled;
         uint32_t excl_all = 0u;
@@ -1196,6 +1197,7 @@ BatchEngine::BatchEngine(int device, int64_t max_systems, int64_t max_beads, int
     sys_.alloc(max_systems);
     OCM_CK(cudaMemset(sys_.p, 0, sizeof(BatchSys) * max_systems));
     order_.alloc(max_systems);
+    order_k_.alloc(max_systems);
     head_.alloc(1);
     energy_.alloc(max_systems * kNumSlots);
     forces_.alloc(3 * nmax_);
@@ -1424,7 +1426,7 @@ int64_t BatchEngine::admit(const SystemDesc& d, const double* pos, const double*
 }
 
 void BatchEngine::launch(bool integrate, bool energy, int k, const std::vector<int32_t>& order,
-                         cudaStream_t s) {
+                         cudaStream_t s, const std::vector<int32_t>* order_k) {
     bool general = false;
     int terms = 0;
     size_t bonded_max = 0;
@@ -1443,10 +1445,14 @@ void BatchEngine::launch(bool integrate, bool energy, int k, const std::vector<i
                        "create the batch with a smaller per-system bead limit");
     OCM_CK(cudaMemcpyAsync(order_.p, order.data(), order.size() * sizeof(int32_t),
                            cudaMemcpyHostToDevice, s));
+    if (order_k)
+        OCM_CK(cudaMemcpyAsync(order_k_.p, order_k->data(), order_k->size() * sizeof(int32_t),
+                               cudaMemcpyHostToDevice, s));
     OCM_CK(cudaMemsetAsync(head_.p, 0, sizeof(int32_t), s));
     BatchArgs a{};
     a.sys = sys_.p;
     a.order = order_.p;
+    a.order_k = order_k ? order_k_.p : nullptr;
     a.n_order = (int)order.size();
     a.head = head_.p;
     a.x = x_.p; a.y = y_.p; a.z = z_.p;
@@ -1477,17 +1483,28 @@ void BatchEngine::run(int32_t k, bool sync) {
             order.push_back((int32_t)s);
     std::stable_sort(order.begin(), order.end(),
                      [&](int32_t a, int32_t b) { return slots_[a].cost > slots_[b].cost; });
+    // Balanced launches: the costliest system does k steps, every other one
+    // as many more as its lower cost allows in the same time (a system's
+    // trajectory does not depend on how its steps are split into launches).
+    std::vector<int32_t> ks(order.size(), k);
+    if (balanced_ && !order.empty()) {
+        const double ref = step_cost(slots_[order.front()].n);
+        for (size_t q = 0; q < order.size(); ++q)
+            ks[q] = (int32_t)std::min<double>(64.0 * k, std::max(1.0, std::floor(k * ref / step_cost(slots_[order[q]].n))));
+    }
     OCM_CK(cudaStreamWaitEvent(stream_, ev_copy_, 0));
     OCM_CK(cudaEventRecord(ev0_, stream_));
-    if (!order.empty()) launch(true, false, k, order, stream_);
+    if (!order.empty()) launch(true, false, k, order, stream_, balanced_ ? &ks : nullptr);
     OCM_CK(cudaEventRecord(ev1_, stream_));
     OCM_CK(cudaMemcpy2DAsync(h_overflow_, sizeof(int), &sys_.p[0].overflow, sizeof(BatchSys),
                              sizeof(int), max_systems_, cudaMemcpyDeviceToHost, stream_));
     OCM_CK(cudaMemcpy2DAsync(h_status_, sizeof(int), &sys_.p[0].status, sizeof(BatchSys),
                              sizeof(int), max_systems_, cudaMemcpyDeviceToHost, stream_));
     ran_ = true;
-    for (int32_t q : order)
-        slots_[q].steps_done = std::min<uint64_t>(slots_[q].steps_target, slots_[q].steps_done + k);
+    for (size_t q = 0; q < order.size(); ++q) {
+        Slot& S = slots_[order[q]];
+        S.steps_done = std::min<uint64_t>(S.steps_target, S.steps_done + (uint64_t)ks[q]);
+    }
     if (sync) OCM_CK(cudaStreamSynchronize(stream_));
 }
 

@@ -6,6 +6,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <map>
 #include <vector>
@@ -92,6 +93,9 @@ class BatchEngine {
     double last_run_ms();
     void set_threads(int threads);  // 256/512/1024 (autotuner)
     void set_list_smem(int kib);    // -1 = all that fits (autotuner)
+    // Balanced launches (the serving loop): the costliest resident system
+    // does steps_per_launch steps, the others proportionally more.
+    void set_balanced(bool on) { balanced_ = on; }
     void slot_stats(int64_t slot, int32_t* builds, int32_t* capacity);
     void set_positions_many(int64_t n, const int64_t* slots, const double* xyz, const double* v);
     void get_positions_many(int64_t n, const int64_t* slots, double* xyz);
@@ -116,7 +120,11 @@ class BatchEngine {
     void grow_lists();
     void sync_steps();
     void launch(bool integrate, bool energy, int k, const std::vector<int32_t>& order,
-                cudaStream_t s);
+                cudaStream_t s, const std::vector<int32_t>* order_k = nullptr);
+    // Estimated time of one MD step of an n-bead system (arbitrary units):
+    // the kernel's per-step time grows with n, with a floor set by the
+    // per-step barriers of small systems.
+    static double step_cost(int64_t n) { return (double)std::max<int64_t>(n, 150); }
     size_t smem_bytes(int nmax, bool general) const;
 
     int device_;
@@ -137,7 +145,8 @@ class BatchEngine {
     int* h_overflow_ = nullptr;  // pinned copy of the records' overflow flags
     int* h_status_ = nullptr;    // pinned copy of the records' status words
     DevBuf<BatchSys> sys_;
-    DevBuf<int32_t> order_, head_;
+    DevBuf<int32_t> order_, order_k_, head_;
+    bool balanced_ = false;
     DevBuf<double> energy_;
     DevBuf<float> forces_;
     // staging of the many-slot state copies (grown on demand)

@@ -286,6 +286,11 @@ class Batch:
     def set_list_smem(self, kib: int) -> None:
         check(lib.ocm_batch_set_list_smem(self._h, int(kib)))
 
+    def set_balanced(self, on: bool = True) -> None:
+        """Balanced launches: the costliest system does the launch's steps,
+        smaller ones proportionally more (for a serving loop)."""
+        check(lib.ocm_batch_set_balanced(self._h, int(bool(on))))
+
     DEFAULT_TUNE_CANDIDATES = ((512, 96), (1024, 96), (512, -1), (1024, -1), (256, 96))
 
     def autotune(self, steps_per_trial: int = 50, candidates=DEFAULT_TUNE_CANDIDATES) -> dict:

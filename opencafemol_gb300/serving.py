@@ -2,12 +2,20 @@
 
 Requests (one coarse-grained system each, with its own temperature, seed
 and step count) arrive over time.  The loop admits waiting requests while
-their device footprint fits the batch's free bead capacity and free slots,
-advances every resident system by one chunk of steps with one launch,
-retires finished systems (freeing their capacity for the next admissions)
-and records each request's completion latency.  Admission happens between
-chunks while every other system stays resident on the device, so new work
-overlaps with work already running.
+their device footprint (``ocm_batch_footprint``: parameters, lists and bead
+state) fits the device-memory budget and the batch has a free slot and bead
+capacity, advances every resident system with one launch per chunk,
+retires finished systems (freeing their memory for the next admissions)
+and records each request's completion latency.  Admission happens while a
+chunk runs and every other system stays resident on the device, so new
+work overlaps with work already running.
+
+Launches are balanced: the largest resident system advances
+``chunk_steps`` steps per launch and smaller ones proportionally more, so
+one large request does not hold every small one to its pace (each
+trajectory is independent of how its steps are split into launches).  A
+system that blows up is retired as failed and its request completes with
+``failed = True``.
 """
 from __future__ import annotations
 
@@ -37,6 +45,8 @@ class Request:
     admitted_at: float = math.nan
     finished_at: float = math.nan
     result: np.ndarray | None = None
+    failed: bool = False
+    footprint: int = -1     # device bytes in a batch (computed at the first admission attempt)
 
     @property
     def beads(self) -> int:
@@ -55,6 +65,10 @@ class ServeStats:
     latencies_s: list = field(default_factory=list)
     chunks: int = 0
     max_resident: int = 0
+    hbm_budget_bytes: int | None = None
+    peak_resident_bytes: int = 0
+    waits_for_memory: int = 0   # admission attempts deferred by the budget
+    failed: int = 0
 
     def summary(self) -> dict:
         lat = np.array(self.latencies_s)
@@ -62,18 +76,26 @@ class ServeStats:
                 "bead_steps_per_s": self.bead_steps / self.wall_s if self.wall_s > 0 else None,
                 "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
                 "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
-                "chunks": self.chunks, "max_resident": self.max_resident}
+                "chunks": self.chunks, "max_resident": self.max_resident,
+                "hbm_budget_bytes": self.hbm_budget_bytes, "peak_resident_bytes": self.peak_resident_bytes,
+                "waits_for_memory": self.waits_for_memory, "failed": self.failed}
 
 
 class Server:
-    """Owns a Batch and runs a request stream through it."""
+    """Owns a Batch and runs a request stream through it.
+
+    ``hbm_budget_bytes``: device memory the resident systems may occupy
+    together (their footprints); None = only the batch's own capacity."""
 
     def __init__(self, max_systems: int, max_total_beads: int, max_beads_per_system: int,
-                 chunk_steps: int = 200, device: int = 0, keep_results: bool = False):
+                 chunk_steps: int = 200, device: int = 0, keep_results: bool = False,
+                 hbm_budget_bytes: int | None = None, balanced: bool = True):
         self.batch = Batch(max_systems, max_total_beads, max_beads_per_system, device=device)
+        self.batch.set_balanced(balanced)
         self.chunk_steps = chunk_steps
         self.max_systems = max_systems
         self.keep_results = keep_results
+        self.hbm_budget_bytes = hbm_budget_bytes
 
     def serve(self, requests: list[Request], realtime: bool = True) -> ServeStats:
         """Run the stream.  With realtime=True requests become visible at
@@ -83,7 +105,10 @@ class Server:
         resident: dict[int, Request] = {}
         done = 0
         nxt = 0
-        stats = ServeStats(requests=len(queue), wall_s=0.0, bead_steps=0.0)
+        stats = ServeStats(requests=len(queue), wall_s=0.0, bead_steps=0.0,
+                           hbm_budget_bytes=self.hbm_budget_bytes)
+        footprint: dict[int, int] = {}   # slot -> device bytes
+        resident_bytes = 0
         t0 = time.perf_counter()
         while done < len(queue):
             now = time.perf_counter() - t0 if realtime else math.inf
@@ -99,6 +124,15 @@ class Server:
                 ran = True
             while waiting and len(resident) < self.max_systems:
                 r = waiting[0]
+                if r.footprint < 0:
+                    r.footprint = Batch.footprint(r.system)
+                need = r.footprint
+                if self.hbm_budget_bytes is not None and resident_bytes + need > self.hbm_budget_bytes:
+                    if not resident:
+                        raise OCMError(3, f"request {r.rid} needs {need} bytes, more than the whole "
+                                          f"budget of {self.hbm_budget_bytes}")
+                    stats.waits_for_memory += 1
+                    break  # wait for a retirement to free memory
                 try:
                     slot = self.batch.admit(r.system, r.positions, temperature=r.temperature,
                                             friction=r.friction, step_size=r.step_size,
@@ -109,8 +143,11 @@ class Server:
                     raise
                 r.admitted_at = time.perf_counter() - t0
                 resident[slot] = r
+                footprint[slot] = need
+                resident_bytes += need
                 waiting.pop(0)
             stats.max_resident = max(stats.max_resident, len(resident))
+            stats.peak_resident_bytes = max(stats.peak_resident_bytes, resident_bytes)
             if not ran:
                 if not resident and nxt < len(queue) and realtime:
                     time.sleep(max(0.0, queue[nxt].arrival - (time.perf_counter() - t0)))
@@ -120,11 +157,15 @@ class Server:
                     continue
                 r = resident.pop(slot)
                 r.finished_at = time.perf_counter() - t0
+                r.failed = self.batch.status(slot) != 0
                 if self.keep_results:
                     r.result = self.batch.positions(slot)
+                steps = self.batch.steps_done(slot)
                 self.batch.retire(slot)
+                resident_bytes -= footprint.pop(slot)
                 stats.latencies_s.append(r.latency if realtime else r.finished_at)
-                stats.bead_steps += r.beads * r.n_steps
+                stats.bead_steps += r.beads * steps
+                stats.failed += int(r.failed)
                 done += 1
         stats.wall_s = time.perf_counter() - t0
         return stats

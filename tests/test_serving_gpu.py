@@ -52,3 +52,43 @@ def test_many_slot_state_copies(gpu):
     # reversed order round-trips too
     rev = slots[::-1]
     assert np.array_equal(b.get_positions_many(rev), np.concatenate([s.pos + 1.5 for s in specs[::-1]]))
+
+
+def test_admission_by_device_memory_budget(gpu):
+    """With a device-memory budget of about three systems' footprints the
+    server never holds more than the budget, defers admissions until
+    retirements free memory, and every request still completes with the
+    result it has alone."""
+    from opencafemol_gb300 import serving
+    reqs = _requests(10, seed=5)
+    fps = [r.system.footprint() for r in reqs]
+    budget = int(sum(sorted(fps)[-3:]))
+    server = serving.Server(max_systems=16, max_total_beads=16 * 700, max_beads_per_system=700,
+                            chunk_steps=40, keep_results=True, hbm_budget_bytes=budget)
+    st = server.serve(reqs, realtime=False)
+    assert len(st.latencies_s) == 10 and st.failed == 0
+    assert 0 < st.peak_resident_bytes <= budget
+    assert st.waits_for_memory > 0
+    r = reqs[7]
+    alone = gpu.Batch(max_systems=1, max_total_beads=800, max_beads_per_system=700)
+    slot = alone.admit(r.system, r.positions, temperature=r.temperature, seed=r.seed, n_steps=r.n_steps)
+    alone.run(r.n_steps)
+    assert np.array_equal(alone.positions(slot), r.result)
+    tiny = serving.Server(max_systems=4, max_total_beads=4000, max_beads_per_system=700,
+                          hbm_budget_bytes=min(fps) // 2)
+    with pytest.raises(gpu.OCMError):
+        tiny.serve(_requests(2, seed=6), realtime=False)
+
+
+def test_blown_up_request_fails_alone(gpu):
+    """A request whose system blows up completes as failed; the others in
+    the same stream complete normally."""
+    from opencafemol_gb300 import serving
+    reqs = _requests(5, seed=8)
+    x = reqs[2].positions.copy()
+    x[-1] = x[0] + np.array([0.01, 0.0, 0.0])
+    reqs[2].positions = x
+    server = serving.Server(max_systems=8, max_total_beads=4000, max_beads_per_system=700, chunk_steps=30)
+    st = server.serve(reqs, realtime=False)
+    assert st.failed == 1 and len(st.latencies_s) == 5
+    assert [r.failed for r in reqs] == [False, False, True, False, False]
