@@ -39,12 +39,31 @@ def local_device() -> int:
     return int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def _go_specs(params):
+    from opencafemol_gb300 import synth
+    return [synth.go_protein(int(n), int(sd), temperature=float(t)) for n, sd, t in params]
+
+
+def go_specs(params, workers=None):
+    """Seeded Go proteins for (beads, seed, temperature) triples, built in a
+    process pool (spawn: the workers run numpy only and never load the
+    engine library); the result is in the order of ``params``."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    workers = workers or min(16, os.cpu_count() or 1)
+    if len(params) < 32 or workers <= 1:
+        return _go_specs(params)
+    step = -(-len(params) // workers)
+    chunks = [params[i:i + step] for i in range(0, len(params), step)]
+    with cf.ProcessPoolExecutor(len(chunks), mp_context=mp.get_context("spawn")) as ex:
+        return [s for part in ex.map(_go_specs, chunks) for s in part]
+
+
 def ensemble_specs(count=N_SYSTEMS, seed=SEED):
     from opencafemol_gb300 import synth
     sizes = synth.ensemble_sizes(count, SIZE_LO, SIZE_HI, seed)
     temps = synth.ensemble_temperatures(count, seed)
-    return [synth.go_protein(int(n), seed * 1000 + k, temperature=float(t))
-            for k, (n, t) in enumerate(zip(sizes, temps))]
+    return go_specs([(int(n), seed * 1000 + k, float(t)) for k, (n, t) in enumerate(zip(sizes, temps))])
 
 
 class ClockSampler:
@@ -324,10 +343,12 @@ def run_e2e(ocm, synth, specs, systems, args, world):
 
 
 def run_serving(ocm, args):
-    """Continuous batching on a scaled request stream with the serving
-    config's shapes: Go proteins of 30..2000 beads (log-uniform), T~U[280,360],
-    Poisson arrivals at 200 req/s; step counts log-uniform in
-    [1e4, 1e6] / scale."""
+    """Continuous batching on a bounded version of the serving stream: Go
+    proteins of 30..2000 beads (log-uniform), T~U[280,360], Poisson arrivals
+    at 200 req/s, admitted against a device-memory budget; step counts
+    log-uniform in [1e4, 1e6] / scale and --serve-requests requests (the
+    full stream is 10,000 requests at scale 1: about 1e12 bead-steps, some
+    minutes of device time, too long for a benchmark run)."""
     from opencafemol_gb300 import serving, synth
     rng = np.random.default_rng(4242)
     n = args.serve_requests
@@ -336,18 +357,21 @@ def run_serving(ocm, args):
     temps = rng.uniform(280.0, 360.0, n)
     arrivals = serving.poisson_arrivals(n, args.serve_rate, seed=4243)
     reqs = []
-    for k in range(n):
-        spec = synth.go_protein(int(sizes[k]), 90000 + k, temperature=float(temps[k]))
+    specs = go_specs([(int(sizes[k]), 90000 + k, float(temps[k])) for k in range(n)])
+    for k, spec in enumerate(specs):
         reqs.append(serving.Request(rid=k, arrival=float(arrivals[k]), system=synth.build_system(spec),
                                     positions=spec.pos, temperature=float(temps[k]),
                                     n_steps=int(steps[k]), seed=k))
     server = serving.Server(max_systems=512, max_total_beads=300_000, max_beads_per_system=2048,
-                            chunk_steps=args.serve_chunk, device=local_device())
+                            chunk_steps=args.serve_chunk, device=local_device(),
+                            hbm_budget_bytes=int(args.serve_hbm_gib * 2 ** 30))
     st = server.serve(reqs, realtime=True).summary()
     offered = float(np.sum(sizes * steps) / arrivals[-1]) if n > 1 else None
     st.update({"offered_bead_steps_per_s": offered, "rate_req_per_s": args.serve_rate,
                "step_scale": args.serve_step_scale, "chunk_steps": args.serve_chunk,
-               "sizes": "log-uniform [30, 2000]", "steps": f"log-uniform [1e4, 1e6] / {args.serve_step_scale}"})
+               "launches": "balanced (the largest resident system does chunk_steps per launch)",
+               "sizes": "log-uniform [30, 2000]", "steps": f"log-uniform [1e4, 1e6] / {args.serve_step_scale}",
+               "requests_of_the_full_stream": 10000})
     return st
 
 
@@ -546,7 +570,7 @@ def main():
     ap.add_argument("--plain-chunks", type=int, default=2)
     ap.add_argument("--cpu-steps", type=int, default=500)  # MD steps of the whole ensemble, ~2 s
     ap.add_argument("--threads", type=int, default=0)
-    ap.add_argument("--serve-requests", type=int, default=96)
+    ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--traffic-bytes", type=float, default=K_BATCH_DRAM_BYTES,
                     help="DRAM bytes per k_batch launch (ncu), reported as roofline.traffic")
     ap.add_argument("--cfg0-steps", type=int, default=10000)
@@ -554,7 +578,8 @@ def main():
     ap.add_argument("--cfg1-relax", type=int, default=3000)
     ap.add_argument("--cfg2-steps", type=int, default=1000)
     ap.add_argument("--serve-rate", type=float, default=200.0)
-    ap.add_argument("--serve-step-scale", type=int, default=50)
+    ap.add_argument("--serve-step-scale", type=int, default=20)
+    ap.add_argument("--serve-hbm-gib", type=float, default=4.0)
     ap.add_argument("--serve-chunk", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

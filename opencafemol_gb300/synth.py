@@ -123,11 +123,17 @@ def _f32(a: np.ndarray) -> np.ndarray:
     return np.asarray(a, np.float32).astype(np.float64)
 
 
+def _cross(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """a x b of two 3-vectors (the products np.cross forms, without its
+    per-call overhead)."""
+    return np.array([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]])
+
+
 def _orthonormal(b: np.ndarray):
     t = np.array([1.0, 0.0, 0.0]) if abs(b[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
-    u = np.cross(b, t)
+    u = _cross(b, t)
     u /= np.linalg.norm(u)
-    return u, np.cross(b, u)
+    return u, _cross(b, u)
 
 
 def saw_chain(n: int, rng: np.random.Generator, bond: float = 0.38, min_dist: float = 0.45,
