@@ -16,9 +16,8 @@ namespace ocm {
 // ---------------------------------------------------------------------------
 // Fixed-point force accumulation.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned long long to_fixed(float f) {
-    return (unsigned long long)__float2ll_rn(f * kFixedScaleF);
-}
+// round(f * 2^32) as int64 without the FP64 pipe (fixed_point.h).
+__device__ __forceinline__ unsigned long long to_fixed(float f) { return fixed_from_float(f); }
 __device__ __forceinline__ void fixed_add(unsigned long long* p, float f) {
     atomicAdd(p, to_fixed(f));
 }

@@ -1,13 +1,14 @@
-// fixed_point.h - read-out of the 64-bit fixed-point force accumulator
-// (2^32 units per kJ/mol/nm) as FP32, written with integer operations only.
+// fixed_point.h - conversions between FP32 forces and the 64-bit fixed-point
+// force accumulator (2^32 units per kJ/mol/nm), written with 32-bit
+// operations only.
 //
 // On GB300 FP64 arithmetic runs on a narrow pipe; the integrators read every
 // bead's force once per step, and going through a double there
 // ((float)((double)F * 2^-32): an int64->f64 conversion, a multiply and an
 // f64->f32 conversion) costs more than the integer version below, which
-// measured ~2% faster on the batched kernel.  (The other direction,
-// f * 2^32 -> int64, stays one FMUL plus one hardware conversion: an
-// integer restatement of it measured slower.)
+// measured ~2% faster on the batched kernel.  The other direction,
+// fixed_from_float, splits the value at the binary point into two 32-bit
+// conversions.
 //
 //   fixed_to_float(F) == F * 2^-32 correctly rounded to FP32
 //                        (round-half-even), equal to
@@ -52,6 +53,31 @@ OCM_HD float f32_from_bits(uint32_t u) {
     __builtin_memcpy(&f, &u, 4);
     return f;
 #endif
+}
+
+// f * 2^32 rounded to the nearest int64 (ties to even), for |f| < 2^31,
+// with 32-bit operations only.  With a = |f|, a = fl + r where fl =
+// floor(a) and r = a - fl are exact (Sterbenz), so round(a * 2^32) =
+// fl * 2^32 + round(r * 2^32), where r * 2^32 < 2^32 - 128 cannot round up
+// to 2^32 and the tie parity is the low word's; rounding half to even is
+// symmetric, so the sign is applied to the integer.  On GB300 a float ->
+// int64 conversion runs on the narrow FP64 pipe; the two float -> uint32
+// conversions here do not.  Out of range (|f| >= 2^31) or NaN give an
+// unspecified value: the engines flag such forces before they matter.
+OCM_HD unsigned long long fixed_from_float(float f) {
+#if defined(__CUDA_ARCH__)
+    const float a = fabsf(f);
+    const float fl = floorf(a);
+    const unsigned int hi = __float2uint_rz(fl);
+    const unsigned int lo = __float2uint_rn((a - fl) * 4294967296.0f);
+#else
+    const float a = __builtin_fabsf(f);
+    const float fl = __builtin_floorf(a);
+    const unsigned int hi = (unsigned int)fl;
+    const unsigned int lo = (unsigned int)__builtin_llrintf((a - fl) * 4294967296.0f);
+#endif
+    const unsigned long long v = ((unsigned long long)hi << 32) + (unsigned long long)lo;
+    return f < 0.f ? (unsigned long long)0 - v : v;
 }
 
 // F * 2^-32 correctly rounded to FP32.

@@ -39,6 +39,24 @@ int main(int argc, char** argv) {
                 ++n;
             }
         }
+    // fixed_from_float against the C library's round-half-even of f * 2^32
+    std::uniform_real_distribution<double> mag(-30.0, 30.5);
+    for (long long k = 0; k < samples; ++k, ++n) {
+        float f = (float)std::ldexp(1.0 + (double)(g() % (1ull << 23)) / 8388608.0, (int)std::floor(mag(g)));
+        if (g() & 1) f = -f;
+        if (!(std::fabs(f) < 2147483648.0f)) continue;
+        const long long a = (long long)fixed_from_float(f);
+        const long long b = std::llrint((double)f * 4294967296.0);
+        if (a != b && bad++ < 40) std::printf("fixed_from_float %.9g: %lld != %lld\n", f, a, b);
+    }
+    // values whose low word is an exact tie, integers, tiny values, zeros
+    for (float f : {0.0f, -0.0f, 1.0f, -1.0f, 0.5f, -0.5f, 1e-12f, -1e-12f, 2.3283064e-10f, -2.3283064e-10f,
+                    3.4924597e-10f, -3.4924597e-10f, 1.0e9f, -1.0e9f, 2147483520.0f, -2147483648.0f}) {
+        const long long a = (long long)fixed_from_float(f);
+        const long long b = std::llrint((double)f * 4294967296.0);
+        if (a != b && bad++ < 60) std::printf("fixed_from_float %.9g: %lld != %lld\n", f, a, b);
+        ++n;
+    }
     std::printf("checked %lld cases, %lld mismatches\n", n, bad);
     return bad == 0 ? 0 : 1;
 }

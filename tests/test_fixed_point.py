@@ -16,6 +16,6 @@ def test_fixed_point_conversions(tmp_path):
     exe = tmp_path / "fixed_point_check"
     subprocess.run([gxx, "-O2", "-std=c++17", "-I", str(ROOT / "opencafemol_gb300" / "csrc"),
                     str(ROOT / "tests" / "fixed_point_check.cpp"), "-o", str(exe)], check=True)
-    out = subprocess.run([str(exe), "4000000"], capture_output=True, text=True, timeout=300)
+    out = subprocess.run([str(exe), "1500000"], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "0 mismatches" in out.stdout
