@@ -47,7 +47,9 @@ def _go_specs(params):
 def go_specs(params, workers=None):
     """Seeded Go proteins for (beads, seed, temperature) triples, built in a
     process pool (spawn: the workers run numpy only and never load the
-    engine library); the result is in the order of ``params``."""
+    engine library); the result is in the order of ``params``.  As with any
+    spawn pool, a script that calls this must keep its own work under
+    ``if __name__ == "__main__"`` (the workers import the main module)."""
     import concurrent.futures as cf
     import multiprocessing as mp
     workers = workers or min(16, os.cpu_count() or 1)
