@@ -239,14 +239,16 @@ def run_ours(args, rank, world):
     slots = [batch.admit(sysobj, s.pos, temperature=s.temperature, friction=s.friction,
                          step_size=s.dt, seed=1000 + k, n_steps=10 ** 12)
              for k, (sysobj, s) in enumerate(zip(systems, specs))]
-    # the autotuner's trial launches are real steps of the same systems and
-    # serve as part of the warm-up; --threads fixes the shape instead
+    # warm-up launches first, so that the systems have relaxed from their
+    # native structures before the autotuner times launch shapes; its trial
+    # launches are real steps of the same systems; --threads fixes the shape
     tuned = None
     if args.threads:
         batch.set_threads(args.threads)
-    else:
-        tuned = batch.autotune(steps_per_trial=K)
     for _ in range(args.warmup):
+        batch.run(K, sync=True)
+    if not args.threads:
+        tuned = batch.autotune(steps_per_trial=K)
         batch.run(K, sync=True)
 
     import torch
@@ -267,7 +269,9 @@ def run_ours(args, rank, world):
     ms_per_step = dev_time / args.steps * 1e3
 
     # ---- end to end through the public API with host buffers ----
-    e2e = run_e2e(ocm, synth, specs, systems, args, world)
+    shape = ((tuned["threads"], tuned["list_smem_kib"], tuned["split_beads"]) if tuned
+             else (args.threads, -1, None))
+    e2e = run_e2e(ocm, synth, specs, systems, args, world, shape)
 
     # ---- plain single-system path on a sample of the same mix ----
     plain = run_plain(ocm, specs, systems, args) if args.plain_sample > 0 else None
@@ -296,6 +300,8 @@ def run_ours(args, rank, world):
                                    f"largest first onto the least-loaded rank; no collective)"
                                    if world > 1 else "one GPU"),
                    "launch_shape": {"threads_per_cta": batch.threads(), "autotuned": tuned is not None,
+                                    "list_smem_kib": tuned["list_smem_kib"] if tuned else None,
+                                    "split_beads": tuned["split_beads"] if tuned else None,
                                     "trials_ms": [t["ms"] for t in tuned["trials"]] if tuned else None},
                    "l2": "flushed (256 MiB write) between timed launches"},
         "e2e": e2e, "gpu_launches": args.steps, "roofline": roof, "cpu_baseline": cpu,
@@ -308,18 +314,21 @@ def run_ours(args, rank, world):
     return line
 
 
-def run_e2e(ocm, synth, specs, systems, args, world):
+def run_e2e(ocm, synth, specs, systems, args, world, shape):
     """End to end through the public API with host buffers: every step
     uploads every replica's positions and velocities from pinned host memory
     (one copy), runs K MD steps and reads every replica's positions back
-    (one copy)."""
+    (one copy).  ``shape`` = (threads, list KiB, split beads) of the
+    device-timed leg."""
     import torch
     K = args.md_steps
     beads = int(sum(s.n for s in specs))
     batch = ocm.Batch(max_systems=len(specs), max_total_beads=beads + 1024,
                       max_beads_per_system=SIZE_HI, device=local_device())
-    if args.threads:
-        batch.set_threads(args.threads)
+    batch.set_threads(shape[0])
+    batch.set_list_smem(shape[1])
+    if shape[2] is not None:
+        batch.set_split(shape[2])
     slots = [batch.admit(sysobj, s.pos, temperature=s.temperature, step_size=s.dt,
                          seed=17 + k, n_steps=10 ** 12)
              for k, (sysobj, s) in enumerate(zip(systems, specs))]

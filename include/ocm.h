@@ -377,6 +377,13 @@ int ocm_batch_finished(ocm_batch* batch, int64_t* slots, int64_t capacity, int64
  * are split into launches.  Meant for a serving loop; the ensemble
  * benchmark keeps every system in step. */
 int ocm_batch_set_balanced(ocm_batch* batch, int on);
+/* Tuning knob of the persistent kernel (set by the autotuner; results do not
+ * depend on it): when a launch has at least two systems per CTA and the
+ * systems a CTA claims have at most `beads` beads, the CTA splits into two
+ * groups of half its threads, each with half of its shared memory,
+ * advancing two systems at a time (default 384; 0 = never split; capped so
+ * that a system's state fits half of the CTA's shared memory). */
+int ocm_batch_set_split(ocm_batch* batch, int32_t beads);
 /* Wait for the last launch; *status = OCM_OK, or OCM_ERR_NONFINITE if the
  * slot's system blew up (it is no longer advanced; its state is the one of
  * the failing step).  The reference terminates the whole run in that case

@@ -118,6 +118,7 @@ SIGNATURES = {
                                          C.c_int64, C.c_int64, _I64P]),
     "ocm_batch_slot_status": (C.c_int, [_P, C.c_int64, _I32P]),
     "ocm_batch_set_balanced": (C.c_int, [_P, C.c_int]),
+    "ocm_batch_set_split": (C.c_int, [_P, C.c_int32]),
     "ocm_batch_run": (C.c_int, [_P, C.c_int32, C.c_int]),
     "ocm_batch_finished": (C.c_int, [_P, _I64P, C.c_int64, _I64P]),
     "ocm_batch_get_positions": (C.c_int, [_P, C.c_int64, _DP]),

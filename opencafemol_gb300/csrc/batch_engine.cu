@@ -74,7 +74,15 @@ struct BatchArgs {
     uint16_t* lists;             // neighbour-list arena
     uint32_t slots_enabled;
     size_t smem_bytes;           // dynamic shared memory of the launch
+    int split_beads;             // a CTA splits into two groups at systems of at most this many beads (0: never)
+    int split_bead_bytes;        // host side: shared-memory state bytes per bead (caps split_beads)
 };
+
+// Named barrier `bar` over nthreads threads (bar 0 over the whole CTA is
+// __syncthreads).
+__device__ __forceinline__ void bar_sync(int bar, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthreads) : "memory");
+}
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -534,345 +542,405 @@ __device__ __forceinline__ float3 scan_forces(int i, int j0, int j1, int nt, con
     return fa;
 }
 
-constexpr int kMaxBeadsPerThread = 8;  // 2048 beads / 256 threads
-
-template <int THREADS, int TERMS, bool LABELS, bool ENERGY, bool INTEGRATE>
-__global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
-    constexpr int NW = THREADS / 32;
-    constexpr int BPT = (32 * kMaxClusters + THREADS - 1) / THREADS;  // beads per thread
-    extern __shared__ __align__(16) unsigned char smem[];
+// One claimed system (order entry q, slot `slot`) advanced by a group of GT
+// threads (gtid = 0..GT-1) whose barrier is `bar` (0: the whole CTA), in
+// the group's shared memory [gsmem, gsmem + gsmem_bytes), with the group's
+// shared words (s_move[2], s_overflow, s_bad, s_energy[kNumSlots]).
+template <int GT, int TERMS, bool LABELS, bool ENERGY, bool INTEGRATE>
+__device__ __forceinline__ void run_system(const BatchArgs& a, int q, int slot, int gtid, int bar,
+                                           unsigned char* gsmem, size_t gsmem_bytes, int* s_move,
+                                           int* s_overflow, int* s_bad, double* s_energy) {
+    constexpr int NWG = GT / 32;
+    constexpr int BPT = (32 * kMaxClusters + GT - 1) / GT;  // cluster rows per warp in the update
+    const int lane = gtid & 31, gwarp = gtid >> 5;
     const int nmax = a.nmax;  // stride of the global force output
-    __shared__ int s_claim;
-    __shared__ int s_move[2];
-    __shared__ int s_overflow;
-    __shared__ int s_bad;
-    __shared__ double s_energy[kNumSlots];
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float nan = __int_as_float(0x7fc00000);
+    const BatchSys& R = a.sys[slot];
+    const int n = R.n, nt = R.nt, npad = nt * 32;
+    const PairConsts pc = R.pc;
+    const LangevinConsts lc = R.lc;
+    const long long boff = R.bead_off;
+    const unsigned char* blob = a.blob + R.blob_off;
+    const float4* gp0 = reinterpret_cast<const float4*>(blob + R.off_p0);
+    const float4* gp1 = reinterpret_cast<const float4*>(blob + R.off_p1);
+    const uint32_t* glab = reinterpret_cast<const uint32_t*>(blob + R.off_lab);
+    const float* ginvm = reinterpret_cast<const float*>(blob + R.off_invm);
+    // ---- shared-memory layout of this system, arrays of stride ns ----
+    // Positions are float-float: hi parts in sx (pair arithmetic), lo
+    // parts in sxl; x = hi + lo carries ~48 significant bits.  fp / fb:
+    // each bead's pair and bonded force of the current step.
+    const int ns = npad;
+    float* fp = reinterpret_cast<float*>(gsmem);
+    float* fb = reinterpret_cast<float*>(gsmem + 12 * (size_t)ns);
+    float4* sx = reinterpret_cast<float4*>(gsmem + 24 * (size_t)ns);
+    float4* sp0 = reinterpret_cast<float4*>(gsmem + 40 * (size_t)ns);
+    float* sxl = reinterpret_cast<float*>(gsmem + 56 * (size_t)ns);
+    float* sv = reinterpret_cast<float*>(gsmem + 68 * (size_t)ns);
+    float* sim = reinterpret_cast<float*>(gsmem + 80 * (size_t)ns);
+    float* sref = reinterpret_cast<float*>(gsmem + 84 * (size_t)ns);
+    uint16_t* scnt = reinterpret_cast<uint16_t*>(gsmem + 96 * (size_t)ns);
+    size_t off = 98 * (size_t)ns;
+    float4* sp1 = nullptr;
+    uint32_t* slab = nullptr;
+    if ((TERMS & kTermLJA) || LABELS) {
+        sp1 = reinterpret_cast<float4*>(gsmem + off);
+        slab = reinterpret_cast<uint32_t*>(gsmem + off + 16 * (size_t)ns);
+        off += 20 * (size_t)ns;
+    }
+    float4* bc = reinterpret_cast<float4*>(gsmem + off);
+    float4* bh = bc + nt;
+    off += 32 * (size_t)nt;
+    float3* carry = reinterpret_cast<float3*>(gsmem + off);
+    off += 36 * (size_t)nt;
+    off = (off + 15) & ~(size_t)15;
+    uint16_t* sseg = reinterpret_cast<uint16_t*>(gsmem + off);
+    off += 2 * kMaxUnits;
+    // bonded records and tables: staged in shared memory when they fit,
+    // read from the blob otherwise
+    const unsigned char* gbonded = blob + R.off_bonded;
+    const bool bonded_smem = off + (size_t)R.bonded_bytes <= gsmem_bytes;
+    unsigned char* sbonded = gsmem + off;
+    if (bonded_smem) off += (size_t)R.bonded_bytes;
+    const unsigned char* bsrc = bonded_smem ? sbonded : gbonded;
+    Bonded B;
+    B.bpar = reinterpret_cast<const float4*>(bsrc + R.rb_p);
+    B.bij = reinterpret_cast<const uint32_t*>(bsrc + R.rb_ij);
+    B.aij = reinterpret_cast<const uint2*>(bsrc + R.ra_ij);
+    B.ak = reinterpret_cast<const float*>(bsrc + R.ra_k);
+    B.drec = reinterpret_cast<const uint4*>(bsrc + R.rd);
+    B.gdp = reinterpret_cast<const float2*>(bsrc + R.rgd);
+    B.fla = reinterpret_cast<const FlaTable*>(bsrc + R.rfla);
+    B.fld = reinterpret_cast<const FldTable*>(bsrc + R.rfld);
+    B.cb = reinterpret_cast<const uint16_t*>(bsrc + R.rcb);
+    B.ca = reinterpret_cast<const uint16_t*>(bsrc + R.rca);
+    B.cd = reinterpret_cast<const uint16_t*>(bsrc + R.rcd);
+    B.gs = reinterpret_cast<const uint16_t*>(bsrc + R.rgs);
+    B.gl = reinterpret_cast<const uint32_t*>(bsrc + R.rgl);
+    uint16_t* slist = reinterpret_cast<uint16_t*>(gsmem + off);
+    const size_t list_bytes = gsmem_bytes > off ? gsmem_bytes - off : 0;
+    const int32_t* ex_start = reinterpret_cast<const int32_t*>(blob + R.off_ex_start);
+    const int32_t* exl = reinterpret_cast<const int32_t*>(blob + R.off_ex);
+    uint16_t* glist = a.lists + R.list_off;
+    const int maxn = R.maxn;
+    // entries per bead kept in shared memory (multiple of 4)
+    const int cap_s = min(maxn, (int)(list_bytes / (2 * (size_t)npad)) & ~3);
+    const int S = pair_split(n);
+    const unsigned long long step0 = R.steps_done;
+    int K = 1;
+    if (INTEGRATE) {
+        const unsigned long long left = R.steps_target > step0 ? R.steps_target - step0 : 0ull;
+        K = (int)min((unsigned long long)(a.order_k ? a.order_k[q] : a.k), left);
+    }
+    const uint32_t slots_en = INTEGRATE ? 0xffffffffu : a.slots_enabled;
+    uint32_t excl_all = 0u;
+    if (!(slots_en & (1u << kSlotEXV))) excl_all |= kTermEXV;
+    if (!(slots_en & (1u << kSlotDH))) excl_all |= kTermDH;
+    if (!(slots_en & (1u << kSlotLJR))) excl_all |= kTermLJR;
+    if (!(slots_en & (1u << kSlotLJA))) excl_all |= kTermLJA;
+    const bool pairs_on = (pc.terms & ~excl_all) != 0;
 
-    while (true) {
-        if (tid == 0) {
-            s_claim = atomicAdd(a.head, 1);
-            s_move[0] = 0;
-            s_move[1] = 0;
-            s_overflow = 0;
-            s_bad = 0;
-        }
-        if (ENERGY && tid < kNumSlots) s_energy[tid] = 0.0;
-        __syncthreads();
-        const int q = s_claim;
-        if (q >= a.n_order) break;
-        const int slot = a.order[q];
-        const BatchSys& R = a.sys[slot];
-        if (INTEGRATE && R.status != 0) {  // blew up earlier: not advanced again
-            __syncthreads();  // every thread has read s_claim before it is rewritten
-            continue;
-        }
-        const int n = R.n, nt = R.nt, npad = nt * 32;
-        const PairConsts pc = R.pc;
-        const LangevinConsts lc = R.lc;
-        const long long boff = R.bead_off;
-        const unsigned char* blob = a.blob + R.blob_off;
-        const float4* gp0 = reinterpret_cast<const float4*>(blob + R.off_p0);
-        const float4* gp1 = reinterpret_cast<const float4*>(blob + R.off_p1);
-        const uint32_t* glab = reinterpret_cast<const uint32_t*>(blob + R.off_lab);
-        const float* ginvm = reinterpret_cast<const float*>(blob + R.off_invm);
-        // ---- shared-memory layout of this system, arrays of stride ns ----
-        // Positions are float-float: hi parts in sx (pair arithmetic), lo
-        // parts in sxl; x = hi + lo carries ~48 significant bits.  fp / fb:
-        // each bead's pair and bonded force of the current step.
-        const int ns = npad;
-        float* fp = reinterpret_cast<float*>(smem);
-        float* fb = reinterpret_cast<float*>(smem + 12 * (size_t)ns);
-        float4* sx = reinterpret_cast<float4*>(smem + 24 * (size_t)ns);
-        float4* sp0 = reinterpret_cast<float4*>(smem + 40 * (size_t)ns);
-        float* sxl = reinterpret_cast<float*>(smem + 56 * (size_t)ns);
-        float* sv = reinterpret_cast<float*>(smem + 68 * (size_t)ns);
-        float* sim = reinterpret_cast<float*>(smem + 80 * (size_t)ns);
-        float* sref = reinterpret_cast<float*>(smem + 84 * (size_t)ns);
-        uint16_t* scnt = reinterpret_cast<uint16_t*>(smem + 96 * (size_t)ns);
-        size_t off = 98 * (size_t)ns;
-        float4* sp1 = nullptr;
-        uint32_t* slab = nullptr;
-        if ((TERMS & kTermLJA) || LABELS) {
-            sp1 = reinterpret_cast<float4*>(smem + off);
-            slab = reinterpret_cast<uint32_t*>(smem + off + 16 * (size_t)ns);
-            off += 20 * (size_t)ns;
-        }
-        float4* bc = reinterpret_cast<float4*>(smem + off);
-        float4* bh = bc + nt;
-        off += 32 * (size_t)nt;
-        float3* carry = reinterpret_cast<float3*>(smem + off);
-        off += 36 * (size_t)nt;
-        off = (off + 15) & ~(size_t)15;
-        uint16_t* sseg = reinterpret_cast<uint16_t*>(smem + off);
-        off += 2 * kMaxUnits;
-        // bonded records and tables: staged in shared memory when they fit,
-        // read from the blob otherwise
-        const unsigned char* gbonded = blob + R.off_bonded;
-        const bool bonded_smem = off + (size_t)R.bonded_bytes <= a.smem_bytes;
-        unsigned char* sbonded = smem + off;
-        if (bonded_smem) off += (size_t)R.bonded_bytes;
-        const unsigned char* bsrc = bonded_smem ? sbonded : gbonded;
-        Bonded B;
-        B.bpar = reinterpret_cast<const float4*>(bsrc + R.rb_p);
-        B.bij = reinterpret_cast<const uint32_t*>(bsrc + R.rb_ij);
-        B.aij = reinterpret_cast<const uint2*>(bsrc + R.ra_ij);
-        B.ak = reinterpret_cast<const float*>(bsrc + R.ra_k);
-        B.drec = reinterpret_cast<const uint4*>(bsrc + R.rd);
-        B.gdp = reinterpret_cast<const float2*>(bsrc + R.rgd);
-        B.fla = reinterpret_cast<const FlaTable*>(bsrc + R.rfla);
-        B.fld = reinterpret_cast<const FldTable*>(bsrc + R.rfld);
-        B.cb = reinterpret_cast<const uint16_t*>(bsrc + R.rcb);
-        B.ca = reinterpret_cast<const uint16_t*>(bsrc + R.rca);
-        B.cd = reinterpret_cast<const uint16_t*>(bsrc + R.rcd);
-        B.gs = reinterpret_cast<const uint16_t*>(bsrc + R.rgs);
-        B.gl = reinterpret_cast<const uint32_t*>(bsrc + R.rgl);
-        uint16_t* slist = reinterpret_cast<uint16_t*>(smem + off);
-        const size_t list_bytes = a.smem_bytes > off ? a.smem_bytes - off : 0;
-        const int32_t* ex_start = reinterpret_cast<const int32_t*>(blob + R.off_ex_start);
-        const int32_t* exl = reinterpret_cast<const int32_t*>(blob + R.off_ex);
-        uint16_t* glist = a.lists + R.list_off;
-        const int maxn = R.maxn;
-        // entries per bead kept in shared memory (multiple of 4)
-        const int cap_s = min(maxn, (int)(list_bytes / (2 * (size_t)npad)) & ~3);
-        const int S = pair_split(n);
-        const unsigned long long step0 = R.steps_done;
-        int K = 1;
-        if (INTEGRATE) {
-            const unsigned long long left = R.steps_target > step0 ? R.steps_target - step0 : 0ull;
-            K = (int)min((unsigned long long)(a.order_k ? a.order_k[q] : a.k), left);
-        }
-        const uint32_t slots_en = INTEGRATE ? 0xffffffffu : a.slots_enabled;
-        uint32_t excl_all = 0u;
-        if (!(slots_en & (1u << kSlotEXV))) excl_all |= kTermEXV;
-        if (!(slots_en & (1u << kSlotDH))) excl_all |= kTermDH;
-        if (!(slots_en & (1u << kSlotLJR))) excl_all |= kTermLJR;
-        if (!(slots_en & (1u << kSlotLJA))) excl_all |= kTermLJA;
-        const bool pairs_on = (pc.terms & ~excl_all) != 0;
-
-        // ---- load ----
-        for (int b = tid; b < npad; b += THREADS) {
-            if (b < n) {
-                const double px = a.x[boff + b], py = a.y[boff + b], pz = a.z[boff + b];
-                const float hx = __double2float_rn(px), hy = __double2float_rn(py),
-                            hz = __double2float_rn(pz);
-                sx[b] = make_float4(hx, hy, hz, 0.f);
-                sxl[b] = __double2float_rn(px - (double)hx);
-                sxl[ns + b] = __double2float_rn(py - (double)hy);
-                sxl[2 * ns + b] = __double2float_rn(pz - (double)hz);
-                sp0[b] = gp0[b];
-                sv[b] = a.vx[boff + b];
-                sv[ns + b] = a.vy[boff + b];
-                sv[2 * ns + b] = a.vz[boff + b];
-                sim[b] = ginvm[b];
-                if ((TERMS & kTermLJA) || LABELS) {
-                    sp1[b] = gp1[b];
-                    slab[b] = glab[b];
-                }
-            } else {
-                sx[b] = make_float4(nan, nan, nan, 0.f);
-                sp0[b] = make_float4(0.f, 0.f, 0.f, 0.f);
-                sim[b] = 0.f;
-                if ((TERMS & kTermLJA) || LABELS) {
-                    sp1[b] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    slab[b] = 0xffffffffu;
-                }
-            }
-        }
-        if (bonded_smem) {
-            const uint4* src = reinterpret_cast<const uint4*>(gbonded);
-            uint4* dst = reinterpret_cast<uint4*>(sbonded);
-            for (int q = tid; q < R.bonded_bytes / 16; q += THREADS) dst[q] = src[q];
-        }
-        __syncthreads();
-        for (int I = warp; I < nt; I += NW) cluster_bbox(I, n, sx, bc, bh, lane);
-        __syncthreads();
-
-        // list cutoff = largest pair cutoff + skin; the scan culls at the
-        // cutoff (with a margin for the FP32 box arithmetic)
-        const float rc = sqrtf(pc.list_rc2);
-        const float lcut = (rc + R.skin) * 1.0001f;
-        const float lcut2 = lcut * lcut;
-        const float tcut = rc * 1.0001f + 1e-4f;
-        const float tcut2 = tcut * tcut;
-        const float half_skin2 = 0.25f * R.skin * R.skin;
-        bool use_scan = false;
-        bool need_build = pairs_on;
-        int builds = 0;
-        int st_done = 0;
-        EnergyAcc ea;
-        if (ENERGY) ea.zero();
-
-        for (int st = 0; st < K; ++st) {
-            if (need_build && !use_scan) {
-                build_lists<LABELS>(n, nt, npad, maxn, cap_s, lcut2, sx, slab, bc, bh, ex_start, exl,
-                                    pc, slist, glist, scnt, sref, ns, tid, THREADS, S, sseg,
-                                    &s_overflow);
-                ++builds;
-                __syncthreads();
-                use_scan = s_overflow != 0;
-            }
-            const unsigned long long step = step0 + (unsigned long long)st;
-            // ---- pair terms: (bead, j-range) units u = i * S + s, 32 per
-            // warp; the S partial sums of a bead meet in a fixed butterfly
-            // and its first sub-lane stores the bead's pair force ----
-            if (pairs_on) {
-                for (int base = warp * 32; base < n * S; base += THREADS) {
-                    const int u = base + lane;
-                    const int i = u / S, sr = u & (S - 1);
-                    float3 fi = make_float3(0.f, 0.f, 0.f);
-                    if (i < n) {
-                        if (!use_scan) {
-                            const int k0 = S > 1 ? (int)sseg[u] : 0;
-                            const int k1 = sr == S - 1 ? (int)scnt[i] : (int)sseg[u + 1];
-                            fi = list_forces<TERMS, ENERGY>(i, k0, k1, cap_s, npad, slist, glist, sx, sp0, sp1,
-                                                            excl_all, pc, ea);
-                        } else {
-                            const int j0 = (sr * n) / S, j1 = sr == S - 1 ? n : ((sr + 1) * n) / S;
-                            fi = scan_forces<TERMS, LABELS, ENERGY>(i, j0, j1, nt, sx, sp0, sp1, slab, bc, bh,
-                                                                    tcut2, ex_start, exl, excl_all, pc, ea);
-                        }
-                    }
-                    for (int o = 1; o < S; o <<= 1) {
-                        fi.x += __shfl_xor_sync(kFull, fi.x, o);
-                        fi.y += __shfl_xor_sync(kFull, fi.y, o);
-                        fi.z += __shfl_xor_sync(kFull, fi.z, o);
-                    }
-                    if (i < n && sr == 0) {
-                        fp[i] = fi.x;
-                        fp[ns + i] = fi.y;
-                        fp[2 * ns + i] = fi.z;
-                    }
-                }
-            }
-            // ---- bonded: one warp per cluster of 32 chain positions,
-            // started from the far end of the warp range so warps that ran
-            // few pair units take the bonded work ----
-            for (int I = NW - 1 - warp; I < nt; I += NW) {
-                const float3 f = bonded_cluster<ENERGY>(B, I, n, lane, sx, sxl, ns, slots_en, carry, ea);
-                const int b = I * 32 + lane;
-                if (b < n) {
-                    fb[b] = f.x;
-                    fb[ns + b] = f.y;
-                    fb[2 * ns + b] = f.z;
-                }
-            }
-            __syncthreads();
-            if (!INTEGRATE) break;
-            // ---- Langevin update, bounding boxes, displacement and
-            // blow-up checks; bead b = I * 32 + lane of cluster I = warp +
-            // c * NW ----
-            const int mv = st & 1;
-#pragma unroll
-            for (int c = 0; c < BPT; ++c) {
-                const int I = warp + c * NW;
-                if (I >= nt) break;
-                const int b = I * 32 + lane;
-                bool moved = false, bad = false;
-                if (b < n) {
-                    float fx = fb[b], fy = fb[ns + b], fz = fb[2 * ns + b];
-                    if (pairs_on) {
-                        fx = fp[b] + fx;
-                        fy = fp[ns + b] + fy;
-                        fz = fp[2 * ns + b] + fz;
-                    }
-                    if (lane < 3 && I > 0) {
-                        const float3 cin = carry[3 * (I - 1) + lane];
-                        fx += cin.x;
-                        fy += cin.y;
-                        fz += cin.z;
-                    }
-                    bad = !(fabsf(fx) <= kForceLimit && fabsf(fy) <= kForceLimit && fabsf(fz) <= kForceLimit);
-                    const float im = sim[b];
-                    if (im > 0.f) {
-                        const float3 g = gaussian3(lc.seed, lc.stream, (uint32_t)b, step, kPurposeLangevin);
-                        const float sq = sqrtf(im) * lc.noise;
-                        const float fs = lc.fscale * im;
-                        const float vx = lc.vscale * sv[b] + fs * fx + sq * g.x;
-                        const float vy = lc.vscale * sv[ns + b] + fs * fy + sq * g.y;
-                        const float vz = lc.vscale * sv[2 * ns + b] + fs * fz + sq * g.z;
-                        sv[b] = vx;
-                        sv[ns + b] = vy;
-                        sv[2 * ns + b] = vz;
-                        float4 h = sx[b];
-                        ff_add(h.x, sxl[b], vx * lc.dt);
-                        ff_add(h.y, sxl[ns + b], vy * lc.dt);
-                        ff_add(h.z, sxl[2 * ns + b], vz * lc.dt);
-                        sx[b] = h;
-                        bad = bad || !(isfinite(h.x) && isfinite(h.y) && isfinite(h.z));
-                        const float dx = h.x - sref[b], dy = h.y - sref[ns + b], dz = h.z - sref[2 * ns + b];
-                        moved = dx * dx + dy * dy + dz * dz > half_skin2;
-                    }
-                }
-                if (__any_sync(kFull, moved) && lane == 0) atomicOr(&s_move[mv], 1);
-                if (__any_sync(kFull, bad) && lane == 0) atomicOr(&s_bad, 1);
-                __syncwarp();
-                cluster_bbox(I, n, sx, bc, bh, lane);
-            }
-            __syncthreads();
-            st_done = st + 1;
-            if (s_bad) break;  // the system blew up this step: stop advancing it
-            need_build = s_move[mv] != 0;
-            if (tid == 0) s_move[mv ^ 1] = 0;
-        }
-
-        // ---- write back ----
-        if (INTEGRATE) {
-            for (int b = tid; b < n; b += THREADS) {
-                const float4 h = sx[b];
-                a.x[boff + b] = (double)h.x + (double)sxl[b];
-                a.y[boff + b] = (double)h.y + (double)sxl[ns + b];
-                a.z[boff + b] = (double)h.z + (double)sxl[2 * ns + b];
-                a.vx[boff + b] = sv[b];
-                a.vy[boff + b] = sv[ns + b];
-                a.vz[boff + b] = sv[2 * ns + b];
-            }
-            if (tid == 0) {
-                a.sys[slot].steps_done = step0 + (unsigned long long)st_done;
-                a.sys[slot].builds = builds;
-                if (s_overflow) a.sys[slot].overflow = 1;
-                if (s_bad) a.sys[slot].status = kBatchStatusBlownUp;
+    // ---- load ----
+    for (int b = gtid; b < npad; b += GT) {
+        if (b < n) {
+            const double px = a.x[boff + b], py = a.y[boff + b], pz = a.z[boff + b];
+            const float hx = __double2float_rn(px), hy = __double2float_rn(py),
+                        hz = __double2float_rn(pz);
+            sx[b] = make_float4(hx, hy, hz, 0.f);
+            sxl[b] = __double2float_rn(px - (double)hx);
+            sxl[ns + b] = __double2float_rn(py - (double)hy);
+            sxl[2 * ns + b] = __double2float_rn(pz - (double)hz);
+            sp0[b] = gp0[b];
+            sv[b] = a.vx[boff + b];
+            sv[ns + b] = a.vy[boff + b];
+            sv[2 * ns + b] = a.vz[boff + b];
+            sim[b] = ginvm[b];
+            if ((TERMS & kTermLJA) || LABELS) {
+                sp1[b] = gp1[b];
+                slab[b] = glab[b];
             }
         } else {
-            bool bad = false;
-            for (int b = tid; b < n; b += THREADS) {
+            sx[b] = make_float4(nan, nan, nan, 0.f);
+            sp0[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+            sim[b] = 0.f;
+            if ((TERMS & kTermLJA) || LABELS) {
+                sp1[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+                slab[b] = 0xffffffffu;
+            }
+        }
+    }
+    if (bonded_smem) {
+        const uint4* src = reinterpret_cast<const uint4*>(gbonded);
+        uint4* dst = reinterpret_cast<uint4*>(sbonded);
+        for (int q = gtid; q < R.bonded_bytes / 16; q += GT) dst[q] = src[q];
+    }
+    bar_sync(bar, GT);
+    for (int I = gwarp; I < nt; I += NWG) cluster_bbox(I, n, sx, bc, bh, lane);
+    bar_sync(bar, GT);
+
+    // list cutoff = largest pair cutoff + skin; the scan culls at the
+    // cutoff (with a margin for the FP32 box arithmetic)
+    const float rc = sqrtf(pc.list_rc2);
+    const float lcut = (rc + R.skin) * 1.0001f;
+    const float lcut2 = lcut * lcut;
+    const float tcut = rc * 1.0001f + 1e-4f;
+    const float tcut2 = tcut * tcut;
+    const float half_skin2 = 0.25f * R.skin * R.skin;
+    bool use_scan = false;
+    bool need_build = pairs_on;
+    int builds = 0;
+    int st_done = 0;
+    EnergyAcc ea;
+    if (ENERGY) ea.zero();
+
+    for (int st = 0; st < K; ++st) {
+        if (need_build && !use_scan) {
+            build_lists<LABELS>(n, nt, npad, maxn, cap_s, lcut2, sx, slab, bc, bh, ex_start, exl,
+                                pc, slist, glist, scnt, sref, ns, gtid, GT, S, sseg,
+                                s_overflow);
+            ++builds;
+            bar_sync(bar, GT);
+            use_scan = *s_overflow != 0;
+        }
+        const unsigned long long step = step0 + (unsigned long long)st;
+        // ---- pair terms: (bead, j-range) units u = i * S + s, 32 per
+        // warp; the S partial sums of a bead meet in a fixed butterfly
+        // and its first sub-lane stores the bead's pair force ----
+        if (pairs_on) {
+            for (int base = gwarp * 32; base < n * S; base += GT) {
+                const int u = base + lane;
+                const int i = u / S, sr = u & (S - 1);
+                float3 fi = make_float3(0.f, 0.f, 0.f);
+                if (i < n) {
+                    if (!use_scan) {
+                        const int k0 = S > 1 ? (int)sseg[u] : 0;
+                        const int k1 = sr == S - 1 ? (int)scnt[i] : (int)sseg[u + 1];
+                        fi = list_forces<TERMS, ENERGY>(i, k0, k1, cap_s, npad, slist, glist, sx, sp0, sp1,
+                                                        excl_all, pc, ea);
+                    } else {
+                        const int j0 = (sr * n) / S, j1 = sr == S - 1 ? n : ((sr + 1) * n) / S;
+                        fi = scan_forces<TERMS, LABELS, ENERGY>(i, j0, j1, nt, sx, sp0, sp1, slab, bc, bh,
+                                                                tcut2, ex_start, exl, excl_all, pc, ea);
+                    }
+                }
+                for (int o = 1; o < S; o <<= 1) {
+                    fi.x += __shfl_xor_sync(kFull, fi.x, o);
+                    fi.y += __shfl_xor_sync(kFull, fi.y, o);
+                    fi.z += __shfl_xor_sync(kFull, fi.z, o);
+                }
+                if (i < n && sr == 0) {
+                    fp[i] = fi.x;
+                    fp[ns + i] = fi.y;
+                    fp[2 * ns + i] = fi.z;
+                }
+            }
+        }
+        // ---- bonded: one warp per cluster of 32 chain positions,
+        // started from the far end of the warp range so warps that ran
+        // few pair units take the bonded work ----
+        for (int I = NWG - 1 - gwarp; I < nt; I += NWG) {
+            const float3 f = bonded_cluster<ENERGY>(B, I, n, lane, sx, sxl, ns, slots_en, carry, ea);
+            const int b = I * 32 + lane;
+            if (b < n) {
+                fb[b] = f.x;
+                fb[ns + b] = f.y;
+                fb[2 * ns + b] = f.z;
+            }
+        }
+        bar_sync(bar, GT);
+        if (!INTEGRATE) break;
+        // ---- Langevin update, bounding boxes, displacement and
+        // blow-up checks; bead b = I * 32 + lane of cluster I = gwarp +
+        // c * NWG ----
+        const int mv = st & 1;
+#pragma unroll 4
+        for (int c = 0; c < BPT; ++c) {
+            const int I = gwarp + c * NWG;
+            if (I >= nt) break;
+            const int b = I * 32 + lane;
+            bool moved = false, bad = false;
+            if (b < n) {
                 float fx = fb[b], fy = fb[ns + b], fz = fb[2 * ns + b];
                 if (pairs_on) {
                     fx = fp[b] + fx;
                     fy = fp[ns + b] + fy;
                     fz = fp[2 * ns + b] + fz;
                 }
-                const int I = b >> 5, l = b & 31;
-                if (l < 3 && I > 0) {
-                    const float3 cin = carry[3 * (I - 1) + l];
+                if (lane < 3 && I > 0) {
+                    const float3 cin = carry[3 * (I - 1) + lane];
                     fx += cin.x;
                     fy += cin.y;
                     fz += cin.z;
                 }
-                bad = bad || !(fabsf(fx) <= kForceLimit && fabsf(fy) <= kForceLimit && fabsf(fz) <= kForceLimit);
-                a.forces[b] = fx;
-                a.forces[nmax + b] = fy;
-                a.forces[2 * nmax + b] = fz;
+                bad = !(fabsf(fx) <= kForceLimit && fabsf(fy) <= kForceLimit && fabsf(fz) <= kForceLimit);
+                const float im = sim[b];
+                if (im > 0.f) {
+                    const float3 g = gaussian3(lc.seed, lc.stream, (uint32_t)b, step, kPurposeLangevin);
+                    const float sq = sqrtf(im) * lc.noise;
+                    const float fs = lc.fscale * im;
+                    const float vx = lc.vscale * sv[b] + fs * fx + sq * g.x;
+                    const float vy = lc.vscale * sv[ns + b] + fs * fy + sq * g.y;
+                    const float vz = lc.vscale * sv[2 * ns + b] + fs * fz + sq * g.z;
+                    sv[b] = vx;
+                    sv[ns + b] = vy;
+                    sv[2 * ns + b] = vz;
+                    float4 h = sx[b];
+                    ff_add(h.x, sxl[b], vx * lc.dt);
+                    ff_add(h.y, sxl[ns + b], vy * lc.dt);
+                    ff_add(h.z, sxl[2 * ns + b], vz * lc.dt);
+                    sx[b] = h;
+                    bad = bad || !(isfinite(h.x) && isfinite(h.y) && isfinite(h.z));
+                    const float dx = h.x - sref[b], dy = h.y - sref[ns + b], dz = h.z - sref[2 * ns + b];
+                    moved = dx * dx + dy * dy + dz * dz > half_skin2;
+                }
             }
-            if (bad) atomicOr(&s_bad, 1);
-            __syncthreads();
-            if (tid == 0) {
-                if (s_overflow) a.sys[slot].overflow = 1;
-                a.sys[slot].eval_status = s_bad ? kBatchStatusBlownUp : 0;
-            }
+            if (__any_sync(kFull, moved) && lane == 0) atomicOr(&s_move[mv], 1);
+            if (__any_sync(kFull, bad) && lane == 0) atomicOr(s_bad, 1);
+            __syncwarp();
+            cluster_bbox(I, n, sx, bc, bh, lane);
         }
-        if (ENERGY) {
+        bar_sync(bar, GT);
+        st_done = st + 1;
+        if (*s_bad) break;  // the system blew up this step: stop advancing it
+        need_build = s_move[mv] != 0;
+        if (gtid == 0) s_move[mv ^ 1] = 0;
+    }
+
+    // ---- write back ----
+    if (INTEGRATE) {
+        for (int b = gtid; b < n; b += GT) {
+            const float4 h = sx[b];
+            a.x[boff + b] = (double)h.x + (double)sxl[b];
+            a.y[boff + b] = (double)h.y + (double)sxl[ns + b];
+            a.z[boff + b] = (double)h.z + (double)sxl[2 * ns + b];
+            a.vx[boff + b] = sv[b];
+            a.vy[boff + b] = sv[ns + b];
+            a.vz[boff + b] = sv[2 * ns + b];
+        }
+        if (gtid == 0) {
+            a.sys[slot].steps_done = step0 + (unsigned long long)st_done;
+            a.sys[slot].builds = builds;
+            if (*s_overflow) a.sys[slot].overflow = 1;
+            if (*s_bad) a.sys[slot].status = kBatchStatusBlownUp;
+        }
+    } else {
+        bool bad = false;
+        for (int b = gtid; b < n; b += GT) {
+            float fx = fb[b], fy = fb[ns + b], fz = fb[2 * ns + b];
+            if (pairs_on) {
+                fx = fp[b] + fx;
+                fy = fp[ns + b] + fy;
+                fz = fp[2 * ns + b] + fz;
+            }
+            const int I = b >> 5, l = b & 31;
+            if (l < 3 && I > 0) {
+                const float3 cin = carry[3 * (I - 1) + l];
+                fx += cin.x;
+                fy += cin.y;
+                fz += cin.z;
+            }
+            bad = bad || !(fabsf(fx) <= kForceLimit && fabsf(fy) <= kForceLimit && fabsf(fz) <= kForceLimit);
+            a.forces[b] = fx;
+            a.forces[nmax + b] = fy;
+            a.forces[2 * nmax + b] = fz;
+        }
+        if (bad) atomicOr(s_bad, 1);
+        bar_sync(bar, GT);
+        if (gtid == 0) {
+            if (*s_overflow) a.sys[slot].overflow = 1;
+            a.sys[slot].eval_status = *s_bad ? kBatchStatusBlownUp : 0;
+        }
+    }
+    if (ENERGY) {
 #pragma unroll
-            for (int k = 0; k < kNumSlots; ++k) {
-                const double v = warp_sum_d(ea.e[k]);
-                if (lane == 0 && v != 0.0) atomicAdd(&s_energy[k], v);
-            }
-            __syncthreads();
-            if (tid < kNumSlots) a.energy[(size_t)slot * kNumSlots + tid] = s_energy[tid];
+        for (int k = 0; k < kNumSlots; ++k) {
+            const double v = warp_sum_d(ea.e[k]);
+            if (lane == 0 && v != 0.0) atomicAdd(&s_energy[k], v);
         }
+        bar_sync(bar, GT);
+        if (gtid < kNumSlots) a.energy[(size_t)slot * kNumSlots + gtid] = s_energy[gtid];
+    }
+}
+
+template <int THREADS, int TERMS, bool LABELS, bool ENERGY, bool INTEGRATE>
+__global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    // per-group state (group 0 only until the split)
+    __shared__ int s_claim[2];
+    __shared__ int s_move[2][2];
+    __shared__ int s_overflow[2];
+    __shared__ int s_bad[2];
+    __shared__ double s_energy[2][kNumSlots];
+    const int tid = threadIdx.x;
+
+    // Whole-CTA phase: every claimed system runs on all THREADS threads
+    // (barrier 0).  When the CTA claims a system small enough for half of its
+    // shared memory, and the launch has at least two systems per CTA, it
+    // leaves this loop with that system: claims come largest first, so every
+    // later system is small too.  Every thread takes the same branch, right
+    // after a CTA-wide barrier.
+    int split_q = -1;
+    while (true) {
+        if (tid == 0) {
+            s_claim[0] = atomicAdd(a.head, 1);
+            s_move[0][0] = 0;
+            s_move[0][1] = 0;
+            s_overflow[0] = 0;
+            s_bad[0] = 0;
+        }
+        if (ENERGY && tid < kNumSlots) s_energy[0][tid] = 0.0;
         __syncthreads();
+        const int q = s_claim[0];
+        if (q >= a.n_order) return;
+        const int slot = a.order[q];
+        const BatchSys& R = a.sys[slot];
+        if (INTEGRATE && R.status != 0) {  // blew up earlier: not advanced again
+            __syncthreads();  // every thread has read s_claim before it is rewritten
+            continue;
+        }
+        if (R.n <= a.split_beads && a.n_order >= 2 * (int)gridDim.x) {
+            split_q = q;
+            break;
+        }
+        run_system<THREADS, TERMS, LABELS, ENERGY, INTEGRATE>(a, q, slot, tid, 0, smem, a.smem_bytes, s_move[0],
+                                                              &s_overflow[0], &s_bad[0], s_energy[0]);
+        __syncthreads();
+    }
+
+    // Split phase, for the rest of the launch: two groups of THREADS / 2
+    // threads, each with half of the shared memory and its own named barrier
+    // (1 + g), each claiming and advancing its own systems; no barrier spans
+    // both groups.  Group 0 starts with the system the CTA claimed (its words
+    // were reset at that claim).  A system's results do not depend on the
+    // threads that run it (the pair split depends on its bead count alone),
+    // so they do not depend on the split either.
+    constexpr int GT = THREADS / 2;
+    const int g = tid / GT, gtid = tid - g * GT;
+    const size_t half = (a.smem_bytes / 2) & ~(size_t)255;
+    unsigned char* gsmem = smem + (size_t)g * half;
+    bool first = g == 0;
+    while (true) {
+        if (!first) {
+            if (gtid == 0) {
+                s_claim[g] = atomicAdd(a.head, 1);
+                s_move[g][0] = 0;
+                s_move[g][1] = 0;
+                s_overflow[g] = 0;
+                s_bad[g] = 0;
+            }
+            if (ENERGY && gtid < kNumSlots) s_energy[g][gtid] = 0.0;
+            bar_sync(1 + g, GT);
+        }
+        const int q = first ? split_q : s_claim[g];
+        first = false;
+        if (q >= a.n_order) return;
+        const int slot = a.order[q];
+        if (INTEGRATE && a.sys[slot].status != 0) {
+            bar_sync(1 + g, GT);
+            continue;
+        }
+        run_system<GT, TERMS, LABELS, ENERGY, INTEGRATE>(a, q, slot, gtid, 1 + g, gsmem, half, s_move[g],
+                                                         &s_overflow[g], &s_bad[g], s_energy[g]);
+        bar_sync(1 + g, GT);
     }
 }
 
@@ -913,6 +981,14 @@ void launch_persistent(Fn fn, int threads, BatchArgs a, int max_grid, size_t sme
     if (want > 0) share = std::min(share, want);
     share = std::max(share, smem) & ~(size_t)15;
     a.smem_bytes = share;
+    if (a.split_beads > 0) {
+        // a group's system must fit half of the share (state of its beads,
+        // the cluster arrays for the largest system, the pair-split offsets)
+        const size_t half = (share / 2) & ~(size_t)255;
+        const size_t fixed = (size_t)(32 + 36) * kMaxClusters + 16 + 2 * kMaxUnits;
+        const int fit = half > fixed ? (int)((half - fixed) / (size_t)a.split_bead_bytes) & ~31 : 0;
+        a.split_beads = std::min(a.split_beads, fit);
+    }
     const int grid = std::max(1, std::min(max_grid, num_sms * per_sm));
     fn<<<grid, threads, share, s>>>(a);
     OCM_CK(cudaGetLastError());
@@ -1234,6 +1310,11 @@ void BatchEngine::set_list_smem(int kib) {
     list_smem_kib_ = kib;
 }
 
+void BatchEngine::set_split(int beads) {
+    if (beads < 0 || beads > 32 * kMaxClusters) throw Error(1, "[error] split bead limit must be in 0..2048");
+    split_beads_ = beads;
+}
+
 void BatchEngine::set_threads(int threads) {
     if (threads != 256 && threads != 512 && threads != 1024)
         throw Error(1, "[error] threads per CTA must be 256, 512 or 1024");
@@ -1464,6 +1545,8 @@ void BatchEngine::launch(bool integrate, bool energy, int k, const std::vector<i
     a.forces = forces_.p;
     a.lists = lists_.p;
     a.slots_enabled = 0xffffffffu;
+    a.split_beads = integrate ? split_beads_ : 0;
+    a.split_bead_bytes = general ? 118 : 98;
     const int grid = (int)order.size();
     if (general)
         launch_batch_threads<15, true>(threads_, a, grid, smem, s, integrate, energy, num_sms_, want);

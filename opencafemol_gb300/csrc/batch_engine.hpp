@@ -96,6 +96,11 @@ class BatchEngine {
     // Balanced launches (the serving loop): the costliest resident system
     // does steps_per_launch steps, the others proportionally more.
     void set_balanced(bool on) { balanced_ = on; }
+    // A CTA splits into two groups of half its threads, each with half of
+    // its shared memory and its own systems, once the systems left are of at
+    // most `beads` beads (0: never; capped so a system fits its half).
+    void set_split(int beads);
+    int split() const { return split_beads_; }
     void slot_stats(int64_t slot, int32_t* builds, int32_t* capacity);
     void set_positions_many(int64_t n, const int64_t* slots, const double* xyz, const double* v);
     void get_positions_many(int64_t n, const int64_t* slots, double* xyz);
@@ -147,6 +152,7 @@ class BatchEngine {
     DevBuf<BatchSys> sys_;
     DevBuf<int32_t> order_, order_k_, head_;
     bool balanced_ = false;
+    int split_beads_ = 384;   // CTA split at systems of at most this many beads (0: never)
     DevBuf<double> energy_;
     DevBuf<float> forces_;
     // staging of the many-slot state copies (grown on demand)

@@ -569,6 +569,7 @@ int ocm_batch_admit_resume(ocm_batch* batch, const ocm_system* s, const double* 
                *slot_out = batch->b->admit(s->g.desc(), pos, vel, T, friction, dt, seed, n_steps, steps_done));
 }
 int ocm_batch_set_balanced(ocm_batch* batch, int on) { BATCH_CALL(batch->b->set_balanced(on != 0)); }
+int ocm_batch_set_split(ocm_batch* batch, int32_t beads) { BATCH_CALL(batch->b->set_split(beads)); }
 int ocm_batch_slot_status(ocm_batch* batch, int64_t slot, int32_t* status) {
     BATCH_CALL(need(status, "status"); *status = batch->b->slot_status(slot));
 }

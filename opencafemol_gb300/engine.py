@@ -286,35 +286,53 @@ class Batch:
     def set_list_smem(self, kib: int) -> None:
         check(lib.ocm_batch_set_list_smem(self._h, int(kib)))
 
+    def set_split(self, beads: int) -> None:
+        """Tuning knob: CTAs split into two groups once their systems have
+        at most ``beads`` beads (0: never)."""
+        check(lib.ocm_batch_set_split(self._h, int(beads)))
+
     def set_balanced(self, on: bool = True) -> None:
         """Balanced launches: the costliest system does the launch's steps,
         smaller ones proportionally more (for a serving loop)."""
         check(lib.ocm_batch_set_balanced(self._h, int(bool(on))))
 
-    DEFAULT_TUNE_CANDIDATES = ((512, 96), (1024, 96), (512, -1), (1024, -1), (256, 96))
+    # (threads per CTA, list shared memory KiB, split beads); -1 KiB = no cap
+    DEFAULT_TUNE_CANDIDATES = ((512, 96, 384), (1024, 96, 512), (512, -1, 384), (1024, -1, 512),
+                               (512, 96, 0), (1024, 96, 0), (256, 96, 0))
 
-    def autotune(self, steps_per_trial: int = 50, candidates=DEFAULT_TUNE_CANDIDATES) -> dict:
-        """Pick the launch shape (threads per CTA, list shared memory in KiB)
-        for the systems resident now.
+    def autotune(self, steps_per_trial: int = 50, candidates=DEFAULT_TUNE_CANDIDATES,
+                 rounds: int = 2) -> dict:
+        """Pick the launch shape (threads per CTA, list shared memory in KiB,
+        split size) for the systems resident now.  A candidate of two
+        entries keeps split 0.
 
-        Every candidate runs two real launches of ``steps_per_trial`` steps
-        (the first absorbs the set-up of that shape); the second is timed
-        with CUDA events and the fastest shape is kept.  Trajectories do not
-        depend on the shape, so the trials are ordinary simulation progress:
-        the resident systems advance by 2 * steps_per_trial steps per
-        candidate (systems with fewer steps left finish early)."""
-        trials = []
-        for th, kib in candidates:
-            self.set_threads(th)
-            self.set_list_smem(kib)
-            self.run(steps_per_trial, sync=True)
-            self.run(steps_per_trial, sync=True)
-            trials.append((self.last_run_ms(), th, kib))
-        ms, th, kib = min(trials)
+        In each of ``rounds`` rounds every candidate runs two real launches
+        of ``steps_per_trial`` steps (the first absorbs the set-up of that
+        shape); the second is timed with CUDA events.  The rounds interleave
+        the candidates, so a drift of the systems' cost while they relax
+        does not favour the candidates timed last; the shape with the
+        smallest mean time is kept.  Trajectories do not depend on the
+        shape, so the trials are ordinary simulation progress: the resident
+        systems advance by 2 * rounds * steps_per_trial steps per candidate
+        (systems with fewer steps left finish early)."""
+        cands = [(c[0], c[1], c[2] if len(c) > 2 else 0) for c in candidates]
+        times = [[] for _ in cands]
+        for _ in range(max(1, rounds)):
+            for k, (th, kib, split) in enumerate(cands):
+                self.set_threads(th)
+                self.set_list_smem(kib)
+                self.set_split(split)
+                self.run(steps_per_trial, sync=True)
+                self.run(steps_per_trial, sync=True)
+                times[k].append(self.last_run_ms())
+        trials = [(sum(t) / len(t), th, kib, split) for t, (th, kib, split) in zip(times, cands)]
+        ms, th, kib, split = min(trials)
         self.set_threads(th)
         self.set_list_smem(kib)
-        return {"threads": th, "list_smem_kib": kib, "ms_per_launch": ms,
-                "trials": [{"threads": t, "list_smem_kib": k, "ms": m} for m, t, k in trials]}
+        self.set_split(split)
+        return {"threads": th, "list_smem_kib": kib, "split_beads": split, "ms_per_launch": ms,
+                "trials": [{"threads": t, "list_smem_kib": k, "split_beads": sp, "ms": m}
+                           for m, t, k, sp in trials]}
 
     def threads(self) -> int:
         t = C.c_int32()

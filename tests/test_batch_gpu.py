@@ -159,13 +159,14 @@ def test_autotune_keeps_results(gpu):
     for tune in (True, False):
         b = gpu.Batch(max_systems=3, max_total_beads=1300, max_beads_per_system=800)
         slots = [b.admit(synth.build_system(s), s.pos, seed=5 + k, n_steps=10 ** 6) for k, s in enumerate(specs)]
-        cands = ((512, 96), (1024, -1), (256, 48))
+        cands = ((512, 96), (1024, -1, 512), (256, 48, 128))
         if tune:
             res = b.autotune(steps_per_trial=20, candidates=cands)
-            assert (res["threads"], res["list_smem_kib"]) in cands and len(res["trials"]) == 3
+            picked = (res["threads"], res["list_smem_kib"], res["split_beads"])
+            assert picked in [c if len(c) == 3 else c + (0,) for c in cands] and len(res["trials"]) == 3
             assert b.threads() == res["threads"]
         else:
-            b.run(2 * 20 * len(cands), sync=True)
+            b.run(2 * 2 * 20 * len(cands), sync=True)
         runs.append([b.positions(k) for k in slots])
     for xa, xb in zip(*runs):
         assert np.array_equal(xa, xb)
@@ -195,3 +196,25 @@ def test_aicg_gaussian_terms_both_engines(gpu):
     ep = ctx.getGroupEnergies()
     for g, name in enumerate(names):
         assert abs(ep[g] - e_ref[name]) <= 1e-5 * max(1.0, abs(e_ref[name])), name
+
+
+def test_cta_split_keeps_results(gpu):
+    """With more resident systems than two per CTA, CTAs split into two
+    groups of half their threads for the small systems; every trajectory is
+    identical to the one advanced by whole CTAs."""
+    from opencafemol_gb300 import synth
+    rng = np.random.default_rng(77)
+    sizes = [int(n) for n in rng.integers(30, 420, 340)]
+    specs = [synth.go_protein(n, 3000 + k) for k, n in enumerate(sizes)]
+    systems = [synth.build_system(s) for s in specs]
+    runs = []
+    for threads, split in ((512, 0), (512, 384), (1024, 512), (256, 128)):
+        b = gpu.Batch(max_systems=len(specs), max_total_beads=sum(sizes) + 64, max_beads_per_system=512)
+        slots = [b.admit(so, s.pos, seed=40 + k, n_steps=10 ** 6) for k, (so, s) in enumerate(zip(systems, specs))]
+        b.set_threads(threads)
+        b.set_split(split)
+        b.run(30, sync=True)
+        b.run(30, sync=True)
+        runs.append(b.get_positions_many(slots))
+    for r in runs[1:]:
+        assert np.array_equal(r, runs[0])
