@@ -245,6 +245,8 @@ def run_ours(args, rank, world):
     tuned = None
     if args.threads:
         batch.set_threads(args.threads)
+        batch.set_list_smem(args.list_smem)
+        batch.set_split(args.split)
     for _ in range(args.warmup):
         batch.run(K, sync=True)
     if not args.threads:
@@ -270,7 +272,7 @@ def run_ours(args, rank, world):
 
     # ---- end to end through the public API with host buffers ----
     shape = ((tuned["threads"], tuned["list_smem_kib"], tuned["split_beads"]) if tuned
-             else (args.threads, -1, None))
+             else (args.threads, args.list_smem, args.split))
     e2e = run_e2e(ocm, synth, specs, systems, args, world, shape)
 
     # ---- plain single-system path on a sample of the same mix ----
@@ -300,8 +302,7 @@ def run_ours(args, rank, world):
                                    f"largest first onto the least-loaded rank; no collective)"
                                    if world > 1 else "one GPU"),
                    "launch_shape": {"threads_per_cta": batch.threads(), "autotuned": tuned is not None,
-                                    "list_smem_kib": tuned["list_smem_kib"] if tuned else None,
-                                    "split_beads": tuned["split_beads"] if tuned else None,
+                                    "list_smem_kib": shape[1], "split_beads": shape[2],
                                     "trials_ms": [t["ms"] for t in tuned["trials"]] if tuned else None},
                    "l2": "flushed (256 MiB write) between timed launches"},
         "e2e": e2e, "gpu_launches": args.steps, "roofline": roof, "cpu_baseline": cpu,
@@ -327,8 +328,7 @@ def run_e2e(ocm, synth, specs, systems, args, world, shape):
                       max_beads_per_system=SIZE_HI, device=local_device())
     batch.set_threads(shape[0])
     batch.set_list_smem(shape[1])
-    if shape[2] is not None:
-        batch.set_split(shape[2])
+    batch.set_split(shape[2])
     slots = [batch.admit(sysobj, s.pos, temperature=s.temperature, step_size=s.dt,
                          seed=17 + k, n_steps=10 ** 12)
              for k, (sysobj, s) in enumerate(zip(systems, specs))]
@@ -580,7 +580,9 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=24)
     ap.add_argument("--plain-chunks", type=int, default=2)
     ap.add_argument("--cpu-steps", type=int, default=500)  # MD steps of the whole ensemble, ~2 s
-    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=0)   # fixes the launch shape (no autotuning) ...
+    ap.add_argument("--list-smem", type=int, default=-1)  # ... with this list budget (KiB, -1 = no cap)
+    ap.add_argument("--split", type=int, default=512)     # ... and this CTA split size (beads)
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--traffic-bytes", type=float, default=K_BATCH_DRAM_BYTES,
                     help="DRAM bytes per k_batch launch (ncu), reported as roofline.traffic")

@@ -381,7 +381,7 @@ int ocm_batch_set_balanced(ocm_batch* batch, int on);
  * depend on it): when a launch has at least two systems per CTA and the
  * systems a CTA claims have at most `beads` beads, the CTA splits into two
  * groups of half its threads, each with half of its shared memory,
- * advancing two systems at a time (default 384; 0 = never split; capped so
+ * advancing two systems at a time (default 512; 0 = never split; capped so
  * that a system's state fits half of the CTA's shared memory). */
 int ocm_batch_set_split(ocm_batch* batch, int32_t beads);
 /* Wait for the last launch; *status = OCM_OK, or OCM_ERR_NONFINITE if the

@@ -47,6 +47,16 @@ constexpr int kMaxClusters = 64;  // 2048 beads per system
 constexpr int kSplitUnits = 512;
 constexpr int kMaxUnits = kSplitUnits;
 constexpr int kMaxSplit = 8;
+// Beads are ordered by their longest sub-list at every list build (bucket
+// sort over this many buckets), so the 32 lanes of a pair pass carry work of
+// similar length.
+constexpr int kSortBuckets = 64;
+// Shared memory of a system: bytes per bead (state, lists' counts, order)
+// and the part that does not grow with the bead count (cluster boxes and
+// carries, pair-split offsets, sort buckets, alignment).
+constexpr int kBeadBytes = 100;
+constexpr int kBeadBytesGeneral = 120;  // with per-bead LJ attraction parameters and labels
+constexpr size_t kFixedBytes = (size_t)(32 + 36) * kMaxClusters + 16 + 2 * kMaxUnits + 4 * kSortBuckets;
 // A force component beyond this (kJ/mol/nm) marks a blown-up system: far
 // above any physical coarse-grained force, and the bound of the plain
 // engine's fixed-point accumulators.
@@ -351,7 +361,10 @@ __device__ __forceinline__ uint32_t label_bits(uint32_t labi, uint32_t labj, con
 // term are dropped.  Entry k of bead i lives in shared memory at
 // slist[k * npad + i] for k < cap_s and in global memory at
 // glist[k * npad + i] for cap_s <= k < maxn.  Sets *overflow when a list
-// exceeds maxn.
+// exceeds maxn.  Then bord = the beads in decreasing length of their
+// longest sub-list (bucket sort; ties in any order), through the group's
+// barrier `bar`; tmp (n words) and hist (kSortBuckets words, zero on entry
+// and on return) are scratch.
 template <bool LABELS>
 __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, int cap_s, float cut2,
                                             const float4* sx, const uint32_t* slab,
@@ -361,13 +374,15 @@ __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, i
                                             const PairConsts& pc, uint16_t* slist,
                                             uint16_t* __restrict__ glist, uint16_t* scnt,
                                             float* sref, int nmax, int tid, int threads,
-                                            int S, uint16_t* sseg, int* overflow) {
+                                            int S, uint16_t* sseg, int* overflow, uint16_t* bord,
+                                            int* hist, uint32_t* tmp, int bar) {
     const float3 nobox = make_float3(0.f, 0.f, 0.f);
     const uint32_t present = (uint32_t)pc.terms;
     for (int i = tid; i < n; i += threads) {
         const float4 xi = sx[i];
         const uint32_t labi = LABELS ? slab[i] : 0u;
         int cnt = 0;
+        int seg0 = 0, longest = 0;  // start of the current sub-list, longest so far
         // list offset where each j-range of the pair split starts
         int s_next = 1;
         int jb = S > 1 ? n / S : 0x7FFFFFFF;
@@ -390,7 +405,10 @@ __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, i
                 if (LABELS) bits |= label_bits<true>(labi, slab[j], pc);
                 if ((bits & present) == present) continue;
                 while (j >= jb) {
-                    sseg[i * S + s_next] = (uint16_t)min(cnt, maxn);
+                    const int c = min(cnt, maxn);
+                    longest = max(longest, c - seg0);
+                    seg0 = c;
+                    sseg[i * S + s_next] = (uint16_t)c;
                     ++s_next;
                     jb = s_next < S ? (s_next * n) / S : 0x7FFFFFFF;
                 }
@@ -409,7 +427,32 @@ __device__ __forceinline__ void build_lists(int n, int nt, int npad, int maxn, i
         sref[i] = xi.x;
         sref[nmax + i] = xi.y;
         sref[2 * nmax + i] = xi.z;
+        longest = max(longest, cnt - seg0);
+        const int bucket = longest < 32 ? longest : min(kSortBuckets - 1, 32 + ((longest - 32) >> 2));
+        tmp[i] = (uint32_t)bucket | (uint32_t)atomicAdd(&hist[bucket], 1) << 8;
     }
+    bar_sync(bar, threads);
+    if (tid < 32) {
+        // exclusive offsets, buckets in decreasing order: lane l holds
+        // buckets 63 - 2l and 62 - 2l
+        const int h0 = hist[kSortBuckets - 1 - 2 * tid], h1 = hist[kSortBuckets - 2 - 2 * tid];
+        const int pair = h0 + h1;
+        int incl = pair;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(kFull, incl, o);
+            if (tid >= o) incl += v;
+        }
+        hist[kSortBuckets - 1 - 2 * tid] = incl - pair;
+        hist[kSortBuckets - 2 - 2 * tid] = incl - pair + h0;
+    }
+    bar_sync(bar, threads);
+    for (int i = tid; i < n; i += threads) {
+        const uint32_t t = tmp[i];
+        bord[hist[t & 255u] + (int)(t >> 8)] = (uint16_t)i;
+    }
+    bar_sync(bar, threads);
+    if (tid < kSortBuckets) hist[tid] = 0;
 }
 
 template <int TERMS, bool ENERGY>
@@ -549,7 +592,7 @@ __device__ __forceinline__ float3 scan_forces(int i, int j0, int j1, int nt, con
 template <int GT, int TERMS, bool LABELS, bool ENERGY, bool INTEGRATE>
 __device__ __forceinline__ void run_system(const BatchArgs& a, int q, int slot, int gtid, int bar,
                                            unsigned char* gsmem, size_t gsmem_bytes, int* s_move,
-                                           int* s_overflow, int* s_bad, double* s_energy) {
+                                           int* s_overflow, int* s_bad, double* s_energy, int* s_item) {
     constexpr int NWG = GT / 32;
     constexpr int BPT = (32 * kMaxClusters + GT - 1) / GT;  // cluster rows per warp in the update
     const int lane = gtid & 31, gwarp = gtid >> 5;
@@ -579,7 +622,8 @@ __device__ __forceinline__ void run_system(const BatchArgs& a, int q, int slot, 
     float* sim = reinterpret_cast<float*>(gsmem + 80 * (size_t)ns);
     float* sref = reinterpret_cast<float*>(gsmem + 84 * (size_t)ns);
     uint16_t* scnt = reinterpret_cast<uint16_t*>(gsmem + 96 * (size_t)ns);
-    size_t off = 98 * (size_t)ns;
+    uint16_t* bord = reinterpret_cast<uint16_t*>(gsmem + 98 * (size_t)ns);
+    size_t off = (size_t)kBeadBytes * ns;
     float4* sp1 = nullptr;
     uint32_t* slab = nullptr;
     if ((TERMS & kTermLJA) || LABELS) {
@@ -595,6 +639,8 @@ __device__ __forceinline__ void run_system(const BatchArgs& a, int q, int slot, 
     off = (off + 15) & ~(size_t)15;
     uint16_t* sseg = reinterpret_cast<uint16_t*>(gsmem + off);
     off += 2 * kMaxUnits;
+    int* hist = reinterpret_cast<int*>(gsmem + off);
+    off += 4 * kSortBuckets;
     // bonded records and tables: staged in shared memory when they fit,
     // read from the blob otherwise
     const unsigned char* gbonded = blob + R.off_bonded;
@@ -673,6 +719,9 @@ __device__ __forceinline__ void run_system(const BatchArgs& a, int q, int slot, 
         uint4* dst = reinterpret_cast<uint4*>(sbonded);
         for (int q = gtid; q < R.bonded_bytes / 16; q += GT) dst[q] = src[q];
     }
+    for (int k = gtid; k < kSortBuckets; k += GT) hist[k] = 0;
+    for (int b = gtid; b < n; b += GT) bord[b] = (uint16_t)b;  // until the first list build
+    if (gtid == 0) *s_item = 0;
     bar_sync(bar, GT);
     for (int I = gwarp; I < nt; I += NWG) cluster_bbox(I, n, sx, bc, bh, lane);
     bar_sync(bar, GT);
@@ -694,59 +743,69 @@ __device__ __forceinline__ void run_system(const BatchArgs& a, int q, int slot, 
 
     for (int st = 0; st < K; ++st) {
         if (need_build && !use_scan) {
+            // fb is free until the bonded terms of this step: sort scratch
             build_lists<LABELS>(n, nt, npad, maxn, cap_s, lcut2, sx, slab, bc, bh, ex_start, exl,
                                 pc, slist, glist, scnt, sref, ns, gtid, GT, S, sseg,
-                                s_overflow);
+                                s_overflow, bord, hist, reinterpret_cast<uint32_t*>(fb), bar);
             ++builds;
             bar_sync(bar, GT);
             use_scan = *s_overflow != 0;
         }
         const unsigned long long step = step0 + (unsigned long long)st;
-        // ---- pair terms: (bead, j-range) units u = i * S + s, 32 per
-        // warp; the S partial sums of a bead meet in a fixed butterfly
-        // and its first sub-lane stores the bead's pair force ----
-        if (pairs_on) {
-            for (int base = gwarp * 32; base < n * S; base += GT) {
-                const int u = base + lane;
-                const int i = u / S, sr = u & (S - 1);
-                float3 fi = make_float3(0.f, 0.f, 0.f);
-                if (i < n) {
-                    if (!use_scan) {
-                        const int k0 = S > 1 ? (int)sseg[u] : 0;
-                        const int k1 = sr == S - 1 ? (int)scnt[i] : (int)sseg[u + 1];
-                        fi = list_forces<TERMS, ENERGY>(i, k0, k1, cap_s, npad, slist, glist, sx, sp0, sp1,
-                                                        excl_all, pc, ea);
-                    } else {
-                        const int j0 = (sr * n) / S, j1 = sr == S - 1 ? n : ((sr + 1) * n) / S;
-                        fi = scan_forces<TERMS, LABELS, ENERGY>(i, j0, j1, nt, sx, sp0, sp1, slab, bc, bh,
-                                                                tcut2, ex_start, exl, excl_all, pc, ea);
-                    }
+        // ---- forces: warps claim work items from the group's counter,
+        // the bonded clusters first (the longest items), then the pair
+        // passes, longest first.  Pair pass p covers units u = 32 p + lane
+        // of the sorted beads: the S units of bead bord[u / S] are adjacent
+        // lanes (sub-lane u % S sums the list entries whose j lies in its
+        // j-range); their partial sums meet in a fixed butterfly and the
+        // first sub-lane stores the bead's pair force.  Every bead's sum is
+        // the same whichever warp and lanes compute it. ----
+        const int n_pass = pairs_on ? (n * S + 31) >> 5 : 0;
+        const int lg_s = __ffs(S) - 1;
+        while (true) {
+            int it = 0;
+            if (lane == 0) it = atomicAdd(s_item, 1);
+            it = __shfl_sync(kFull, it, 0);
+            if (it >= nt + n_pass) break;
+            if (it < nt) {
+                const float3 f = bonded_cluster<ENERGY>(B, it, n, lane, sx, sxl, ns, slots_en, carry, ea);
+                const int b = it * 32 + lane;
+                if (b < n) {
+                    fb[b] = f.x;
+                    fb[ns + b] = f.y;
+                    fb[2 * ns + b] = f.z;
                 }
-                for (int o = 1; o < S; o <<= 1) {
-                    fi.x += __shfl_xor_sync(kFull, fi.x, o);
-                    fi.y += __shfl_xor_sync(kFull, fi.y, o);
-                    fi.z += __shfl_xor_sync(kFull, fi.z, o);
-                }
-                if (i < n && sr == 0) {
-                    fp[i] = fi.x;
-                    fp[ns + i] = fi.y;
-                    fp[2 * ns + i] = fi.z;
+                continue;
+            }
+            const int u = ((it - nt) << 5) + lane;
+            const int sb = u >> lg_s, sr = u & (S - 1);
+            const int i = sb < n ? (int)bord[sb] : n;
+            float3 fi = make_float3(0.f, 0.f, 0.f);
+            if (i < n) {
+                if (!use_scan) {
+                    const int k0 = S > 1 ? (int)sseg[i * S + sr] : 0;
+                    const int k1 = sr == S - 1 ? (int)scnt[i] : (int)sseg[i * S + sr + 1];
+                    fi = list_forces<TERMS, ENERGY>(i, k0, k1, cap_s, npad, slist, glist, sx, sp0, sp1,
+                                                    excl_all, pc, ea);
+                } else {
+                    const int j0 = (sr * n) / S, j1 = sr == S - 1 ? n : ((sr + 1) * n) / S;
+                    fi = scan_forces<TERMS, LABELS, ENERGY>(i, j0, j1, nt, sx, sp0, sp1, slab, bc, bh,
+                                                            tcut2, ex_start, exl, excl_all, pc, ea);
                 }
             }
-        }
-        // ---- bonded: one warp per cluster of 32 chain positions,
-        // started from the far end of the warp range so warps that ran
-        // few pair units take the bonded work ----
-        for (int I = NWG - 1 - gwarp; I < nt; I += NWG) {
-            const float3 f = bonded_cluster<ENERGY>(B, I, n, lane, sx, sxl, ns, slots_en, carry, ea);
-            const int b = I * 32 + lane;
-            if (b < n) {
-                fb[b] = f.x;
-                fb[ns + b] = f.y;
-                fb[2 * ns + b] = f.z;
+            for (int o = 1; o < S; o <<= 1) {
+                fi.x += __shfl_xor_sync(kFull, fi.x, o);
+                fi.y += __shfl_xor_sync(kFull, fi.y, o);
+                fi.z += __shfl_xor_sync(kFull, fi.z, o);
+            }
+            if (i < n && sr == 0) {
+                fp[i] = fi.x;
+                fp[ns + i] = fi.y;
+                fp[2 * ns + i] = fi.z;
             }
         }
         bar_sync(bar, GT);
+        if (gtid == 0) *s_item = 0;  // read again only after the next barrier
         if (!INTEGRATE) break;
         // ---- Langevin update, bounding boxes, displacement and
         // blow-up checks; bead b = I * 32 + lane of cluster I = gwarp +
@@ -870,6 +929,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
     __shared__ int s_overflow[2];
     __shared__ int s_bad[2];
     __shared__ double s_energy[2][kNumSlots];
+    __shared__ int s_item[2];
     const int tid = threadIdx.x;
 
     // Whole-CTA phase: every claimed system runs on all THREADS threads
@@ -902,7 +962,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
             break;
         }
         run_system<THREADS, TERMS, LABELS, ENERGY, INTEGRATE>(a, q, slot, tid, 0, smem, a.smem_bytes, s_move[0],
-                                                              &s_overflow[0], &s_bad[0], s_energy[0]);
+                                                              &s_overflow[0], &s_bad[0], s_energy[0], &s_item[0]);
         __syncthreads();
     }
 
@@ -939,7 +999,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
             continue;
         }
         run_system<GT, TERMS, LABELS, ENERGY, INTEGRATE>(a, q, slot, gtid, 1 + g, gsmem, half, s_move[g],
-                                                         &s_overflow[g], &s_bad[g], s_energy[g]);
+                                                         &s_overflow[g], &s_bad[g], s_energy[g], &s_item[g]);
         bar_sync(1 + g, GT);
     }
 }
@@ -985,8 +1045,7 @@ void launch_persistent(Fn fn, int threads, BatchArgs a, int max_grid, size_t sme
         // a group's system must fit half of the share (state of its beads,
         // the cluster arrays for the largest system, the pair-split offsets)
         const size_t half = (share / 2) & ~(size_t)255;
-        const size_t fixed = (size_t)(32 + 36) * kMaxClusters + 16 + 2 * kMaxUnits;
-        const int fit = half > fixed ? (int)((half - fixed) / (size_t)a.split_bead_bytes) & ~31 : 0;
+        const int fit = half > kFixedBytes ? (int)((half - kFixedBytes) / (size_t)a.split_bead_bytes) & ~31 : 0;
         a.split_beads = std::min(a.split_beads, fit);
     }
     const int grid = std::max(1, std::min(max_grid, num_sms * per_sm));
@@ -1292,10 +1351,10 @@ BatchEngine::~BatchEngine() {
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
 }
 
-// Shared memory of the per-system state: 98 B per bead (118 with the
-// general pair terms), cluster boxes and carries, the pair-split offsets.
+// Shared memory of the per-system state: kBeadBytes per bead
+// (kBeadBytesGeneral with the general pair terms) and kFixedBytes.
 size_t BatchEngine::smem_bytes(int nmax, bool general) const {
-    return (size_t)nmax * (general ? 118 : 98) + (32 + 36) * (size_t)kMaxClusters + 16 + 2 * kMaxUnits;
+    return (size_t)nmax * (general ? kBeadBytesGeneral : kBeadBytes) + kFixedBytes;
 }
 
 int64_t BatchEngine::footprint(const SystemDesc& d) {
@@ -1546,7 +1605,7 @@ void BatchEngine::launch(bool integrate, bool energy, int k, const std::vector<i
     a.lists = lists_.p;
     a.slots_enabled = 0xffffffffu;
     a.split_beads = integrate ? split_beads_ : 0;
-    a.split_bead_bytes = general ? 118 : 98;
+    a.split_bead_bytes = general ? kBeadBytesGeneral : kBeadBytes;
     const int grid = (int)order.size();
     if (general)
         launch_batch_threads<15, true>(threads_, a, grid, smem, s, integrate, energy, num_sms_, want);

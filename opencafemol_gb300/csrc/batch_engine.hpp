@@ -152,7 +152,7 @@ class BatchEngine {
     DevBuf<BatchSys> sys_;
     DevBuf<int32_t> order_, order_k_, head_;
     bool balanced_ = false;
-    int split_beads_ = 384;   // CTA split at systems of at most this many beads (0: never)
+    int split_beads_ = 512;   // CTA split at systems of at most this many beads (0: never)
     DevBuf<double> energy_;
     DevBuf<float> forces_;
     // staging of the many-slot state copies (grown on demand)
