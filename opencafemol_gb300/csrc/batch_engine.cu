@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -1941,6 +1942,29 @@ static __device__ __align__(256) long long g_noalloc_dst[kNoAllocMaxSlots];
 static __device__ __align__(256) int g_noalloc_n[kNoAllocMaxSlots];
 }  // namespace
 
+// Segment table of a many-slot copy (each slot's bead offset in the state
+// arrays, its offset in the packed host buffer, its bead count), uploaded
+// only when it differs from the last one (a loop over the same slots reuses
+// it).  Called with the stream idle; the host vectors are staged before the
+// copies return.
+void BatchEngine::upload_segments(int64_t n, const std::vector<long long>& bead,
+                                  const std::vector<long long>& off, const std::vector<int>& cnt) {
+    if ((int64_t)seg_n_.n < n) {
+        seg_bead_.alloc(n);
+        seg_off_.alloc(n);
+        seg_n_.alloc(n);
+        seg_cnt_h_.clear();
+    }
+    if (seg_cnt_h_ == cnt && seg_off_h_ == off && seg_bead_h_ == bead) return;
+    // on the engine's stream, ahead of the kernel that reads the table
+    OCM_CK(cudaMemcpyAsync(seg_bead_.p, bead.data(), n * sizeof(long long), cudaMemcpyHostToDevice, stream_));
+    OCM_CK(cudaMemcpyAsync(seg_off_.p, off.data(), n * sizeof(long long), cudaMemcpyHostToDevice, stream_));
+    OCM_CK(cudaMemcpyAsync(seg_n_.p, cnt.data(), n * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    seg_bead_h_ = bead;
+    seg_off_h_ = off;
+    seg_cnt_h_ = cnt;
+}
+
 void BatchEngine::set_positions_many(int64_t n, const int64_t* slots, const double* xyz,
                                      const double* v) {
     OCM_CK(cudaSetDevice(device_));
@@ -1956,23 +1980,18 @@ void BatchEngine::set_positions_many(int64_t n, const int64_t* slots, const doub
         cnt[k] = (int)slots_[sl].n;
         total += slots_[sl].n;
     }
-    for (long long k = 0; k < 3 * total; ++k)
-        if (!std::isfinite(xyz[k])) throw Error(7, "[error] non-finite position");
+    // |x| <= DBL_MAX is false for infinities and NaN (branch-free scan)
+    bool finite = true;
+    for (long long k = 0; k < 3 * total; ++k) finite &= std::fabs(xyz[k]) <= DBL_MAX;
+    if (!finite) throw Error(7, "[error] non-finite position");
     OCM_CK(cudaStreamSynchronize(stream_));
-    if ((int64_t)seg_n_.n < n) {
-        seg_bead_.alloc(n);
-        seg_off_.alloc(n);
-        seg_n_.alloc(n);
-    }
+    upload_segments(n, bead, src, cnt);
     if ((int64_t)stage_.n < (v ? 6 : 3) * total) stage_.alloc((v ? 6 : 3) * total);
     DevBuf<long long>& db = seg_bead_;
     DevBuf<long long>& ds = seg_off_;
     DevBuf<int>& dn = seg_n_;
     DevBuf<double>& buf = stage_;
     cudaStream_t s = stream_;
-    OCM_CK(cudaMemcpyAsync(db.p, bead.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s));
-    OCM_CK(cudaMemcpyAsync(ds.p, src.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s));
-    OCM_CK(cudaMemcpyAsync(dn.p, cnt.data(), n * sizeof(int), cudaMemcpyHostToDevice, s));
     OCM_CK(cudaMemcpyAsync(buf.p, xyz, 3 * total * sizeof(double), cudaMemcpyHostToDevice, s));
     if (v) OCM_CK(cudaMemcpyAsync(buf.p + 3 * total, v, 3 * total * sizeof(double), cudaMemcpyHostToDevice, s));
     const dim3 grid(8, (unsigned)n);
@@ -1997,20 +2016,13 @@ void BatchEngine::get_positions_many(int64_t n, const int64_t* slots, double* xy
         total += slots_[sl].n;
     }
     OCM_CK(cudaStreamSynchronize(stream_));
-    if ((int64_t)seg_n_.n < n) {
-        seg_bead_.alloc(n);
-        seg_off_.alloc(n);
-        seg_n_.alloc(n);
-    }
+    upload_segments(n, bead, dst, cnt);
     if ((int64_t)stage_.n < 3 * total) stage_.alloc(3 * total);
     DevBuf<long long>& db = seg_bead_;
     DevBuf<long long>& dd = seg_off_;
     DevBuf<int>& dn = seg_n_;
     DevBuf<double>& buf = stage_;
     cudaStream_t s = stream_;
-    OCM_CK(cudaMemcpyAsync(db.p, bead.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s));
-    OCM_CK(cudaMemcpyAsync(dd.p, dst.data(), n * sizeof(long long), cudaMemcpyHostToDevice, s));
-    OCM_CK(cudaMemcpyAsync(dn.p, cnt.data(), n * sizeof(int), cudaMemcpyHostToDevice, s));
     const dim3 grid(8, (unsigned)n);
     k_gather_pos<<<grid, 128, 0, s>>>((int)n, db.p, dd.p, dn.p, x_.p, y_.p, z_.p, buf.p);
     OCM_CK(cudaGetLastError());

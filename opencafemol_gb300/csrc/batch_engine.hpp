@@ -158,6 +158,10 @@ class BatchEngine {
     // staging of the many-slot state copies (grown on demand)
     DevBuf<long long> seg_bead_, seg_off_;
     DevBuf<int> seg_n_;
+    std::vector<long long> seg_bead_h_, seg_off_h_;  // host copies of the segment table on the device
+    std::vector<int> seg_cnt_h_;
+    void upload_segments(int64_t n, const std::vector<long long>& bead, const std::vector<long long>& off,
+                         const std::vector<int>& cnt);
     DevBuf<double> stage_;
     std::vector<BatchSys> sys_host_;
 };

@@ -297,8 +297,8 @@ class Batch:
         check(lib.ocm_batch_set_balanced(self._h, int(bool(on))))
 
     # (threads per CTA, list shared memory KiB, split beads); -1 KiB = no cap
-    DEFAULT_TUNE_CANDIDATES = ((512, 96, 512), (512, 96, 768), (512, -1, 512), (1024, 96, 512),
-                               (1024, -1, 768), (512, 96, 0), (1024, 96, 0), (256, 96, 0))
+    DEFAULT_TUNE_CANDIDATES = ((512, 96, 512), (512, -1, 512), (512, 96, 384), (1024, 96, 512),
+                               (1024, -1, 512), (512, 96, 0), (1024, 96, 0), (256, 96, 384))
 
     def autotune(self, steps_per_trial: int = 50, candidates=DEFAULT_TUNE_CANDIDATES,
                  rounds: int = 2) -> dict:
