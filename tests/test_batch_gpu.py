@@ -218,3 +218,28 @@ def test_cta_split_keeps_results(gpu):
         runs.append(b.get_positions_many(slots))
     for r in runs[1:]:
         assert np.array_equal(r, runs[0])
+
+
+def test_positions_reset_mid_run(gpu):
+    """A batch whose positions are reset mid-run (far from where its lists
+    were built) continues exactly as a fresh batch resumed from that state
+    (same step counter, velocities)."""
+    from opencafemol_gb300 import synth
+    specs = _systems([90, 260, 540], seed0=970)
+    systems = [synth.build_system(s) for s in specs]
+    a = gpu.Batch(max_systems=3, max_total_beads=1024, max_beads_per_system=800)
+    slots = [a.admit(so, s.pos, seed=30 + k, n_steps=10 ** 6) for k, (so, s) in enumerate(zip(systems, specs))]
+    for _ in range(3):
+        a.run(20, sync=True)
+    v = [a.velocities(k) for k in slots]
+    # back to the starting structures (far from where the lists were built)
+    a.set_positions_many(slots, np.concatenate([s.pos for s in specs]))
+    a.run(25, sync=True)
+    a.run(25, sync=True)
+    b = gpu.Batch(max_systems=3, max_total_beads=1024, max_beads_per_system=800)
+    sb = [b.admit(so, s.pos, velocities=v[k], seed=30 + k, n_steps=10 ** 6, steps_done=60)
+          for k, (so, s) in enumerate(zip(systems, specs))]
+    b.run(50, sync=True)
+    for ka, kb in zip(slots, sb):
+        assert np.array_equal(a.positions(ka), b.positions(kb))
+        assert np.array_equal(a.velocities(ka), b.velocities(kb))
