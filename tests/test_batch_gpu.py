@@ -243,3 +243,47 @@ def test_positions_reset_mid_run(gpu):
     for ka, kb in zip(slots, sb):
         assert np.array_equal(a.positions(ka), b.positions(kb))
         assert np.array_equal(a.velocities(ka), b.velocities(kb))
+
+
+def _lj_protein(n, seed):
+    """A Go-model chain whose excluded volume is replaced by HPS-style
+    Lennard-Jones repulsion and attraction (per-bead sigma and lambda), with
+    its Debye-Hueckel charges: the general pair kernel."""
+    from opencafemol_gb300 import synth
+    s = synth.go_protein(n, seed)
+    rng = np.random.default_rng(seed)
+    sig = rng.uniform(0.3, 0.5, n)
+    lam = rng.uniform(0.0, 1.0, n)
+    ratio = 2.0 / (0.5 * (np.sort(sig)[-1] + np.sort(sig)[-2]))
+    s.exv = None
+    s.ljr = synth.PairTerm(ratio=ratio, p0=np.full(n, 0.2 * synth.KJ_PER_KCAL), p1=sig, ign_bond=3)
+    s.lja = synth.PairTerm(ratio=ratio, p0=0.2 * lam * synth.KJ_PER_KCAL, p1=sig, ign_bond=3)
+    return s
+
+
+def test_cta_split_general_pair_kernel(gpu):
+    """Small chains on the general pair kernel (Lennard-Jones terms): one
+    chain's forces against the oracle, and every trajectory identical with
+    and without the CTA split (more than two systems per CTA)."""
+    from opencafemol_gb300 import synth
+    from oracle import oracle
+    rng = np.random.default_rng(91)
+    lengths = [int(n) for n in rng.integers(30, 300, 320)]
+    specs = [_lj_protein(n, 4000 + k) for k, n in enumerate(lengths)]
+    systems = [synth.build_system(s) for s in specs]
+    one = gpu.Batch(max_systems=1, max_total_beads=512, max_beads_per_system=512)
+    slot = one.admit(systems[0], specs[0].pos, seed=1, n_steps=1)
+    f, _ = one.state(slot)
+    f_ref, _ = oracle.evaluate(specs[0])
+    assert rel_force_err(f, f_ref) <= 1e-4
+    runs = []
+    for threads, split in ((512, 0), (512, 384), (1024, 512)):
+        b = gpu.Batch(max_systems=len(specs), max_total_beads=sum(lengths) + 64, max_beads_per_system=512)
+        slots = [b.admit(so, s.pos, seed=50 + k, n_steps=10 ** 6) for k, (so, s) in enumerate(zip(systems, specs))]
+        b.set_threads(threads)
+        b.set_split(split)
+        b.run(30, sync=True)
+        b.run(30, sync=True)
+        runs.append(b.get_positions_many(slots))
+    for r in runs[1:]:
+        assert np.array_equal(r, runs[0])
