@@ -273,7 +273,7 @@ def run_ours(args, rank, world):
     # ---- end to end through the public API with host buffers ----
     shape = ((tuned["threads"], tuned["list_smem_kib"], tuned["split_beads"]) if tuned
              else (args.threads, args.list_smem, args.split))
-    e2e = run_e2e(ocm, synth, specs, systems, args, world, shape)
+    e2e = run_e2e(batch, slots, beads, args, world)
 
     # ---- plain single-system path on a sample of the same mix ----
     plain = run_plain(ocm, specs, systems, args) if args.plain_sample > 0 else None
@@ -315,27 +315,19 @@ def run_ours(args, rank, world):
     return line
 
 
-def run_e2e(ocm, synth, specs, systems, args, world, shape):
+def run_e2e(batch, slots, beads, args, world):
     """End to end through the public API with host buffers, as a host-driven
-    loop runs it: every step uploads every replica's positions from pinned
-    host memory (one copy; the positions read back by the step before, so the
-    trajectory continues, velocities stay on the device), runs K MD steps and
-    reads every replica's positions back (one copy).  ``shape`` = (threads,
-    list KiB, split beads) of the device-timed leg."""
+    loop runs it, on the batch of the device-timed leg (its trajectories
+    continue): every step uploads every replica's positions from pinned host
+    memory (one copy; the positions read back by the step before;
+    velocities stay on the device), runs K MD steps and reads every
+    replica's positions back (one copy)."""
     import torch
     K = args.md_steps
-    beads = int(sum(s.n for s in specs))
-    batch = ocm.Batch(max_systems=len(specs), max_total_beads=beads + 1024,
-                      max_beads_per_system=SIZE_HI, device=local_device())
-    batch.set_threads(shape[0])
-    batch.set_list_smem(shape[1])
-    batch.set_split(shape[2])
-    slots = [batch.admit(sysobj, s.pos, temperature=s.temperature, step_size=s.dt,
-                         seed=17 + k, n_steps=10 ** 12)
-             for k, (sysobj, s) in enumerate(zip(systems, specs))]
-    host = torch.from_numpy(np.concatenate([s.pos for s in specs])).pin_memory()
+    host = torch.zeros((beads, 3), dtype=torch.float64).pin_memory()
     buf = host.numpy()
-    for _ in range(args.warmup):
+    batch.get_positions_many(slots, buf)
+    for _ in range(2):
         batch.set_positions_many(slots, buf)
         batch.run(K, sync=True)
         batch.get_positions_many(slots, buf)
@@ -350,7 +342,7 @@ def run_e2e(ocm, synth, specs, systems, args, world, shape):
     return {"value": dist_sum(float(beads), world) * K * args.steps / t, "unit": "bead-steps/s",
             "h2d_bytes_per_step": int(buf.nbytes), "d2h_bytes_per_step": int(buf.nbytes),
             "what": "positions H2D (pinned; the previous step's read-back) -> K MD steps -> positions D2H, "
-                    "per step"}
+                    "per step, continuing the device-timed batch"}
 
 
 def run_serving(ocm, args):

@@ -29,6 +29,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "batch_engine.hpp"
@@ -1025,16 +1026,36 @@ template <typename Fn>
 // for (state + bonded records + the list budget), 0 = all that fits.
 void launch_persistent(Fn fn, int threads, BatchArgs a, int max_grid, size_t smem,
                        cudaStream_t s, int num_sms, size_t want) {
-    int optin = 0, per_sm_smem = 0, dev = 0;
+    // The kernel's shared-memory opt-in and its occupancy at this smem
+    // size, looked up once per (kernel, device, size): the runtime queries
+    // cost tens of microseconds per launch otherwise.
+    struct Shape {
+        int max_dyn, per_sm_smem, per_sm;
+    };
+    static std::mutex mu;
+    static std::map<std::tuple<const void*, int, size_t, int>, Shape> cache;
+    int dev = 0;
     OCM_CK(cudaGetDevice(&dev));
-    OCM_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    OCM_CK(cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
-    cudaFuncAttributes fa{};
-    OCM_CK(cudaFuncGetAttributes(&fa, fn));
-    const int max_dyn = optin - (int)fa.sharedSizeBytes;
-    OCM_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn));
-    int per_sm = 0;
-    OCM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    Shape sh{};
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        const auto key = std::make_tuple(reinterpret_cast<const void*>(fn), dev, smem, threads);
+        auto it = cache.find(key);
+        if (it == cache.end()) {
+            int optin = 0;
+            OCM_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+            OCM_CK(cudaDeviceGetAttribute(&sh.per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+            cudaFuncAttributes fa{};
+            OCM_CK(cudaFuncGetAttributes(&fa, fn));
+            sh.max_dyn = optin - (int)fa.sharedSizeBytes;
+            OCM_CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.max_dyn));
+            OCM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh.per_sm, fn, threads, smem));
+            it = cache.emplace(key, sh).first;
+        }
+        sh = it->second;
+    }
+    const int max_dyn = sh.max_dyn, per_sm_smem = sh.per_sm_smem;
+    const int per_sm = sh.per_sm;
     if (per_sm < 1) throw Error(6, "[error] batched kernel does not fit on an SM");
     size_t share = (size_t)per_sm_smem / per_sm;
     share = share > 2048 ? share - 2048 : share;  // static + reserved per block
@@ -1330,6 +1351,8 @@ BatchEngine::BatchEngine(int device, int64_t max_systems, int64_t max_beads, int
     std::memset(h_overflow_, 0, sizeof(int) * max_systems);
     OCM_CK(cudaMallocHost(&h_status_, sizeof(int) * max_systems));
     std::memset(h_status_, 0, sizeof(int) * max_systems);
+    OCM_CK(cudaMallocHost(&h_check_, sizeof(int)));
+    check_.alloc(1);
     sys_.alloc(max_systems);
     OCM_CK(cudaMemset(sys_.p, 0, sizeof(BatchSys) * max_systems));
     order_.alloc(max_systems);
@@ -1348,6 +1371,7 @@ BatchEngine::~BatchEngine() {
     if (ev_copy_) cudaEventDestroy(ev_copy_);
     if (h_overflow_) cudaFreeHost(h_overflow_);
     if (h_status_) cudaFreeHost(h_status_);
+    if (h_check_) cudaFreeHost(h_check_);
     if (stream_) cudaStreamDestroy(stream_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
 }
@@ -1893,12 +1917,24 @@ void BatchEngine::slot_stats(int64_t slot, int32_t* builds, int32_t* capacity) {
 // Scatter / gather of many slots' states through one pinned staging buffer
 // and one kernel, so a whole ensemble moves host<->device in two copies.
 namespace {
+// Sets *bad when any of the m values is not finite (|v| <= DBL_MAX is
+// false for infinities and NaN).
+__global__ void k_check_finite(long long m, const double* __restrict__ v, int* bad) {
+    bool ok = true;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x)
+        ok = ok && fabs(v[k]) <= DBL_MAX;
+    if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) *bad = 1;
+}
+
+// Positions (and velocities) of many slots from the packed staging buffer;
+// writes nothing when the check above found a non-finite position.
 __global__ void k_scatter_state(int nseg, const long long* __restrict__ seg_bead,
                                 const long long* __restrict__ seg_src, const int* __restrict__ seg_n,
                                 const double* __restrict__ src, int with_v, double* x, double* y,
-                                double* z, float* vx, float* vy, float* vz, long long total) {
+                                double* z, float* vx, float* vy, float* vz, long long total,
+                                const int* __restrict__ bad) {
     const int g = blockIdx.y;
-    if (g >= nseg) return;
+    if (g >= nseg || *bad) return;
     const int n = seg_n[g];
     const long long b0 = seg_bead[g], s0 = seg_src[g];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -1945,8 +1981,9 @@ static __device__ __align__(256) int g_noalloc_n[kNoAllocMaxSlots];
 // Segment table of a many-slot copy (each slot's bead offset in the state
 // arrays, its offset in the packed host buffer, its bead count), uploaded
 // only when it differs from the last one (a loop over the same slots reuses
-// it).  Called with the stream idle; the host vectors are staged before the
-// copies return.
+// it).  The copies are ordered on the engine's stream after any kernel that
+// still reads the old table; the host vectors are staged before they
+// return.
 void BatchEngine::upload_segments(int64_t n, const std::vector<long long>& bead,
                                   const std::vector<long long>& off, const std::vector<int>& cnt) {
     if ((int64_t)seg_n_.n < n) {
@@ -1980,11 +2017,8 @@ void BatchEngine::set_positions_many(int64_t n, const int64_t* slots, const doub
         cnt[k] = (int)slots_[sl].n;
         total += slots_[sl].n;
     }
-    // |x| <= DBL_MAX is false for infinities and NaN (branch-free scan)
-    bool finite = true;
-    for (long long k = 0; k < 3 * total; ++k) finite &= std::fabs(xyz[k]) <= DBL_MAX;
-    if (!finite) throw Error(7, "[error] non-finite position");
-    OCM_CK(cudaStreamSynchronize(stream_));
+    // every step below is ordered on the engine's stream; the positions are
+    // checked on the device and written only when all are finite
     upload_segments(n, bead, src, cnt);
     if ((int64_t)stage_.n < (v ? 6 : 3) * total) stage_.alloc((v ? 6 : 3) * total);
     DevBuf<long long>& db = seg_bead_;
@@ -1994,11 +2028,16 @@ void BatchEngine::set_positions_many(int64_t n, const int64_t* slots, const doub
     cudaStream_t s = stream_;
     OCM_CK(cudaMemcpyAsync(buf.p, xyz, 3 * total * sizeof(double), cudaMemcpyHostToDevice, s));
     if (v) OCM_CK(cudaMemcpyAsync(buf.p + 3 * total, v, 3 * total * sizeof(double), cudaMemcpyHostToDevice, s));
+    OCM_CK(cudaMemsetAsync(check_.p, 0, sizeof(int), s));
+    k_check_finite<<<(unsigned)std::min<long long>(4 * num_sms_, (3 * total + 255) / 256), 256, 0, s>>>(
+        3 * total, buf.p, check_.p);
     const dim3 grid(8, (unsigned)n);
     k_scatter_state<<<grid, 128, 0, s>>>((int)n, db.p, ds.p, dn.p, buf.p, v ? 1 : 0, x_.p, y_.p, z_.p,
-                                         vx_.p, vy_.p, vz_.p, total);
+                                         vx_.p, vy_.p, vz_.p, total, check_.p);
     OCM_CK(cudaGetLastError());
+    OCM_CK(cudaMemcpyAsync(h_check_, check_.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     OCM_CK(cudaStreamSynchronize(s));
+    if (*h_check_) throw Error(7, "[error] non-finite position");
 }
 
 void BatchEngine::get_positions_many(int64_t n, const int64_t* slots, double* xyz) {
@@ -2015,7 +2054,6 @@ void BatchEngine::get_positions_many(int64_t n, const int64_t* slots, double* xy
         cnt[k] = (int)slots_[sl].n;
         total += slots_[sl].n;
     }
-    OCM_CK(cudaStreamSynchronize(stream_));
     upload_segments(n, bead, dst, cnt);
     if ((int64_t)stage_.n < 3 * total) stage_.alloc(3 * total);
     DevBuf<long long>& db = seg_bead_;

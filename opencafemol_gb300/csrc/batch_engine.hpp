@@ -149,6 +149,8 @@ class BatchEngine {
     DevBuf<uint16_t> lists_;
     int* h_overflow_ = nullptr;  // pinned copy of the records' overflow flags
     int* h_status_ = nullptr;    // pinned copy of the records' status words
+    int* h_check_ = nullptr;     // pinned: non-finite values found by the upload check
+    DevBuf<int> check_;          // the device side of that flag
     DevBuf<BatchSys> sys_;
     DevBuf<int32_t> order_, order_k_, head_;
     bool balanced_ = false;

@@ -287,3 +287,22 @@ def test_cta_split_general_pair_kernel(gpu):
         runs.append(b.get_positions_many(slots))
     for r in runs[1:]:
         assert np.array_equal(r, runs[0])
+
+
+def test_many_slot_upload_rejects_non_finite(gpu):
+    """A non-finite position in a many-slot upload is refused with
+    OCM_ERR_NONFINITE and changes no slot's state."""
+    from opencafemol_gb300 import synth
+    specs = _systems([40, 130], seed0=990)
+    b = gpu.Batch(max_systems=2, max_total_beads=256, max_beads_per_system=200)
+    slots = [b.admit(synth.build_system(s), s.pos, n_steps=10) for s in specs]
+    before = b.get_positions_many(slots)
+    for bad in (np.nan, np.inf, -np.inf):
+        xyz = before + 0.5
+        xyz[150, 1] = bad
+        with pytest.raises(gpu.OCMError) as ei:
+            b.set_positions_many(slots, xyz, np.zeros_like(xyz))
+        assert ei.value.code == 7
+        assert np.array_equal(b.get_positions_many(slots), before)
+    b.set_positions_many(slots, before + 0.5)
+    assert np.array_equal(b.get_positions_many(slots), before + 0.5)
