@@ -162,6 +162,14 @@ class Batch:
         self._h = h
         self._n: dict[int, int] = {}
         self._systems: dict[int, System] = {}
+        self._sizes = np.zeros(int(max_systems), np.int64)  # beads per slot (0: free)
+
+    def _total(self, sl: np.ndarray) -> int:
+        """Beads of the slots in ``sl`` (out-of-range slots count 0: the C
+        call refuses them)."""
+        if sl.size == 0 or sl.min() < 0 or sl.max() >= self._sizes.size:
+            return 0
+        return int(self._sizes[sl].sum())
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -195,6 +203,7 @@ class Batch:
                                       float(friction), float(step_size), int(seed), int(n_steps),
                                       C.byref(slot)))
         self._n[slot.value] = system.n
+        self._sizes[slot.value] = system.n
         self._systems[slot.value] = system
         return slot.value
 
@@ -230,6 +239,9 @@ class Batch:
         sl = np.ascontiguousarray(slots, np.int64)
         x = as_f64(xyz)
         v = None if velocities is None else as_f64(velocities)
+        total = self._total(sl)
+        if x.size != 3 * total or (v is not None and v.size != 3 * total):
+            raise ValueError(f"positions (and velocities) must hold {total} x 3 values for these slots")
         check(lib.ocm_batch_set_positions_many(self._h, len(sl), i64ptr(sl), dptr(x), dptr(v)))
 
     @staticmethod
@@ -245,7 +257,7 @@ class Batch:
 
     def get_positions_many(self, slots, out=None) -> np.ndarray:
         sl = np.ascontiguousarray(slots, np.int64)
-        total = sum(self._n[int(k)] for k in sl)
+        total = self._total(sl)
         out = self._out_buffer(out, total)
         check(lib.ocm_batch_get_positions_many(self._h, len(sl), i64ptr(sl), dptr(out)))
         return out
@@ -254,7 +266,7 @@ class Batch:
         """``get_positions_many`` through fixed per-device scratch (no device
         allocation; at most 131072 beads and 2048 slots per call)."""
         sl = np.ascontiguousarray(slots, np.int64)
-        total = sum(self._n[int(k)] for k in sl)
+        total = self._total(sl)
         out = self._out_buffer(out, total)
         check(lib.ocm_batch_get_positions_many_noalloc(self._h, len(sl), i64ptr(sl), dptr(out)))
         return out
@@ -273,6 +285,7 @@ class Batch:
     def retire(self, slot: int) -> None:
         check(lib.ocm_batch_retire(self._h, int(slot)))
         self._n.pop(slot, None)
+        self._sizes[slot] = 0
         self._systems.pop(slot, None)
 
     def active(self) -> tuple[int, int]:

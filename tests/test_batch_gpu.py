@@ -306,3 +306,5 @@ def test_many_slot_upload_rejects_non_finite(gpu):
         assert np.array_equal(b.get_positions_many(slots), before)
     b.set_positions_many(slots, before + 0.5)
     assert np.array_equal(b.get_positions_many(slots), before + 0.5)
+    with pytest.raises(ValueError):  # fewer values than the slots' beads
+        b.set_positions_many(slots, before[:-1])
