@@ -393,7 +393,10 @@ int ocm_batch_get_positions(ocm_batch* batch, int64_t slot, double* xyz);
 int ocm_batch_get_velocities(ocm_batch* batch, int64_t slot, double* v);
 /* Replace the positions (and, if v is not NULL, velocities) of n slots in
  * one host->device copy; xyz (and v) hold the slots' beads back to back in
- * the order of `slots`. */
+ * the order of `slots` (3 x the slots' total beads values each).  The
+ * positions are checked on the device: a non-finite one returns
+ * OCM_ERR_NONFINITE and no slot changes.  Returns after the copy, so the
+ * host buffers may be reused at once. */
 int ocm_batch_set_positions_many(ocm_batch* batch, int64_t n, const int64_t* slots,
                                  const double* xyz, const double* v);
 /* Read the positions of n slots, back to back in the order of `slots`, in
