@@ -755,8 +755,9 @@ __device__ __forceinline__ void run_system(const BatchArgs& a, int q, int slot, 
         }
         const unsigned long long step = step0 + (unsigned long long)st;
         // ---- forces: warps claim work items from the group's counter,
-        // the bonded clusters first (the longest items), then the pair
-        // passes, longest first.  Pair pass p covers units u = 32 p + lane
+        // the bonded clusters first, then the pair passes, longest first
+        // (claiming the longest passes before the bonded clusters measured
+        // slower).  Pair pass p covers units u = 32 p + lane
         // of the sorted beads: the S units of bead bord[u / S] are adjacent
         // lanes (sub-lane u % S sums the list entries whose j lies in its
         // j-range); their partial sums meet in a fixed butterfly and the
@@ -935,11 +936,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_batch(BatchArgs a) {
     const int tid = threadIdx.x;
 
     // Whole-CTA phase: every claimed system runs on all THREADS threads
-    // (barrier 0).  When the CTA claims a system small enough for half of its
-    // shared memory, and the launch has at least two systems per CTA, it
-    // leaves this loop with that system: claims come largest first, so every
-    // later system is small too.  Every thread takes the same branch, right
-    // after a CTA-wide barrier.
+    // (barrier 0).  When the CTA claims a system of at most split_beads
+    // beads (capped on the host so that it fits half of the shared memory),
+    // and the launch has at least two systems per CTA, it leaves this loop
+    // with that system: claims come largest first, so every later system is
+    // small too.  Every thread takes the same branch, right after a CTA-wide
+    // barrier.
     int split_q = -1;
     while (true) {
         if (tid == 0) {
