@@ -89,8 +89,12 @@ class Server:
 
     def __init__(self, max_systems: int, max_total_beads: int, max_beads_per_system: int,
                  chunk_steps: int = 200, device: int = 0, keep_results: bool = False,
-                 hbm_budget_bytes: int | None = None, balanced: bool = True):
-        self.batch = Batch(max_systems, max_total_beads, max_beads_per_system, device=device)
+                 hbm_budget_bytes: int | None = None, balanced: bool = True, batch=None):
+        """``batch``: an existing object with Batch's admit / run / finished /
+        status / positions / steps_done / retire / footprint calls to serve
+        through (default: a new Batch of the given capacity)."""
+        self.batch = batch if batch is not None else Batch(max_systems, max_total_beads, max_beads_per_system,
+                                                           device=device)
         self.batch.set_balanced(balanced)
         self.chunk_steps = chunk_steps
         self.max_systems = max_systems
@@ -125,7 +129,7 @@ class Server:
             while waiting and len(resident) < self.max_systems:
                 r = waiting[0]
                 if r.footprint < 0:
-                    r.footprint = Batch.footprint(r.system)
+                    r.footprint = self.batch.footprint(r.system)
                 need = r.footprint
                 if self.hbm_budget_bytes is not None and resident_bytes + need > self.hbm_budget_bytes:
                     if not resident:
