@@ -322,8 +322,9 @@ class Batch:
         In each of ``rounds`` rounds every candidate runs two real launches
         of ``steps_per_trial`` steps (the first absorbs the set-up of that
         shape); the second is timed with CUDA events.  The rounds interleave
-        the candidates, so a drift of the systems' cost while they relax
-        does not favour the candidates timed last; the shape with the
+        the candidates, so a transient of the systems' cost while they relax
+        spreads over every candidate instead of falling on the first ones
+        (warm up before tuning, as the benchmark does); the shape with the
         smallest mean time is kept.  Trajectories do not depend on the
         shape, so the trials are ordinary simulation progress: the resident
         systems advance by 2 * rounds * steps_per_trial steps per candidate
