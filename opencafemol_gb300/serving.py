@@ -15,7 +15,8 @@ Launches are balanced: the largest resident system advances
 one large request does not hold every small one to its pace (each
 trajectory is independent of how its steps are split into launches).  A
 system that blows up is retired as failed and its request completes with
-``failed = True``.
+``failed = True``.  A request whose ``cancelled`` flag the client sets
+leaves the queue, or its slot, at the next pass of the loop.
 """
 from __future__ import annotations
 
@@ -47,6 +48,10 @@ class Request:
     result: np.ndarray | None = None
     failed: bool = False
     footprint: int = -1     # device bytes in a batch (computed at the first admission attempt)
+    # set by the client (any thread) to withdraw the request: a waiting one
+    # is dropped, a resident one retired at the next pass of the loop; it
+    # completes with the steps it did and no result
+    cancelled: bool = False
 
     @property
     def beads(self) -> int:
@@ -69,6 +74,7 @@ class ServeStats:
     peak_resident_bytes: int = 0
     waits_for_memory: int = 0   # admission attempts deferred by the budget
     failed: int = 0
+    cancelled: int = 0
 
     def summary(self) -> dict:
         lat = np.array(self.latencies_s)
@@ -78,7 +84,8 @@ class ServeStats:
                 "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
                 "chunks": self.chunks, "max_resident": self.max_resident,
                 "hbm_budget_bytes": self.hbm_budget_bytes, "peak_resident_bytes": self.peak_resident_bytes,
-                "waits_for_memory": self.waits_for_memory, "failed": self.failed}
+                "waits_for_memory": self.waits_for_memory, "failed": self.failed,
+                "cancelled": self.cancelled}
 
 
 class Server:
@@ -119,6 +126,21 @@ class Server:
             while nxt < len(queue) and queue[nxt].arrival <= now:
                 waiting.append(queue[nxt])
                 nxt += 1
+            # withdrawn requests: waiting ones leave the queue, resident ones
+            # their slots
+            for r in [r for r in waiting if r.cancelled]:
+                waiting.remove(r)
+                self._complete(r, t0, realtime, stats, steps=0)
+                done += 1
+            for slot in [k for k, r in resident.items() if r.cancelled]:
+                r = resident.pop(slot)
+                steps = self.batch.steps_done(slot)
+                self.batch.retire(slot)
+                resident_bytes -= footprint.pop(slot)
+                self._complete(r, t0, realtime, stats, steps=steps)
+                done += 1
+            if done == len(queue):
+                break
             ran = False
             if resident:
                 # launch the chunk first: the admissions below (host-side
@@ -160,19 +182,24 @@ class Server:
                 if slot not in resident:
                     continue
                 r = resident.pop(slot)
-                r.finished_at = time.perf_counter() - t0
                 r.failed = self.batch.status(slot) != 0
                 if self.keep_results:
                     r.result = self.batch.positions(slot)
                 steps = self.batch.steps_done(slot)
                 self.batch.retire(slot)
                 resident_bytes -= footprint.pop(slot)
-                stats.latencies_s.append(r.latency if realtime else r.finished_at)
-                stats.bead_steps += r.beads * steps
-                stats.failed += int(r.failed)
+                self._complete(r, t0, realtime, stats, steps=steps)
                 done += 1
         stats.wall_s = time.perf_counter() - t0
         return stats
+
+    @staticmethod
+    def _complete(r: Request, t0: float, realtime: bool, stats: ServeStats, steps: int) -> None:
+        r.finished_at = time.perf_counter() - t0
+        stats.latencies_s.append(r.latency if realtime else r.finished_at)
+        stats.bead_steps += r.beads * steps
+        stats.failed += int(r.failed)
+        stats.cancelled += int(r.cancelled)
 
 
 def poisson_arrivals(n: int, rate_per_s: float, seed: int) -> np.ndarray:

@@ -1,6 +1,6 @@
 """The continuous-batching loop's host logic with a stand-in batch (no GPU):
 admission against slot, bead and device-memory limits, waits for
-retirements, completion records, failed requests."""
+retirements, completion records, failed and cancelled requests."""
 import numpy as np
 import pytest
 
@@ -123,3 +123,27 @@ def test_capacity_waits_then_admits_after_retirement():
     st = server.serve(_requests([800, 700, 600], [100, 100, 100]), realtime=False)
     assert len(st.latencies_s) == 3 and st.max_resident == 1
     assert fake.launches >= 3
+
+
+def test_cancelled_requests_leave_queue_and_slot():
+    """A resident request cancelled by its client gives up its slot at the
+    next pass (completing with the steps it did, no result); a waiting one
+    never gets admitted; the others complete."""
+    reqs = _requests([100, 200, 300, 400], [1000, 1000, 1000, 1000])
+
+    class _Client(_FakeBatch):
+        def run(self, k, sync=False):
+            super().run(k, sync)
+            if self.launches == 2:
+                reqs[0].cancelled = True  # resident by now
+                reqs[3].cancelled = True  # still waiting (capacity two)
+
+    fake = _Client(max_systems=2, max_beads=10 ** 6)
+    server = serving.Server(2, 10 ** 6, 800, chunk_steps=100, keep_results=True, batch=fake)
+    st = server.serve(reqs, realtime=False)
+    assert st.cancelled == 2 and len(st.latencies_s) == 4 and st.failed == 0
+    assert reqs[0].result is None and reqs[3].result is None
+    assert reqs[1].result is not None and reqs[2].result is not None
+    # request 0 ran two launches; request 3 never ran
+    assert st.bead_steps == 100 * 200 + 200 * 1000 + 300 * 1000
+    assert not fake.slots
