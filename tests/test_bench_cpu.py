@@ -37,3 +37,15 @@ def test_reference_arm_line():
     # the whole 512-replica workload, and the engine library never mapped
     assert line["config"]["replicas"] == 512 and line["config"]["md_steps_per_step"] == 2
     assert line["engine_library_loaded"] is False
+
+
+def test_clock_records_that_force_a_remeasure():
+    import bench
+    ok = {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": []}
+    assert not bench.clocks_rejected(ok)
+    assert not bench.clocks_rejected(dict(ok, sm_mhz=1800.0, reasons=["sw_power_cap"]))  # kept, noted
+    for r in ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown"):
+        assert bench.clocks_rejected(dict(ok, reasons=[r]))
+    assert bench.clocks_rejected(dict(ok, sm_mhz=1400.0))  # well below max, no reason: a clock lock
+    assert not bench.clocks_rejected(dict(ok, sm_mhz=1950.0))
+    assert not bench.clocks_rejected({"reasons": [], "samples": 0})  # no samples: nothing to judge
